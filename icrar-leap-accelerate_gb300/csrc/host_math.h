@@ -1,0 +1,21 @@
+// Host-side FP64 set-up maths shared by the C ABI and the C++ calibrator.
+#pragma once
+
+#include <cstdint>
+#include <string>
+#include <vector>
+
+namespace leapgb {
+
+// MetaData::GenerateDDMatrix (LA/model/cpu/MetaData.cc:166-203); dd is 3x3 row-major.
+void dd_matrix(double phase_ra, double phase_dec, double ra, double dec, double* dd);
+
+// PhaseMatrixFunction (LA/algorithm/cpu/PhaseMatrixFunction.cc:35-93).  ref_ant < 0 = none.
+// A is returned column-major (rows x cols).  Returns a LEAP_* status.
+int phase_matrix(const int32_t* a1, const int32_t* a2, const uint8_t* fg, int32_t n, int32_t ref_ant,
+                 std::vector<double>& A, std::vector<int32_t>& I, int32_t& rows, int32_t& cols, std::string& err);
+
+// SVDPseudoInverse (LA/math/cpu/matrix_invert.h:49-56): A (m x n, column-major) -> Ad (n x m, column-major).
+int pseudo_inverse(const double* A, int32_t m, int32_t n, double* Ad, std::string& err);
+
+}  // namespace leapgb

@@ -1,0 +1,570 @@
+// C ABI of the GB300 LEAP calibration hot path: context, resident buffers,
+// launch configuration.  See include/leap_gb300.h for the contract of each
+// entry point and the reference interface it replaces.
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <map>
+#include <memory>
+#include <string>
+#include <vector>
+
+#include "leap_gb300.h"
+#include "host_math.h"
+#include "kernels_rotate.cuh"
+#include "kernels_solve.cuh"
+
+using namespace leapgb;
+
+namespace {
+
+thread_local std::string g_last_error;
+
+// Grow-only device buffer: steady-state calls reuse it and never allocate.
+struct DeviceBuffer {
+  void* ptr = nullptr;
+  size_t bytes = 0;
+  cudaError_t ensure(size_t need) {
+    if (need <= bytes) return cudaSuccess;
+    if (ptr) cudaFree(ptr);
+    ptr = nullptr;
+    bytes = 0;
+    cudaError_t e = cudaMalloc(&ptr, need);
+    if (e == cudaSuccess) bytes = need;
+    return e;
+  }
+  void release() {
+    if (ptr) cudaFree(ptr);
+    ptr = nullptr;
+    bytes = 0;
+  }
+  template <typename T> T* as() const { return static_cast<T*>(ptr); }
+};
+
+struct Integration {
+  DeviceBuffer vis, uvw;
+  int32_t vis_type = LEAP_VIS_C64;
+  int64_t rows = 0;
+  int32_t channels = 0, pols = 0;
+};
+
+struct Metadata {
+  bool set = false;
+  leap_constants k{};
+  int32_t S = 0, Arows = 0, A1rows = 0, Kpad = 0;
+  DeviceBuffer I1, Ad1, Ad, Ad_f32, arow, arow_val;
+};
+
+}  // namespace
+
+struct leap_ctx {
+  int device = 0;
+  cudaStream_t stream = nullptr;
+  std::string err;
+  Metadata md;
+  std::map<int32_t, Integration> integ;
+  // scratch, shared by calls on this context
+  DeviceBuffer partial, avg, cal1, dphi, gemm_partial, dd, cal, dev_err, lambda;
+  int last_ndir = 0, last_pols = 0, last_nbl = 0;
+  std::vector<double> lambda_host;
+  double lambda_f0 = 0.0, lambda_df = 0.0;
+  // Ring of (start, after rotate, end) events, one triple per recorded call.
+  static constexpr int kRing = 256;
+  cudaEvent_t ring[kRing][3] = {};
+  int ring_count = 0;
+  int kernels_last = 0;
+};
+
+namespace {
+
+int fail(leap_ctx* ctx, int code, const std::string& msg) {
+  if (ctx) ctx->err = msg;
+  g_last_error = msg;
+  return code;
+}
+
+int cuda_fail(leap_ctx* ctx, cudaError_t e, const char* what) {
+  return fail(ctx, e == cudaErrorMemoryAllocation ? LEAP_ERR_OUT_OF_MEMORY : LEAP_ERR_CUDA,
+              std::string(what) + ": " + cudaGetErrorString(e));
+}
+
+#define LEAP_CUDA(call, what)                         \
+  do {                                                \
+    cudaError_t e_ = (call);                          \
+    if (e_ != cudaSuccess) return cuda_fail(ctx, e_, what); \
+  } while (0)
+
+struct DeviceGuard {
+  int prev = -1;
+  explicit DeviceGuard(int dev) {
+    cudaGetDevice(&prev);
+    if (prev != dev) cudaSetDevice(dev);
+  }
+  ~DeviceGuard() {
+    int cur = -1;
+    cudaGetDevice(&cur);
+    if (prev >= 0 && cur != prev) cudaSetDevice(prev);
+  }
+};
+
+int grid_1d(int64_t n, int threads) {
+  int64_t b = (n + threads - 1) / threads;
+  return static_cast<int>(std::min<int64_t>(std::max<int64_t>(b, 1), 152 * 32));
+}
+
+// Slab split of (timestep, channel) space so the grid covers the GPU.
+void choose_slabs(int timesteps, int channels, int64_t base_blocks, int& t_per, int& c_per, int& nts, int& ncs) {
+  const int64_t target = 152 * 8;
+  int64_t want = std::max<int64_t>(1, (target + base_blocks - 1) / base_blocks);
+  // Keep at least 64 (timestep, channel) pairs per slab.
+  const int64_t max_slabs = std::max<int64_t>(1, (static_cast<int64_t>(timesteps) * channels) / 64);
+  want = std::min(want, max_slabs);
+  nts = static_cast<int>(std::min<int64_t>(want, timesteps));
+  t_per = (timesteps + nts - 1) / nts;
+  nts = (timesteps + t_per - 1) / t_per;
+  int64_t rest = (want + nts - 1) / nts;
+  ncs = static_cast<int>(std::min<int64_t>(rest, std::max(1, channels / 16)));
+  c_per = (channels + ncs - 1) / ncs;
+  ncs = (channels + c_per - 1) / c_per;
+}
+
+template <typename VisT, int P>
+void launch_rotate(const RotateArgs& a, dim3 grid, int precision, cudaStream_t s) {
+  if (precision == LEAP_PRECISION_FP64) {
+    rotate_average_fp64<VisT, P, 2><<<grid, 128, 0, s>>>(a);
+  } else {
+    rotate_average_mixed<VisT, P, 4><<<grid, 128, 0, s>>>(a);
+  }
+}
+
+template <typename VisT>
+int dispatch_pols(const RotateArgs& a, dim3 grid, int precision, cudaStream_t s) {
+  switch (a.pols) {
+    case 1: launch_rotate<VisT, 1>(a, grid, precision, s); return 0;
+    case 2: launch_rotate<VisT, 2>(a, grid, precision, s); return 0;
+    case 4: launch_rotate<VisT, 4>(a, grid, precision, s); return 0;
+    default: return -1;
+  }
+}
+
+int calibrate_impl(leap_ctx* ctx, int32_t slot, const double* d_dd, int32_t ndir, int32_t precision,
+                   double* d_cal, cudaStream_t s) {
+  if (!ctx->md.set) return fail(ctx, LEAP_ERR_NOT_READY, "metadata not set");
+  auto it = ctx->integ.find(slot);
+  if (it == ctx->integ.end()) return fail(ctx, LEAP_ERR_NOT_READY, "integration slot not set");
+  if (ndir <= 0) return fail(ctx, LEAP_ERR_INVALID_ARGUMENT, "ndirections must be positive");
+  if (precision != LEAP_PRECISION_FP64 && precision != LEAP_PRECISION_MIXED)
+    return fail(ctx, LEAP_ERR_INVALID_ARGUMENT, "unknown precision");
+  Integration& in = it->second;
+  Metadata& md = ctx->md;
+  const int32_t nbl = static_cast<int32_t>(md.k.nbaselines);
+  const int32_t P = in.pols;
+  if (in.rows % nbl != 0)
+    return fail(ctx, LEAP_ERR_INVALID_ARGUMENT, "integration rows not a multiple of the baseline count");
+  const int32_t T = static_cast<int32_t>(in.rows / nbl);
+  const int32_t C = in.channels;
+
+  // Launch shape: 32 baselines per warp, 4 warps per block.
+  const int dpw = precision == LEAP_PRECISION_FP64 ? 2 : 4;
+  const int tiles = (nbl + 31) / 32;
+  const int dgroups = (ndir + 4 * dpw - 1) / (4 * dpw);
+  int t_per, c_per, nts, ncs;
+  choose_slabs(T, C, static_cast<int64_t>(tiles) * dgroups, t_per, c_per, nts, ncs);
+  const int nslab = nts * ncs;
+  const int64_t avg_elems = static_cast<int64_t>(ndir) * P * nbl;
+
+  LEAP_CUDA(ctx->avg.ensure(sizeof(double2) * avg_elems), "alloc avgData");
+  if (nslab > 1) LEAP_CUDA(ctx->partial.ensure(sizeof(double2) * avg_elems * nslab), "alloc partial sums");
+  LEAP_CUDA(ctx->lambda.ensure(sizeof(double) * C), "alloc wavelengths");
+  LEAP_CUDA(ctx->cal1.ensure(sizeof(double) * ndir * md.S), "alloc cal1");
+  LEAP_CUDA(ctx->dphi.ensure(sizeof(double) * static_cast<size_t>(ndir) * md.Kpad), "alloc dphi");
+  const int kchunk = 512;
+  const int nk = (md.Arows + kchunk - 1) / kchunk;
+  LEAP_CUDA(ctx->gemm_partial.ensure(sizeof(double) * static_cast<size_t>(nk) * ndir * md.S), "alloc gemm partial");
+
+  // Channel wavelengths, computed exactly as Constants::GetChannelWavelength does;
+  // uploaded only when the channel count or the spectral window changes.
+  if (ctx->lambda_host.size() != static_cast<size_t>(C) || ctx->lambda_f0 != md.k.freq_start_hz ||
+      ctx->lambda_df != md.k.freq_inc_hz) {
+    ctx->lambda_host.resize(C);
+    for (int c = 0; c < C; ++c) ctx->lambda_host[c] = kSpeedOfLight / (md.k.freq_start_hz + c * md.k.freq_inc_hz);
+    ctx->lambda_f0 = md.k.freq_start_hz;
+    ctx->lambda_df = md.k.freq_inc_hz;
+    LEAP_CUDA(cudaMemcpyAsync(ctx->lambda.ptr, ctx->lambda_host.data(), sizeof(double) * C, cudaMemcpyHostToDevice, s),
+              "upload wavelengths");
+  }
+
+  RotateArgs ra{};
+  ra.vis = in.vis.ptr;
+  ra.uvw = in.uvw.as<double>();
+  ra.dd = d_dd;
+  ra.lambda = ctx->lambda.as<double>();
+  ra.rows = in.rows;
+  ra.channels = C;
+  ra.pols = P;
+  ra.nbl = nbl;
+  ra.timesteps = T;
+  ra.ndir = ndir;
+  ra.f0 = md.k.freq_start_hz;
+  ra.df = md.k.freq_inc_hz;
+  ra.t_per_slab = t_per;
+  ra.c_per_slab = c_per;
+  ra.n_tslab = nts;
+  ra.n_cslab = ncs;
+  ra.out = nslab > 1 ? ctx->partial.as<double2>() : ctx->avg.as<double2>();
+  ra.err = ctx->dev_err.as<int>();
+
+  int kernels = 0;
+  cudaEvent_t* ev = ctx->ring[ctx->ring_count % leap_ctx::kRing];
+  cudaEventRecord(ev[0], s);
+  const dim3 grid(tiles, dgroups, nslab);
+  int rc = in.vis_type == LEAP_VIS_C64 ? dispatch_pols<float2>(ra, grid, precision, s)
+                                       : dispatch_pols<double2>(ra, grid, precision, s);
+  if (rc != 0) return fail(ctx, LEAP_ERR_INVALID_ARGUMENT, "unsupported polarisation count (1, 2 or 4)");
+  ++kernels;
+  if (nslab > 1) {
+    reduce_slabs<<<grid_1d(avg_elems, 256), 256, 0, s>>>(ctx->partial.as<double2>(), nslab, avg_elems,
+                                                            ctx->avg.as<double2>());
+    ++kernels;
+  }
+  cudaEventRecord(ev[1], s);
+
+  SolveArgs sa{};
+  sa.avg = ctx->avg.as<double2>();
+  sa.nbl = nbl;
+  sa.pols = P;
+  sa.ndir = ndir;
+  sa.S = md.S;
+  sa.I1 = md.I1.as<int32_t>();
+  sa.Ad1 = md.Ad1.as<double>();
+  sa.A1rows = md.A1rows;
+  sa.arow = md.arow.as<int4>();
+  sa.arow_val = md.arow_val.as<double2>();
+  sa.Arows = md.Arows;
+  sa.Kpad = md.Kpad;
+  sa.cal1 = ctx->cal1.as<double>();
+  sa.dphi = ctx->dphi.ptr;
+  solve_cal1<<<ndir, 256, sizeof(double) * md.A1rows, s>>>(sa);
+  ++kernels;
+  const dim3 gd((md.Kpad + 255) / 256, ndir);
+  const dim3 gg((md.S + 63) / 64, (ndir + 15) / 16, nk);
+  if (precision == LEAP_PRECISION_FP64) {
+    solve_dint_fp64<<<gd, 256, 0, s>>>(sa);
+    gemm_ad_partial<double><<<gg, 256, 0, s>>>(md.Ad.as<double>(), md.S, md.Arows, static_cast<double*>(sa.dphi),
+                                                md.Kpad, ndir, kchunk, ctx->gemm_partial.as<double>());
+  } else {
+    solve_dint_mixed<<<gd, 256, 0, s>>>(sa);
+    gemm_ad_partial<float><<<gg, 256, 0, s>>>(md.Ad_f32.as<float>(), md.S, md.Arows, static_cast<float*>(sa.dphi),
+                                               md.Kpad, ndir, kchunk, ctx->gemm_partial.as<double>());
+  }
+  gemm_ad_finish<<<(ndir * md.S + 255) / 256, 256, 0, s>>>(ctx->gemm_partial.as<double>(), nk, ndir, md.S,
+                                                           ctx->cal1.as<double>(), d_cal);
+  kernels += 3;
+  cudaEventRecord(ev[2], s);
+  ctx->ring_count++;
+  LEAP_CUDA(cudaGetLastError(), "kernel launch");
+  ctx->last_ndir = ndir;
+  ctx->last_pols = P;
+  ctx->last_nbl = nbl;
+  ctx->kernels_last = kernels;
+  return LEAP_OK;
+}
+
+int check_device_error(leap_ctx* ctx) {
+  int h = 0;
+  LEAP_CUDA(cudaMemcpy(&h, ctx->dev_err.ptr, sizeof(int), cudaMemcpyDeviceToHost), "read device error word");
+  if (h != 0) {
+    cudaMemset(ctx->dev_err.ptr, 0, sizeof(int));
+    if (h & kDevErrTimeout) return fail(ctx, LEAP_ERR_DEVICE_TIMEOUT, "a bounded device wait gave up");
+    return fail(ctx, LEAP_ERR_INTERNAL, "device reported an inconsistent shape");
+  }
+  return LEAP_OK;
+}
+
+int fill_timings(leap_ctx* ctx, leap_timings* out) {
+  *out = leap_timings{};
+  const int n = std::min(ctx->ring_count, leap_ctx::kRing);
+  if (n == 0) return LEAP_OK;
+  LEAP_CUDA(cudaEventSynchronize(ctx->ring[(ctx->ring_count - 1) % leap_ctx::kRing][2]), "wait for timing events");
+  for (int i = 0; i < n; ++i) {
+    float a = 0, b = 0;
+    LEAP_CUDA(cudaEventElapsedTime(&a, ctx->ring[i][0], ctx->ring[i][1]), "elapsed time");
+    LEAP_CUDA(cudaEventElapsedTime(&b, ctx->ring[i][1], ctx->ring[i][2]), "elapsed time");
+    out->rotate_ms += a;
+    out->solve_ms += b;
+  }
+  out->total_ms = out->rotate_ms + out->solve_ms;
+  out->kernels = ctx->kernels_last;
+  out->calls = n;
+  return LEAP_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int32_t leap_create(int32_t device, leap_ctx** out) {
+  if (!out) return fail(nullptr, LEAP_ERR_INVALID_ARGUMENT, "out is NULL");
+  *out = nullptr;
+  int n = 0;
+  cudaError_t e = cudaGetDeviceCount(&n);
+  if (e != cudaSuccess || n == 0) return fail(nullptr, LEAP_ERR_CUDA, "no CUDA device available");
+  if (device < 0 || device >= n) return fail(nullptr, LEAP_ERR_INVALID_ARGUMENT, "device index out of range");
+  leap_ctx* ctx = new leap_ctx();
+  ctx->device = device;
+  int rc = [&]() -> int {
+    DeviceGuard g(device);
+    LEAP_CUDA(cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking), "create stream");
+    for (auto& tri : ctx->ring)
+      for (auto& ev : tri) LEAP_CUDA(cudaEventCreate(&ev), "create event");
+    LEAP_CUDA(ctx->dev_err.ensure(sizeof(int)), "alloc error word");
+    LEAP_CUDA(cudaMemset(ctx->dev_err.ptr, 0, sizeof(int)), "clear error word");
+    return LEAP_OK;
+  }();
+  if (rc != LEAP_OK) {
+    g_last_error = ctx->err;
+    leap_destroy(ctx);
+    return rc;
+  }
+  *out = ctx;
+  return LEAP_OK;
+}
+
+void leap_destroy(leap_ctx* ctx) {
+  if (!ctx) return;
+  {
+    DeviceGuard g(ctx->device);
+    cudaStreamSynchronize(ctx->stream);
+    for (auto& kv : ctx->integ) {
+      kv.second.vis.release();
+      kv.second.uvw.release();
+    }
+    Metadata& md = ctx->md;
+    md.I1.release(); md.Ad1.release(); md.Ad.release(); md.Ad_f32.release(); md.arow.release(); md.arow_val.release();
+    ctx->partial.release(); ctx->avg.release(); ctx->cal1.release(); ctx->dphi.release();
+    ctx->gemm_partial.release(); ctx->dd.release(); ctx->cal.release(); ctx->dev_err.release(); ctx->lambda.release();
+    for (auto& tri : ctx->ring)
+      for (auto& ev : tri)
+        if (ev) cudaEventDestroy(ev);
+    if (ctx->stream) cudaStreamDestroy(ctx->stream);
+  }
+  delete ctx;
+}
+
+const char* leap_last_error(const leap_ctx* ctx) { return ctx ? ctx->err.c_str() : g_last_error.c_str(); }
+
+int32_t leap_set_metadata(leap_ctx* ctx, const leap_constants* k, const double* A, int32_t A_rows, int32_t A_cols,
+                          const int32_t* I, const double* Ad, const double* A1, int32_t A1_rows, const int32_t* I1,
+                          const double* Ad1) {
+  if (!ctx || !k || !A || !Ad || !A1 || !I1 || !Ad1) return fail(ctx, LEAP_ERR_INVALID_ARGUMENT, "NULL argument");
+  (void)I;
+  if (A_rows < 1 || A_cols < 1 || A1_rows < 1) return fail(ctx, LEAP_ERR_INVALID_ARGUMENT, "empty phase matrix");
+  if (k->nbaselines == 0) return fail(ctx, LEAP_ERR_INVALID_ARGUMENT, "nbaselines must be positive");
+  if (static_cast<int64_t>(A_rows) - 1 > static_cast<int64_t>(k->nbaselines))
+    return fail(ctx, LEAP_ERR_INVALID_ARGUMENT, "A has more rows than baselines + 1");
+  for (int32_t i = 0; i + 1 < A1_rows; ++i) {
+    const int64_t idx = I1[i] < 0 ? static_cast<int64_t>(I1[i]) + k->nbaselines : I1[i];
+    if (idx < 0 || idx >= static_cast<int64_t>(k->nbaselines))
+      return fail(ctx, LEAP_ERR_INVALID_ARGUMENT, "I1 index out of range");
+  }
+  DeviceGuard g(ctx->device);
+  Metadata& md = ctx->md;
+  md.set = false;
+  md.k = *k;
+  md.S = A_cols;
+  md.Arows = A_rows;
+  md.A1rows = A1_rows;
+  md.Kpad = ((A_rows + 127) / 128) * 128;
+  // Sparse row form of A: the two non-zeros of each row, in column order.
+  std::vector<int4> arow(A_rows);
+  std::vector<double2> aval(A_rows);
+  for (int32_t r = 0; r < A_rows; ++r) {
+    int nz = 0;
+    int cidx[2] = {0, 0};
+    double v[2] = {0.0, 0.0};
+    for (int32_t c = 0; c < A_cols; ++c) {
+      const double x = A[r + static_cast<size_t>(A_rows) * c];
+      if (x != 0.0) {
+        if (nz == 2) return fail(ctx, LEAP_ERR_INVALID_ARGUMENT, "A row has more than two non-zeros");
+        cidx[nz] = c;
+        v[nz] = x;
+        ++nz;
+      }
+    }
+    arow[r] = make_int4(cidx[0], nz > 1 ? cidx[1] : cidx[0], 0, 0);
+    aval[r] = make_double2(v[0], v[1]);
+  }
+  std::vector<float> adf(static_cast<size_t>(A_cols) * A_rows);
+  for (size_t i = 0; i < adf.size(); ++i) adf[i] = static_cast<float>(Ad[i]);
+  const size_t nI1 = static_cast<size_t>(std::max(A1_rows - 1, 0));
+  LEAP_CUDA(md.I1.ensure(sizeof(int32_t) * std::max<size_t>(nI1, 1)), "alloc I1");
+  LEAP_CUDA(md.Ad1.ensure(sizeof(double) * A_cols * A1_rows), "alloc Ad1");
+  LEAP_CUDA(md.Ad.ensure(sizeof(double) * A_cols * A_rows), "alloc Ad");
+  LEAP_CUDA(md.Ad_f32.ensure(sizeof(float) * A_cols * A_rows), "alloc Ad f32");
+  LEAP_CUDA(md.arow.ensure(sizeof(int4) * A_rows), "alloc A rows");
+  LEAP_CUDA(md.arow_val.ensure(sizeof(double2) * A_rows), "alloc A values");
+  if (nI1) LEAP_CUDA(cudaMemcpy(md.I1.ptr, I1, sizeof(int32_t) * nI1, cudaMemcpyHostToDevice), "upload I1");
+  LEAP_CUDA(cudaMemcpy(md.Ad1.ptr, Ad1, sizeof(double) * A_cols * A1_rows, cudaMemcpyHostToDevice), "upload Ad1");
+  LEAP_CUDA(cudaMemcpy(md.Ad.ptr, Ad, sizeof(double) * A_cols * A_rows, cudaMemcpyHostToDevice), "upload Ad");
+  LEAP_CUDA(cudaMemcpy(md.Ad_f32.ptr, adf.data(), sizeof(float) * adf.size(), cudaMemcpyHostToDevice), "upload Ad f32");
+  LEAP_CUDA(cudaMemcpy(md.arow.ptr, arow.data(), sizeof(int4) * A_rows, cudaMemcpyHostToDevice), "upload A rows");
+  LEAP_CUDA(cudaMemcpy(md.arow_val.ptr, aval.data(), sizeof(double2) * A_rows, cudaMemcpyHostToDevice), "upload A vals");
+  md.set = true;
+  return LEAP_OK;
+}
+
+int32_t leap_set_integration(leap_ctx* ctx, int32_t slot, int32_t vis_type, const void* vis, const double* uvw,
+                             int64_t rows, int32_t channels, int32_t pols, int32_t memory) {
+  if (!ctx || !vis || !uvw) return fail(ctx, LEAP_ERR_INVALID_ARGUMENT, "NULL argument");
+  if (slot < 0) return fail(ctx, LEAP_ERR_INVALID_ARGUMENT, "slot must be >= 0");
+  if (vis_type != LEAP_VIS_C64 && vis_type != LEAP_VIS_C128) return fail(ctx, LEAP_ERR_INVALID_ARGUMENT, "unknown vis type");
+  if (rows <= 0 || channels <= 0 || pols <= 0) return fail(ctx, LEAP_ERR_INVALID_ARGUMENT, "empty integration");
+  if (pols != 1 && pols != 2 && pols != 4) return fail(ctx, LEAP_ERR_INVALID_ARGUMENT, "pols must be 1, 2 or 4");
+  if (memory != LEAP_MEMORY_HOST && memory != LEAP_MEMORY_DEVICE) return fail(ctx, LEAP_ERR_INVALID_ARGUMENT, "unknown memory kind");
+  DeviceGuard g(ctx->device);
+  Integration& in = ctx->integ[slot];
+  const size_t esz = vis_type == LEAP_VIS_C64 ? sizeof(float2) : sizeof(double2);
+  const int64_t groups = rows * channels;
+  const size_t vbytes = esz * static_cast<size_t>(groups) * pols;
+  LEAP_CUDA(in.vis.ensure(vbytes), "alloc vis");
+  LEAP_CUDA(in.uvw.ensure(sizeof(double) * 3 * rows), "alloc uvw");
+  const cudaMemcpyKind kind = memory == LEAP_MEMORY_HOST ? cudaMemcpyHostToDevice : cudaMemcpyDeviceToDevice;
+  LEAP_CUDA(cudaMemcpyAsync(in.vis.ptr, vis, vbytes, kind, ctx->stream), "copy vis");
+  LEAP_CUDA(cudaMemcpyAsync(in.uvw.ptr, uvw, sizeof(double) * 3 * rows, kind, ctx->stream), "copy uvw");
+  const int grid = grid_1d(groups, 256);
+  if (vis_type == LEAP_VIS_C64) {
+    float2* p = in.vis.as<float2>();
+    if (pols == 4) sanitize_nan_groups<float2, 4><<<grid, 256, 0, ctx->stream>>>(p, p, groups);
+    else sanitize_nan_groups_generic<float2><<<grid, 256, 0, ctx->stream>>>(p, p, groups, pols);
+  } else {
+    double2* p = in.vis.as<double2>();
+    if (pols == 4) sanitize_nan_groups<double2, 4><<<grid, 256, 0, ctx->stream>>>(p, p, groups);
+    else sanitize_nan_groups_generic<double2><<<grid, 256, 0, ctx->stream>>>(p, p, groups, pols);
+  }
+  LEAP_CUDA(cudaGetLastError(), "sanitize launch");
+  LEAP_CUDA(cudaStreamSynchronize(ctx->stream), "set integration");
+  in.vis_type = vis_type;
+  in.rows = rows;
+  in.channels = channels;
+  in.pols = pols;
+  return LEAP_OK;
+}
+
+int32_t leap_release_integration(leap_ctx* ctx, int32_t slot) {
+  if (!ctx) return fail(ctx, LEAP_ERR_INVALID_ARGUMENT, "NULL context");
+  auto it = ctx->integ.find(slot);
+  if (it == ctx->integ.end()) return fail(ctx, LEAP_ERR_NOT_READY, "integration slot not set");
+  DeviceGuard g(ctx->device);
+  cudaStreamSynchronize(ctx->stream);
+  it->second.vis.release();
+  it->second.uvw.release();
+  ctx->integ.erase(it);
+  return LEAP_OK;
+}
+
+int32_t leap_calibrate(leap_ctx* ctx, int32_t slot, const double* dd, int32_t ndir, int32_t precision, double* cal_out) {
+  if (!ctx || !dd || !cal_out) return fail(ctx, LEAP_ERR_INVALID_ARGUMENT, "NULL argument");
+  if (ndir <= 0) return fail(ctx, LEAP_ERR_INVALID_ARGUMENT, "ndirections must be positive");
+  if (!ctx->md.set) return fail(ctx, LEAP_ERR_NOT_READY, "metadata not set");
+  DeviceGuard g(ctx->device);
+  const int S = ctx->md.S;
+  LEAP_CUDA(ctx->dd.ensure(sizeof(double) * 9 * ndir), "alloc dd");
+  LEAP_CUDA(ctx->cal.ensure(sizeof(double) * S * ndir), "alloc cal");
+  LEAP_CUDA(cudaMemcpyAsync(ctx->dd.ptr, dd, sizeof(double) * 9 * ndir, cudaMemcpyHostToDevice, ctx->stream), "upload dd");
+  int rc = calibrate_impl(ctx, slot, ctx->dd.as<double>(), ndir, precision, ctx->cal.as<double>(), ctx->stream);
+  if (rc != LEAP_OK) return rc;
+  LEAP_CUDA(cudaMemcpyAsync(cal_out, ctx->cal.ptr, sizeof(double) * S * ndir, cudaMemcpyDeviceToHost, ctx->stream), "download cal");
+  LEAP_CUDA(cudaStreamSynchronize(ctx->stream), "calibrate");
+  return check_device_error(ctx);
+}
+
+int32_t leap_calibrate_async(leap_ctx* ctx, int32_t slot, const double* d_dd, int32_t ndir, int32_t precision,
+                             double* d_cal_out, void* stream) {
+  if (!ctx || !d_dd || !d_cal_out) return fail(ctx, LEAP_ERR_INVALID_ARGUMENT, "NULL argument");
+  DeviceGuard g(ctx->device);
+  cudaStream_t s = stream ? static_cast<cudaStream_t>(stream) : ctx->stream;
+  return calibrate_impl(ctx, slot, d_dd, ndir, precision, d_cal_out, s);
+}
+
+int32_t leap_get_avgdata(leap_ctx* ctx, int32_t direction, double* out) {
+  if (!ctx || !out) return fail(ctx, LEAP_ERR_INVALID_ARGUMENT, "NULL argument");
+  if (direction < 0 || direction >= ctx->last_ndir) return fail(ctx, LEAP_ERR_INVALID_ARGUMENT, "direction out of range");
+  DeviceGuard g(ctx->device);
+  const size_t n = static_cast<size_t>(ctx->last_pols) * ctx->last_nbl;
+  LEAP_CUDA(cudaStreamSynchronize(ctx->stream), "sync");
+  LEAP_CUDA(cudaMemcpy(out, ctx->avg.as<double2>() + n * direction, sizeof(double2) * n, cudaMemcpyDeviceToHost), "download avgData");
+  return LEAP_OK;
+}
+
+int32_t leap_rotate_uvw(leap_ctx* ctx, int32_t slot, const double* dd, int32_t ndir, double* out) {
+  if (!ctx || !dd || !out) return fail(ctx, LEAP_ERR_INVALID_ARGUMENT, "NULL argument");
+  auto it = ctx->integ.find(slot);
+  if (it == ctx->integ.end()) return fail(ctx, LEAP_ERR_NOT_READY, "integration slot not set");
+  if (ndir <= 0) return fail(ctx, LEAP_ERR_INVALID_ARGUMENT, "ndirections must be positive");
+  DeviceGuard g(ctx->device);
+  const int64_t rows = it->second.rows;
+  DeviceBuffer d_dd, d_out;
+  LEAP_CUDA(d_dd.ensure(sizeof(double) * 9 * ndir), "alloc dd");
+  LEAP_CUDA(d_out.ensure(sizeof(double) * 3 * rows * ndir), "alloc rotated uvw");
+  LEAP_CUDA(cudaMemcpyAsync(d_dd.ptr, dd, sizeof(double) * 9 * ndir, cudaMemcpyHostToDevice, ctx->stream), "upload dd");
+  rotate_uvw<<<grid_1d(rows * ndir, 256), 256, 0, ctx->stream>>>(d_dd.as<double>(), it->second.uvw.as<double>(), rows, ndir,
+                                                                d_out.as<double>());
+  LEAP_CUDA(cudaGetLastError(), "rotate_uvw launch");
+  LEAP_CUDA(cudaMemcpyAsync(out, d_out.ptr, sizeof(double) * 3 * rows * ndir, cudaMemcpyDeviceToHost, ctx->stream), "download");
+  LEAP_CUDA(cudaStreamSynchronize(ctx->stream), "rotate_uvw");
+  d_dd.release();
+  d_out.release();
+  return LEAP_OK;
+}
+
+int32_t leap_get_timings(leap_ctx* ctx, leap_timings* out) {
+  if (!ctx || !out) return fail(ctx, LEAP_ERR_INVALID_ARGUMENT, "NULL argument");
+  DeviceGuard g(ctx->device);
+  return fill_timings(ctx, out);
+}
+
+int32_t leap_timing_reset(leap_ctx* ctx) {
+  if (!ctx) return fail(ctx, LEAP_ERR_INVALID_ARGUMENT, "NULL context");
+  ctx->ring_count = 0;
+  return LEAP_OK;
+}
+
+int32_t leap_synchronize(leap_ctx* ctx) {
+  if (!ctx) return fail(ctx, LEAP_ERR_INVALID_ARGUMENT, "NULL context");
+  DeviceGuard g(ctx->device);
+  LEAP_CUDA(cudaStreamSynchronize(ctx->stream), "synchronize");
+  LEAP_CUDA(cudaDeviceSynchronize(), "synchronize device");
+  return check_device_error(ctx);
+}
+
+void leap_dd_matrix(double phase_ra, double phase_dec, double ra, double dec, double* dd_out) {
+  if (dd_out) dd_matrix(phase_ra, phase_dec, ra, dec, dd_out);
+}
+
+int32_t leap_phase_matrix(const int32_t* a1, const int32_t* a2, const uint8_t* fg, int32_t n, int32_t ref_ant,
+                          double* A_out, int32_t* I_out, int32_t* rows_out, int32_t* cols_out) {
+  if (n > 0 && (!a1 || !a2 || !fg || !A_out || !I_out || !rows_out || !cols_out))
+    return fail(nullptr, LEAP_ERR_INVALID_ARGUMENT, "NULL argument");
+  std::vector<double> A;
+  std::vector<int32_t> I;
+  int32_t rows = 0, cols = 0;
+  std::string err;
+  int rc = phase_matrix(a1, a2, fg, n, ref_ant, A, I, rows, cols, err);
+  if (rc != LEAP_OK) return fail(nullptr, rc, err);
+  std::memcpy(A_out, A.data(), sizeof(double) * A.size());
+  if (!I.empty()) std::memcpy(I_out, I.data(), sizeof(int32_t) * I.size());
+  *rows_out = rows;
+  *cols_out = cols;
+  return LEAP_OK;
+}
+
+int32_t leap_pseudo_inverse(const double* A, int32_t rows, int32_t cols, double* Ad_out) {
+  if (!A || !Ad_out) return fail(nullptr, LEAP_ERR_INVALID_ARGUMENT, "NULL argument");
+  std::string err;
+  int rc = pseudo_inverse(A, rows, cols, Ad_out, err);
+  if (rc != LEAP_OK) return fail(nullptr, rc, err);
+  return LEAP_OK;
+}
+
+}  // extern "C"

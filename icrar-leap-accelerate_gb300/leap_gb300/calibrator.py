@@ -1,0 +1,308 @@
+"""Python mirror of the reference calibration interface over the C ABI.
+
+``GpuLeapCalibrator.calibrate`` has the argument meaning and error behaviour of
+``ILeapCalibrator::Calibrate`` (LA/algorithm/ILeapCalibrator.h:62-68) and the
+loop structure of ``CudaLeapCalibrator::Calibrate``
+(LA/algorithm/cuda/CudaLeapCalibrator.cu:94-233): MetaData once, then per
+solution interval one resident integration and one batched call over all
+directions.  ``Context`` exposes the C ABI one entry point per method.
+
+(LA/ = src/icrar/leap-accelerate/ in the reference project.)
+"""
+from __future__ import annotations
+
+import ctypes
+from dataclasses import dataclass
+from typing import List, Optional, Sequence, Tuple
+
+import numpy as np
+
+from . import _abi
+from ._abi import lib
+
+SPEED_OF_LIGHT = 299792458.0
+
+
+class LeapError(RuntimeError):
+    def __init__(self, code: int, msg: str):
+        super().__init__(f"[{code}] {msg}")
+        self.code = code
+
+
+class InvalidArgument(LeapError, ValueError):
+    """Where the reference throws icrar::invalid_argument_exception."""
+
+
+def _raise(code: int, msg: str):
+    if code == _abi.LEAP_ERR_INVALID_ARGUMENT:
+        raise InvalidArgument(code, msg)
+    raise LeapError(code, msg)
+
+
+def _check(code: int, ctx=None):
+    if code != _abi.LEAP_OK:
+        msg = lib.leap_last_error(ctx)
+        _raise(code, msg.decode() if msg else "")
+
+
+def _ptr(a: np.ndarray):
+    return a.ctypes.data_as(ctypes.c_void_p)
+
+
+# ---------------------------------------------------------------------------
+# Host set-up maths (the library's own C++ code)
+# ---------------------------------------------------------------------------
+
+def dd_matrix(phase_ra: float, phase_dec: float, ra: float, dec: float) -> np.ndarray:
+    """MetaData::GenerateDDMatrix (LA/model/cpu/MetaData.cc:166-203)."""
+    out = np.zeros(9, dtype=np.float64)
+    lib.leap_dd_matrix(phase_ra, phase_dec, ra, dec, _ptr(out))
+    return out.reshape(3, 3)
+
+
+def phase_matrix(a1, a2, fg, ref_ant: Optional[int]) -> Tuple[np.ndarray, np.ndarray]:
+    """PhaseMatrixFunction (LA/algorithm/cpu/PhaseMatrixFunction.cc:35-93): (A, I)."""
+    a1 = np.ascontiguousarray(a1, dtype=np.int32)
+    a2 = np.ascontiguousarray(a2, dtype=np.int32)
+    fg = np.ascontiguousarray(fg, dtype=np.uint8)
+    n = a1.size
+    if a2.size != n or fg.size != n:
+        raise InvalidArgument(_abi.LEAP_ERR_INVALID_ARGUMENT, "a1, a2 and fg must be equal size")
+    cols_cap = int(max(a1.max(), a2.max())) + 1 if n else 1
+    A = np.zeros((n + 1) * cols_cap, dtype=np.float64)
+    I = np.zeros(max(n, 1), dtype=np.int32)
+    rows, cols = ctypes.c_int32(0), ctypes.c_int32(0)
+    _check(lib.leap_phase_matrix(_ptr(a1), _ptr(a2), _ptr(fg), n, -1 if ref_ant is None else int(ref_ant),
+                                 _ptr(A), _ptr(I), ctypes.byref(rows), ctypes.byref(cols)))
+    r, c = rows.value, cols.value
+    return A[: r * c].reshape(c, r).T.copy(), I[: r - 1].copy()
+
+
+def pseudo_inverse(A: np.ndarray) -> np.ndarray:
+    """SVDPseudoInverse (LA/math/cpu/matrix_invert.h:49-56)."""
+    A = np.asfortranarray(A, dtype=np.float64)
+    m, n = A.shape
+    Ad = np.zeros((n, m), dtype=np.float64, order="F")
+    _check(lib.leap_pseudo_inverse(_ptr(A), m, n, _ptr(Ad)))
+    return np.ascontiguousarray(Ad)
+
+
+@dataclass
+class MetaData:
+    """The fields of cpu::MetaData the calibration path uses (LA/model/cpu/MetaData.h:107-127)."""
+    nbaselines: int
+    reference_antenna: int
+    channels: int
+    num_pols: int
+    stations: int
+    rows: int
+    freq_start_hz: float
+    freq_inc_hz: float
+    phase_centre_ra_rad: float
+    phase_centre_dec_rad: float
+    A: np.ndarray
+    I: np.ndarray
+    Ad: np.ndarray
+    A1: np.ndarray
+    I1: np.ndarray
+    Ad1: np.ndarray
+
+    def constants(self) -> _abi.LeapConstants:
+        return _abi.LeapConstants(self.nbaselines, self.reference_antenna, self.channels, self.num_pols,
+                                  self.stations, self.rows, self.freq_start_hz, self.freq_inc_hz,
+                                  self.phase_centre_ra_rad, self.phase_centre_dec_rad, 0.0, 0.0)
+
+
+def filtered_baselines(obs, minimum_baseline_threshold: float) -> np.ndarray:
+    """MeasurementSet::GetFilteredBaselines (LA/ms/MeasurementSet.cc:181-240)."""
+    nbl = obs.nbaselines
+    flagged = np.asarray(obs.flags[:nbl], dtype=bool)
+    short = np.zeros(nbl, dtype=bool)
+    if minimum_baseline_threshold > 0.0:
+        uv = obs.uvw[:nbl]
+        short = np.sqrt(uv[:, 0] ** 2 + uv[:, 1] ** 2) < minimum_baseline_threshold
+    return flagged | short
+
+
+def build_metadata(obs, reference_antenna: Optional[int] = None, minimum_baseline_threshold: float = 0.0) -> MetaData:
+    """cpu::MetaData construction (LA/model/cpu/MetaData.cc:42-137) on the host."""
+    ref = reference_antenna if reference_antenna is not None else obs.total_antennas - 1
+    fg = filtered_baselines(obs, minimum_baseline_threshold)
+    a1 = obs.antenna1[: obs.nbaselines]
+    a2 = obs.antenna2[: obs.nbaselines]
+    A1, I1 = phase_matrix(a1, a2, fg, ref)
+    A, I = phase_matrix(a1, a2, fg, None)
+    return MetaData(obs.nbaselines, ref, obs.channels, obs.pols, obs.num_stations, obs.rows,
+                    obs.freq_start_hz, obs.freq_inc_hz, obs.phase_centre[0], obs.phase_centre[1],
+                    A, I, pseudo_inverse(A), A1, I1, pseudo_inverse(A1))
+
+
+# ---------------------------------------------------------------------------
+# Device context
+# ---------------------------------------------------------------------------
+
+def _vis_type(dtype) -> int:
+    if dtype == np.complex64:
+        return _abi.LEAP_VIS_C64
+    if dtype == np.complex128:
+        return _abi.LEAP_VIS_C128
+    raise InvalidArgument(_abi.LEAP_ERR_INVALID_ARGUMENT, f"unsupported visibility dtype {dtype}")
+
+
+class Context:
+    """One device, one stream, the resident buffers (leap_create ... leap_destroy)."""
+
+    def __init__(self, device: int = 0):
+        h = ctypes.c_void_p()
+        _check(lib.leap_create(device, ctypes.byref(h)))
+        self._h = h
+        self.device = device
+        self.md: Optional[MetaData] = None
+        self.slots = {}
+        self._last_slot = None
+
+    @property
+    def handle(self):
+        return self._h
+
+    def close(self):
+        if self._h:
+            lib.leap_destroy(self._h)
+            self._h = None
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def _check(self, code: int):
+        _check(code, self._h)
+
+    def set_metadata(self, md: MetaData):
+        k = md.constants()
+        A = np.asfortranarray(md.A, dtype=np.float64)
+        Ad = np.asfortranarray(md.Ad, dtype=np.float64)
+        A1 = np.asfortranarray(md.A1, dtype=np.float64)
+        Ad1 = np.asfortranarray(md.Ad1, dtype=np.float64)
+        I = np.ascontiguousarray(md.I, dtype=np.int32)
+        I1 = np.ascontiguousarray(md.I1, dtype=np.int32)
+        if I.size == 0:
+            I = np.zeros(1, dtype=np.int32)
+        if I1.size == 0:
+            I1 = np.zeros(1, dtype=np.int32)
+        self._check(lib.leap_set_metadata(self._h, ctypes.byref(k), _ptr(A), A.shape[0], A.shape[1], _ptr(I),
+                                          _ptr(Ad), _ptr(A1), A1.shape[0], _ptr(I1), _ptr(Ad1)))
+        self.md = md
+
+    def set_integration(self, slot: int, vis, uvw):
+        """vis: (channels, rows, pols) complex64/complex128 numpy array or CUDA torch tensor
+        (a torch complex tensor or its real view); uvw: (rows, 3) float64."""
+        if isinstance(vis, np.ndarray):
+            vis = np.ascontiguousarray(vis)
+            uvw = np.ascontiguousarray(uvw, dtype=np.float64)
+            C, rows, P = vis.shape
+            self._check(lib.leap_set_integration(self._h, slot, _vis_type(vis.dtype), _ptr(vis), _ptr(uvw),
+                                                 rows, C, P, _abi.LEAP_MEMORY_HOST))
+        else:  # torch tensor on the device
+            import torch
+            assert vis.is_cuda and vis.is_contiguous() and uvw.is_cuda and uvw.is_contiguous()
+            vt = {torch.complex64: _abi.LEAP_VIS_C64, torch.complex128: _abi.LEAP_VIS_C128}[vis.dtype]
+            C, rows, P = vis.shape
+            self._check(lib.leap_set_integration(self._h, slot, vt, vis.data_ptr(), uvw.data_ptr(), rows, C, P,
+                                                 _abi.LEAP_MEMORY_DEVICE))
+        self.slots[slot] = (C, rows, P)
+
+    def release_integration(self, slot: int):
+        self._check(lib.leap_release_integration(self._h, slot))
+        self.slots.pop(slot, None)
+
+    def calibrate(self, slot: int, dds: np.ndarray, precision: int = _abi.LEAP_PRECISION_FP64) -> np.ndarray:
+        dds = np.ascontiguousarray(dds, dtype=np.float64).reshape(-1, 9)
+        D = dds.shape[0]
+        S = self.md.A.shape[1]
+        cal = np.zeros((D, S), dtype=np.float64)
+        self._check(lib.leap_calibrate(self._h, slot, _ptr(dds), D, precision, _ptr(cal)))
+        self._last_slot = slot
+        return cal
+
+    def calibrate_async(self, slot: int, dd_ptr: int, ndir: int, precision: int, cal_ptr: int, stream: int = 0):
+        self._check(lib.leap_calibrate_async(self._h, slot, dd_ptr, ndir, precision, cal_ptr, stream or None))
+
+    def avgdata(self, direction: int) -> np.ndarray:
+        """avgData of one direction from the last call, as (nbl, pols) complex128."""
+        C, rows, P = self.slots[self._last_slot]
+        nbl = self.md.nbaselines
+        out = np.zeros(2 * nbl * P, dtype=np.float64)
+        self._check(lib.leap_get_avgdata(self._h, direction, _ptr(out)))
+        return out.view(np.complex128).reshape(P, nbl).T.copy()
+
+    def rotate_uvw(self, slot: int, dds: np.ndarray) -> np.ndarray:
+        dds = np.ascontiguousarray(dds, dtype=np.float64).reshape(-1, 9)
+        C, rows, P = self.slots[slot]
+        out = np.zeros((dds.shape[0], rows, 3), dtype=np.float64)
+        self._check(lib.leap_rotate_uvw(self._h, slot, _ptr(dds), dds.shape[0], _ptr(out)))
+        return out
+
+    def timings(self) -> dict:
+        t = _abi.LeapTimings()
+        self._check(lib.leap_get_timings(self._h, ctypes.byref(t)))
+        return {"rotate_ms": t.rotate_ms, "solve_ms": t.solve_ms, "total_ms": t.total_ms, "kernels": t.kernels,
+                "calls": t.calls}
+
+    def timing_reset(self):
+        self._check(lib.leap_timing_reset(self._h))
+
+    def synchronize(self):
+        self._check(lib.leap_synchronize(self._h))
+
+
+# ---------------------------------------------------------------------------
+# ILeapCalibrator mirror
+# ---------------------------------------------------------------------------
+
+def evaluate_slice(start: int, interval: int, end: int, collection_size: int):
+    """Slice::Evaluate + Range (LA/common/Slice.h:47-54, LA/common/Range.h:40-63)."""
+    s = collection_size if start == -1 else start
+    i = collection_size if interval == -1 else interval
+    e = collection_size if end == -1 else end
+    if s < 0 or i < 1 or e < 0:
+        raise InvalidArgument(_abi.LEAP_ERR_INVALID_ARGUMENT, "expected a positive integer")
+    return s, i, e, (e - s) // i
+
+
+class GpuLeapCalibrator:
+    """ILeapCalibrator::Calibrate over the GB300 path (ComputeImplementation "gb300")."""
+
+    def __init__(self, device: int = 0, precision: int = _abi.LEAP_PRECISION_FP64):
+        self.ctx = Context(device)
+        self.precision = precision
+
+    def calibrate(self, obs, directions: Sequence[Sequence[float]], solution_interval=(0, -1, -1),
+                  minimum_baseline_threshold: float = 0.0, reference_antenna: Optional[int] = None,
+                  is_file_system_cache_enabled: bool = False, md: Optional[MetaData] = None) -> List[dict]:
+        if md is None:
+            md = build_metadata(obs, reference_antenna, minimum_baseline_threshold)
+        self.ctx.set_metadata(md)
+        _, interval, _, solutions = evaluate_slice(*solution_interval, obs.timesteps)
+        nbl = obs.nbaselines
+        directions = np.asarray(directions, dtype=np.float64).reshape(-1, 2)
+        dds = np.stack([dd_matrix(md.phase_centre_ra_rad, md.phase_centre_dec_rad, r, d) for r, d in directions])
+        out = []
+        for s in range(solutions):
+            r0 = s * interval * nbl  # start row ignores Slice.start, as CpuLeapCalibrator.cc:116 does
+            nrows = interval * nbl
+            self.ctx.set_integration(0, np.ascontiguousarray(obs.vis[:, r0:r0 + nrows, :]), obs.uvw[r0:r0 + nrows])
+            cal = self.ctx.calibrate(0, dds, self.precision)
+            out.append({
+                "epoch": {"start": float(obs.epochs[s * interval]), "end": float(obs.epochs[(s + 1) * interval - 1])},
+                "calibration": [{"direction": [float(x) for x in directions[i]], "beamCalibration": cal[i].tolist()}
+                                for i in range(len(directions))],
+            })
+        return out

@@ -1,0 +1,175 @@
+/*
+ * leap_gb300.h — C ABI of the GB300-native LEAP calibration hot path.
+ *
+ * Plain C types only (pointers, sizes, POD structs); every entry point returns
+ * an int32 status and never throws.  A context owns one CUDA device, one
+ * stream and the device-resident buffers the reference keeps in its
+ * ConstantBuffer / SolutionIntervalBuffer / DirectionBuffer / DeviceIntegration
+ * objects (LA/model/cuda/DeviceMetaData.h:63-217, LA/model/cuda/DeviceIntegration.h:64-124).
+ *
+ * Citations name the reference interface each entry point replaces, as
+ * path:line within the reference project (LA/ = src/icrar/leap-accelerate/).
+ *
+ * Layout conventions (all the reference's own):
+ *   vis      (pol, row, channel) column-major complex tensor, i.e. a C array
+ *            [channels][rows][pols] of (re, im)               (LA/ms/utils.h:133-145)
+ *   uvw      [rows][3] doubles (u, v, w) in metres            (LA/ms/utils.h:44-78)
+ *   A, Ad    column-major doubles, A is Arows x S, Ad is S x Arows
+ *            (LA/algorithm/cpu/PhaseMatrixFunction.cc:59, LA/math/cpu/matrix_invert.h:55)
+ *   dd       [ndirections][9] row-major 3x3 direction matrices
+ *            (LA/model/cpu/MetaData.cc:166-203)
+ *   cal      [ndirections][S] doubles, per-antenna phase calibration
+ *            (LA/model/cpu/calibration/BeamCalibration.h:45-124)
+ *   avgData  per direction [pols][nbl] complex doubles (nbl x pols column-major,
+ *            LA/model/cpu/MetaData.h:127)
+ */
+#ifndef LEAP_GB300_H
+#define LEAP_GB300_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* Status codes.  LEAP_ERR_INVALID_ARGUMENT is where the reference throws
+ * icrar::invalid_argument_exception (LA/exception/exception.h:35-92). */
+#define LEAP_OK 0
+#define LEAP_ERR_INVALID_ARGUMENT 1
+#define LEAP_ERR_CUDA 2
+#define LEAP_ERR_NOT_READY 3
+#define LEAP_ERR_DEVICE_TIMEOUT 4
+#define LEAP_ERR_OUT_OF_MEMORY 5
+#define LEAP_ERR_INTERNAL 6
+
+/* Visibility element types. */
+#define LEAP_VIS_C64 0  /* complex<float>  (the MeasurementSet DATA type) */
+#define LEAP_VIS_C128 1 /* complex<double> (the reference Integration type) */
+
+/* Arithmetic forms. */
+#define LEAP_PRECISION_FP64 0  /* all-FP64, matches the reference CPU path to <= 1e-10 rad */
+#define LEAP_PRECISION_MIXED 1 /* FP64 phase arguments, FP32 rotation + Kahan averaging */
+
+/* Where a pointer argument lives. */
+#define LEAP_MEMORY_HOST 0
+#define LEAP_MEMORY_DEVICE 1
+
+typedef struct leap_ctx leap_ctx;
+
+/* cpu::Constants (LA/model/cpu/MetaData.h:76-101), field for field. */
+typedef struct leap_constants {
+    uint32_t nbaselines;
+    uint32_t referenceAntenna;
+    uint32_t channels;
+    uint32_t num_pols;
+    uint32_t stations;
+    uint32_t rows;
+    double freq_start_hz;
+    double freq_inc_hz;
+    double phase_centre_ra_rad;
+    double phase_centre_dec_rad;
+    double dlm_ra;
+    double dlm_dec;
+} leap_constants;
+
+/* One unit of a batched call: directions [first_direction, first_direction +
+ * ndirections) of the dd array are calibrated against integration `slot`. */
+typedef struct leap_work_item {
+    int32_t slot;
+    int32_t first_direction;
+    int32_t ndirections;
+    int32_t reserved;
+} leap_work_item;
+
+/* Device-side timings (CUDA events on the launching stream), summed over the
+ * calibrate calls recorded since the last leap_timing_reset (at most 256). */
+typedef struct leap_timings {
+    float rotate_ms;   /* rotate + average (the hot kernel) */
+    float solve_ms;    /* phase angles + both contractions */
+    float total_ms;
+    int32_t kernels;   /* kernels launched by one call (the last one) */
+    int32_t calls;     /* calls summed */
+} leap_timings;
+
+/* Context lifetime.  Replaces CudaLeapCalibrator's constructor/destructor and
+ * its cuBLAS handle (LA/algorithm/cuda/CudaLeapCalibrator.cu:73-92). */
+int32_t leap_create(int32_t device, leap_ctx** out);
+void leap_destroy(leap_ctx* ctx);
+
+/* Message of the last failure on this context ("" if none).  Thread-local
+ * message for failures without a context (ctx == NULL). */
+const char* leap_last_error(const leap_ctx* ctx);
+
+/* Upload the calibration constants; replaces ConstantBuffer construction
+ * (LA/model/cuda/DeviceMetaData.h:63-112, DeviceMetaData.cu:33-47, called at
+ * LA/algorithm/cuda/CudaLeapCalibrator.cu:140-148).  Every row of A must hold at
+ * most two non-zeros (true of every PhaseMatrixFunction output). */
+int32_t leap_set_metadata(leap_ctx* ctx, const leap_constants* constants, const double* A, int32_t A_rows,
+                          int32_t A_cols, const int32_t* I, const double* Ad, const double* A1,
+                          int32_t A1_rows, const int32_t* I1, const double* Ad1);
+
+/* Make an integration resident in HBM under `slot` (any int >= 0; a later
+ * call with the same slot replaces it).  Replaces HostIntegration +
+ * DeviceIntegration::Set and SolutionIntervalBuffer::SetUVW
+ * (LA/model/cuda/DeviceIntegration.cu:69-84, LA/algorithm/cuda/CudaLeapCalibrator.cu:177-212).
+ * `memory` says whether vis/uvw are host or device pointers; the data is
+ * copied either way and groups of pols holding a NaN are zeroed on the copy. */
+int32_t leap_set_integration(leap_ctx* ctx, int32_t slot, int32_t vis_type, const void* vis, const double* uvw,
+                             int64_t rows, int32_t channels, int32_t pols, int32_t memory);
+
+/* Release the HBM held by one integration slot. */
+int32_t leap_release_integration(leap_ctx* ctx, int32_t slot);
+
+/* Calibrate ndirections directions against one resident integration: the body
+ * of the direction loop of CudaLeapCalibrator::Calibrate
+ * (LA/algorithm/cuda/CudaLeapCalibrator.cu:198-227, PhaseRotate :235-262).
+ * dd and cal_out are HOST pointers; the call blocks until cal_out is written. */
+int32_t leap_calibrate(leap_ctx* ctx, int32_t slot, const double* dd, int32_t ndirections, int32_t precision,
+                       double* cal_out);
+
+/* Same with DEVICE pointers, stream-ordered on `stream` (a cudaStream_t; NULL
+ * selects the context's stream).  Does not synchronise; the context's scratch
+ * buffers are shared by all calls, so calls on different streams must not overlap. */
+int32_t leap_calibrate_async(leap_ctx* ctx, int32_t slot, const double* d_dd, int32_t ndirections,
+                             int32_t precision, double* d_cal_out, void* stream);
+
+/* Copy the avgData of `direction` from the last calibrate call to host memory
+ * (pols x nbl complex doubles): MetaData::GetAvgData after RotateVisibilities
+ * (LA/model/cpu/MetaData.h:127; DeviceMetaData::ToHost). */
+int32_t leap_get_avgdata(leap_ctx* ctx, int32_t direction, double* out);
+
+/* Rotate the UVWs of a resident integration by ndirections direction matrices
+ * (host dd, host out [ndirections][rows][3]).  Replaces MetaData::CalcUVW /
+ * g_RotateUVW (LA/model/cpu/MetaData.cc:220-229, LA/algorithm/cuda/CudaLeapCalibrator.cu:271-293). */
+int32_t leap_rotate_uvw(leap_ctx* ctx, int32_t slot, const double* dd, int32_t ndirections, double* out);
+
+/* Timings summed over the calls since the last reset; waits for the last
+ * recorded call to finish on its stream. */
+int32_t leap_get_timings(leap_ctx* ctx, leap_timings* out);
+
+/* Forget the recorded calls. */
+int32_t leap_timing_reset(leap_ctx* ctx);
+
+/* Block until the context's stream is idle and report any device-side error. */
+int32_t leap_synchronize(leap_ctx* ctx);
+
+/* ---- host helpers (FP64, no device needed) ---- */
+
+/* MetaData::GenerateDDMatrix (LA/model/cpu/MetaData.cc:166-203). */
+void leap_dd_matrix(double phase_ra, double phase_dec, double ra, double dec, double* dd_out);
+
+/* PhaseMatrixFunction (LA/algorithm/cpu/PhaseMatrixFunction.cc:35-93).  ref_ant < 0 = none.
+ * A_out holds (n+1) * (max(a1, a2) + 1) doubles, written column-major with leading
+ * dimension *rows_out; I_out holds n ints. */
+int32_t leap_phase_matrix(const int32_t* a1, const int32_t* a2, const uint8_t* fg, int32_t n, int32_t ref_ant,
+                          double* A_out, int32_t* I_out, int32_t* rows_out, int32_t* cols_out);
+
+/* SVDPseudoInverse (LA/math/cpu/matrix_invert.h:49-56): A is rows x cols
+ * column-major, Ad_out cols x rows column-major. */
+int32_t leap_pseudo_inverse(const double* A, int32_t rows, int32_t cols, double* Ad_out);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* LEAP_GB300_H */
