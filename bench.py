@@ -195,7 +195,10 @@ def run_gpu(args, rank: int, world: int):
     ctx.set_integration(0, vis_dev, uvw_dev)
     dd_dev = torch.from_numpy(dds.reshape(-1)).to(f"cuda:{local}")
     cal_dev = torch.empty((D, S), dtype=torch.float64, device=f"cuda:{local}")
-    stream = torch.cuda.current_stream().cuda_stream
+    # A dedicated stream: the calls and the timing events go on the same (non-null) stream.
+    bstream = torch.cuda.Stream(device=f"cuda:{local}")
+    torch.cuda.set_stream(bstream)
+    stream = bstream.cuda_stream
     prec = lg.LEAP_PRECISION_MIXED if args.precision == "mixed" else lg.LEAP_PRECISION_FP64
 
     def step(p):

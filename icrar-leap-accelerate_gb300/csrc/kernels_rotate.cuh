@@ -27,6 +27,7 @@ struct RotateArgs {
   const double* uvw;        // [rows][3]
   const double* dd;         // [ndir][9] row-major direction matrices
   const double* lambda;     // [channels] c / (f0 + ch*df), as the reference computes it
+  const float2* twiddle;    // [kTwiddleSize] (cos, sin) table for the mixed form
   int64_t rows;
   int32_t channels, pols, nbl, timesteps, ndir;
   double f0, df;
@@ -56,13 +57,17 @@ __device__ __forceinline__ void load_sample_f(const VisT* __restrict__ p, float&
 // ---------------------------------------------------------------------------
 // All-FP64 form.  Lanes own baselines, a warp owns DPW directions, a block's
 // warps share one baseline tile (so the visibility loads of one warp hit L1
-// for the others).  Arithmetic follows the reference expression by expression:
-// shiftRad = shiftFactor / lambda_c with lambda_c = c / (f0 + ch*df), then
-// exp(i*shiftRad) = (cos, sin) and a complex multiply.
+// for the others).  The reference phase is shiftRad(c) = shiftFactor / lambda_c
+// = shiftFactor * (f0 + c*df) / c_light, linear in the channel index, so
+// exp(i*shiftRad) is advanced channel to channel by one complex multiply with
+// exp(i*shiftFactor*df/c_light) and re-seeded with an exact FP64 sincos every
+// kSeed channels (drift below 1e-14 rad).  FP64 sincos runs at about 1/25 of
+// the DFMA rate on GB300, so this removes it from the inner loop.
 // ---------------------------------------------------------------------------
 template <typename VisT, int P, int DPW>
 __global__ void __launch_bounds__(128) rotate_average_fp64(RotateArgs a) {
   constexpr int NW = 4;
+  constexpr int kSeed = 16;
   const int lane = threadIdx.x & 31;
   const int warp = threadIdx.x >> 5;
   const int b = blockIdx.x * 32 + lane;
@@ -88,31 +93,39 @@ __global__ void __launch_bounds__(128) rotate_average_fp64(RotateArgs a) {
 #pragma unroll
     for (int p = 0; p < P; ++p) accr[j][p] = acci[j][p] = 0.0;
 
+  const double inv_c = 1.0 / kSpeedOfLight;
   const VisT* vis = static_cast<const VisT*>(a.vis);
   if (valid) {
     for (int t = t_lo; t < t_hi; ++t) {
       const int64_t r = static_cast<int64_t>(t) * a.nbl + b;
       const double u = __ldg(a.uvw + 3 * r), v = __ldg(a.uvw + 3 * r + 1), w = __ldg(a.uvw + 3 * r + 2);
-      double sf[DPW];
+      double sf[DPW], wr[DPW], wi[DPW];
 #pragma unroll
       for (int j = 0; j < DPW; ++j) {
         const double wrot = dd2[j][0] * u + dd2[j][1] * v + dd2[j][2] * w;
         sf[j] = -kTwoPi * (wrot - w);
+        sincos(sf[j] * (a.df * inv_c), &wi[j], &wr[j]);
       }
-      for (int c = c_lo; c < c_hi; ++c) {
-        const double lam = __ldg(a.lambda + c);
-        const VisT* src = vis + (static_cast<int64_t>(c) * a.rows + r) * P;
-        double vr[P], vi[P];
+      for (int cb = c_lo; cb < c_hi; cb += kSeed) {
+        const int ce = min(c_hi, cb + kSeed);
+        double zr[DPW], zi[DPW];
 #pragma unroll
-        for (int p = 0; p < P; ++p) load_sample(src + p, vr[p], vi[p]);
+        for (int j = 0; j < DPW; ++j) sincos(sf[j] / __ldg(a.lambda + cb), &zi[j], &zr[j]);
+        for (int c = cb; c < ce; ++c) {
+          const VisT* src = vis + (static_cast<int64_t>(c) * a.rows + r) * P;
+          double vr[P], vi[P];
 #pragma unroll
-        for (int j = 0; j < DPW; ++j) {
-          double s, co;
-          sincos(sf[j] / lam, &s, &co);
+          for (int p = 0; p < P; ++p) load_sample(src + p, vr[p], vi[p]);
 #pragma unroll
-          for (int p = 0; p < P; ++p) {
-            accr[j][p] += vr[p] * co - vi[p] * s;
-            acci[j][p] += vr[p] * s + vi[p] * co;
+          for (int j = 0; j < DPW; ++j) {
+#pragma unroll
+            for (int p = 0; p < P; ++p) {
+              accr[j][p] += vr[p] * zr[j] - vi[p] * zi[j];
+              acci[j][p] += vr[p] * zi[j] + vi[p] * zr[j];
+            }
+            const double nr = zr[j] * wr[j] - zi[j] * wi[j];
+            zi[j] = zr[j] * wi[j] + zi[j] * wr[j];
+            zr[j] = nr;
           }
         }
       }
@@ -135,8 +148,10 @@ __global__ void __launch_bounds__(128) rotate_average_fp64(RotateArgs a) {
 // Mixed-precision form (direct loads).  Per (row, direction) the phase
 //     turns(c) = -(w_rot - w) * (f0 + c*df) / c_light = A + c*B
 // is formed in FP64 once per timestep and reduced to 32-bit fixed-point
-// fractions of a turn; each channel then costs one integer multiply-add, a
-// bit-cast to an angle in [-pi, pi), FP32 sin/cos and FP32 complex MACs.
+// fractions of a turn; each channel then costs one integer multiply-add, the
+// table twiddle of twiddle_turns (about 1e-7 absolute; the hardware sin/cos
+// approximations, about 5e-7, are not accurate enough for nearly cancelling
+// sums) and FP32 complex MACs.
 // Sums run in FP32 over blocks of KB channels and are folded into Kahan
 // (sum, compensation) pairs, written out as sum - compensation in FP64.
 // ---------------------------------------------------------------------------
@@ -144,6 +159,9 @@ template <typename VisT, int P, int DPW>
 __global__ void __launch_bounds__(128) rotate_average_mixed(RotateArgs a) {
   constexpr int NW = 4;
   constexpr int KB = 16;
+  __shared__ float2 tab[kTwiddleSize];
+  for (int i = threadIdx.x; i < kTwiddleSize; i += blockDim.x) tab[i] = __ldg(a.twiddle + i);
+  __syncthreads();
   const int lane = threadIdx.x & 31;
   const int warp = threadIdx.x >> 5;
   const int b = blockIdx.x * 32 + lane;
@@ -173,8 +191,7 @@ __global__ void __launch_bounds__(128) rotate_average_mixed(RotateArgs a) {
         const int d = min(d0 + j, a.ndir - 1);
         const double wrot = __ldg(a.dd + 9 * d + 6) * u + __ldg(a.dd + 9 * d + 7) * v + __ldg(a.dd + 9 * d + 8) * w;
         const double dw = wrot - w;
-        // +256: round (instead of truncate) the 9 low bits dropped by turns_u32_to_angle.
-        pa[j] = frac_turns_u32(-dw * kA) + 256u;
+        pa[j] = frac_turns_u32(-dw * kA);
         pb[j] = frac_turns_u32(-dw * kB);
       }
       for (int cb = c_lo; cb < c_hi; cb += KB) {
@@ -191,9 +208,8 @@ __global__ void __launch_bounds__(128) rotate_average_mixed(RotateArgs a) {
           for (int p = 0; p < P; ++p) load_sample_f(src + p, vr[p], vi[p]);
 #pragma unroll
           for (int j = 0; j < DPW; ++j) {
-            const float ang = turns_u32_to_angle(pa[j] + static_cast<uint32_t>(c) * pb[j]);
             float s, co;
-            __sincosf(ang, &s, &co);
+            twiddle_turns(pa[j] + static_cast<uint32_t>(c) * pb[j], tab, co, s);
 #pragma unroll
             for (int p = 0; p < P; ++p) {
               pr[j][p] = fmaf(vr[p], co, fmaf(-vi[p], s, pr[j][p]));
@@ -229,6 +245,341 @@ __global__ void __launch_bounds__(128) rotate_average_mixed(RotateArgs a) {
             make_double2(static_cast<double>(sr[j][p]) - static_cast<double>(cr[j][p]),
                          static_cast<double>(si[j][p]) - static_cast<double>(ci[j][p]));
     }
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Mixed-precision form, pipelined (4 pols, complex<float>): the hot kernel.
+//
+// Persistent blocks of NC warps.  Work units are (32-baseline tile, direction
+// group of NC*DPW, timestep slab), visited round-robin by the blocks.  Each
+// unit is a sequence of chunks = (timestep, 16 channels).  The visibility
+// tensor is viewed as a 2-D array [channel][row*8 floats]; a chunk of the tile
+// is one TMA box of 256 floats (32 baselines x 4 pols x complex) by 16 channels
+// (16 KB), loaded with cp.async.bulk.tensor into a shared-memory stage and
+// completing on the stage's "full" mbarrier.  Boxes past the last channel or
+// row are zero-filled by the TMA unit; rows of a partial tile that belong to
+// the next timestep are loaded but not used.  Every warp releases a stage
+// through its "empty" mbarrier; lane 0 of warp 0 then refills it with the
+// chunk kPipeStages ahead.  (A separate producer warp would make 9 warps, 3
+// on one SM sub-partition, and cap registers at 168.)  All waits are bounded
+// and report a device error instead of hanging.
+//
+// Per (row, direction) the phase turns(c) = A + c*B is formed in FP64 once
+// per timestep as 32-bit fixed-point fractions of a turn.  The twiddle is
+// table-accurate (twiddle_turns) every kReseed channels and is advanced by
+// one FP32 complex multiply per channel in between (drift over 8 steps about
+// 5e-7; it reaches the cal phases only through baselines that the FP64
+// reference-antenna pass does not cover, with weight ~1/S).  Sums: FP32 over
+// each chunk, folded into Kahan pairs.
+//
+// Shared-memory reads: lane i reads its 32 bytes as two 16-byte halves; lanes
+// with bit 2 set read the upper half first so that each quarter-warp covers
+// all 32 banks (conflict-free).  Those lanes hold pols (2,3,0,1) in register
+// slots (0,1,2,3) and swap back when writing out.
+// ---------------------------------------------------------------------------
+struct PipeArgs {
+  RotateArgs a;
+  int tiles, dgroups, nslab;   // unit grid
+};
+
+constexpr int kPipeChunk = 16;    // channels per stage (TMA box height)
+constexpr int kPipeReseed = 8;    // channels between table-accurate twiddles
+constexpr int kPipeStages = 4;
+constexpr int kPipeItemBytes = 32 * 4 * 8;  // 32 baselines x 4 pols x complex<float>
+constexpr int kPipeStageBytes = kPipeChunk * kPipeItemBytes;
+
+// Position in a block's chunk sequence (unit, timestep, first channel).
+struct ChunkCursor {
+  int u, t, cb;
+  int t_lo, t_hi, c_lo, c_hi;
+};
+
+__device__ __forceinline__ void cursor_unit(ChunkCursor& k, const PipeArgs& p) {
+  const RotateArgs& a = p.a;
+  const int slab = k.u % p.nslab;
+  const int ts = slab / a.n_cslab, cs = slab % a.n_cslab;
+  k.t_lo = ts * a.t_per_slab;
+  k.t_hi = min(a.timesteps, k.t_lo + a.t_per_slab);
+  k.c_lo = cs * a.c_per_slab;
+  k.c_hi = min(a.channels, k.c_lo + a.c_per_slab);
+  k.t = k.t_lo;
+  k.cb = k.c_lo;
+}
+
+__device__ __forceinline__ void cursor_next(ChunkCursor& k, const PipeArgs& p, int units) {
+  k.cb += kPipeChunk;
+  if (k.cb < k.c_hi) return;
+  k.cb = k.c_lo;
+  if (++k.t < k.t_hi) return;
+  k.u += gridDim.x;
+  if (k.u < units) cursor_unit(k, p);
+}
+
+// Issue the TMA load of the chunk at cursor k into stage st.
+__device__ __forceinline__ void issue_chunk(const ChunkCursor& k, const PipeArgs& p, const CUtensorMap* map,
+                                           unsigned char* stage_mem, uint64_t* full, int st) {
+  const int tile = k.u / (p.dgroups * p.nslab);
+  mbar_arrive_expect_tx(&full[st], kPipeStageBytes);
+  tma_load_2d(stage_mem + st * kPipeStageBytes, map, (k.t * p.a.nbl + tile * 32) * 8, k.cb, &full[st]);
+}
+
+template <int DPW>
+__device__ __forceinline__ void mac_channel(const unsigned char* src, int h, float (&pr)[DPW][4], float (&pi)[DPW][4],
+                                            float (&zr)[DPW], float (&zi)[DPW], const float (&wr)[DPW],
+                                            const float (&wi)[DPW]) {
+  const float4 x0 = *reinterpret_cast<const float4*>(src + 16 * h);
+  const float4 x1 = *reinterpret_cast<const float4*>(src + 16 * (1 - h));
+  const float vr[4] = {x0.x, x0.z, x1.x, x1.z};
+  const float vi[4] = {x0.y, x0.w, x1.y, x1.w};
+#pragma unroll
+  for (int j = 0; j < DPW; ++j) {
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+      pr[j][q] = fmaf(vr[q], zr[j], fmaf(-vi[q], zi[j], pr[j][q]));
+      pi[j][q] = fmaf(vr[q], zi[j], fmaf(vi[q], zr[j], pi[j][q]));
+    }
+    const float nr = fmaf(zr[j], wr[j], -zi[j] * wi[j]);
+    zi[j] = fmaf(zr[j], wi[j], zi[j] * wr[j]);
+    zr[j] = nr;
+  }
+}
+
+template <int NC, int DPW>
+__global__ void __launch_bounds__(NC * 32, 1)
+    rotate_average_mixed_pipe(const __grid_constant__ CUtensorMap vis_map, PipeArgs pa_) {
+  const RotateArgs& a = pa_.a;
+  extern __shared__ __align__(128) unsigned char smem[];
+  unsigned char* stage_mem = smem;
+  float2* tab = reinterpret_cast<float2*>(smem + kPipeStages * kPipeStageBytes);
+  uint64_t* full = reinterpret_cast<uint64_t*>(tab + kTwiddleSize);
+  uint64_t* empty = full + kPipeStages;
+
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const bool producer = threadIdx.x == 0;
+  for (int i = threadIdx.x; i < kTwiddleSize; i += blockDim.x) tab[i] = __ldg(a.twiddle + i);
+  const int units = pa_.tiles * pa_.dgroups * pa_.nslab;
+  ChunkCursor pc{};  // producer cursor, kPipeStages chunks ahead of the consumers
+  uint32_t issued = 0;
+  if (producer) {
+    for (int i = 0; i < kPipeStages; ++i) {
+      mbar_init(&full[i], 1);
+      mbar_init(&empty[i], NC);
+    }
+    fence_mbar_init();
+    pc.u = blockIdx.x;
+    if (pc.u < units) cursor_unit(pc, pa_);
+    for (; issued < kPipeStages && pc.u < units; ++issued) {
+      issue_chunk(pc, pa_, &vis_map, stage_mem, full, issued);
+      cursor_next(pc, pa_, units);
+    }
+  }
+  __syncthreads();
+
+  const int h = (lane >> 2) & 1;  // read order of the two 16-byte halves
+  const double kA = a.f0 / kSpeedOfLight, kB = a.df / kSpeedOfLight;
+  uint32_t it = 0;
+  bool ok = true;
+  for (int u = blockIdx.x; u < units && ok; u += gridDim.x) {
+    const int tile = u / (pa_.dgroups * pa_.nslab);
+    const int dg = (u / pa_.nslab) % pa_.dgroups;
+    const int slab = u % pa_.nslab;
+    const int ts = slab / a.n_cslab, cs = slab % a.n_cslab;
+    const int t_lo = ts * a.t_per_slab, t_hi = min(a.timesteps, t_lo + a.t_per_slab);
+    const int c_lo = cs * a.c_per_slab, c_hi = min(a.channels, c_lo + a.c_per_slab);
+    const int b = tile * 32 + lane;
+    const bool valid = b < a.nbl;
+    const int d0 = (dg * NC + warp) * DPW;
+    const bool active = d0 < a.ndir;
+
+    float sr[DPW][4], si[DPW][4], cr[DPW][4], ci[DPW][4];
+#pragma unroll
+    for (int j = 0; j < DPW; ++j)
+#pragma unroll
+      for (int q = 0; q < 4; ++q) sr[j][q] = si[j][q] = cr[j][q] = ci[j][q] = 0.f;
+
+    for (int t = t_lo; t < t_hi && ok; ++t) {
+      uint32_t pa[DPW], pb[DPW];
+      float wr[DPW], wi[DPW];
+      if (active) {
+        const int64_t r = static_cast<int64_t>(t) * a.nbl + (valid ? b : 0);
+        const double uu = __ldg(a.uvw + 3 * r), vv = __ldg(a.uvw + 3 * r + 1), ww = __ldg(a.uvw + 3 * r + 2);
+#pragma unroll
+        for (int j = 0; j < DPW; ++j) {
+          const int d = min(d0 + j, a.ndir - 1);
+          const double wrot = __ldg(a.dd + 9 * d + 6) * uu + __ldg(a.dd + 9 * d + 7) * vv + __ldg(a.dd + 9 * d + 8) * ww;
+          const double dw = wrot - ww;
+          pa[j] = frac_turns_u32(-dw * kA);
+          pb[j] = frac_turns_u32(-dw * kB);
+          twiddle_turns(pb[j], tab, wr[j], wi[j]);
+        }
+      }
+      for (int cb = c_lo; cb < c_hi; cb += kPipeChunk, ++it) {
+        const int n = min(kPipeChunk, c_hi - cb);
+        const int st = it % kPipeStages;
+        if (!mbar_wait_bounded(&full[st], (it / kPipeStages) & 1)) {
+          atomicOr(a.err, kDevErrTimeout);
+          ok = false;
+          break;
+        }
+        if (active) {
+          float pr[DPW][4], pi[DPW][4];
+          float zr[DPW], zi[DPW];
+#pragma unroll
+          for (int j = 0; j < DPW; ++j)
+#pragma unroll
+            for (int q = 0; q < 4; ++q) pr[j][q] = pi[j][q] = 0.f;
+          const unsigned char* src = stage_mem + st * kPipeStageBytes + lane * 32;
+          if (n == kPipeChunk) {
+#pragma unroll
+            for (int sub = 0; sub < kPipeChunk; sub += kPipeReseed) {
+#pragma unroll
+              for (int j = 0; j < DPW; ++j)
+                twiddle_turns(pa[j] + static_cast<uint32_t>(cb + sub) * pb[j], tab, zr[j], zi[j]);
+#pragma unroll
+              for (int k = 0; k < kPipeReseed; ++k)
+                mac_channel<DPW>(src + (sub + k) * kPipeItemBytes, h, pr, pi, zr, zi, wr, wi);
+            }
+          } else {
+            for (int k = 0; k < n; ++k) {
+              if (k % kPipeReseed == 0) {
+#pragma unroll
+                for (int j = 0; j < DPW; ++j)
+                  twiddle_turns(pa[j] + static_cast<uint32_t>(cb + k) * pb[j], tab, zr[j], zi[j]);
+              }
+              mac_channel<DPW>(src + k * kPipeItemBytes, h, pr, pi, zr, zi, wr, wi);
+            }
+          }
+#pragma unroll
+          for (int j = 0; j < DPW; ++j)
+#pragma unroll
+            for (int q = 0; q < 4; ++q) {
+              float y = pr[j][q] - cr[j][q];
+              float tt = sr[j][q] + y;
+              cr[j][q] = (tt - sr[j][q]) - y;
+              sr[j][q] = tt;
+              y = pi[j][q] - ci[j][q];
+              tt = si[j][q] + y;
+              ci[j][q] = (tt - si[j][q]) - y;
+              si[j][q] = tt;
+            }
+        }
+        __syncwarp();
+        if (lane == 0) mbar_arrive(&empty[st]);
+        if (producer && pc.u < units) {
+          // Refill this stage with the chunk kPipeStages ahead once every warp released it.
+          if (!mbar_wait_bounded(&empty[st], (it / kPipeStages) & 1)) {
+            atomicOr(a.err, kDevErrTimeout);
+            ok = false;
+          } else {
+            issue_chunk(pc, pa_, &vis_map, stage_mem, full, st);
+            cursor_next(pc, pa_, units);
+            ++issued;
+          }
+        }
+        __syncwarp();
+      }
+    }
+    if (ok && active && valid) {
+      const int64_t slab_off = static_cast<int64_t>(slab) * a.ndir * 4 * a.nbl;
+#pragma unroll
+      for (int j = 0; j < DPW; ++j) {
+        const int d = d0 + j;
+        if (d < a.ndir) {
+#pragma unroll
+          for (int q = 0; q < 4; ++q) {
+            const int p = q ^ (2 * h);
+            a.out[slab_off + (static_cast<int64_t>(d) * 4 + p) * a.nbl + b] =
+                make_double2(static_cast<double>(sr[j][q]) - static_cast<double>(cr[j][q]),
+                             static_cast<double>(si[j][q]) - static_cast<double>(ci[j][q]));
+          }
+        }
+      }
+    }
+  }
+  if (producer) {
+    // Do not leave while copies issued by this block may still land in shared memory.
+    for (uint32_t j = (issued > kPipeStages ? issued - kPipeStages : 0); j < issued; ++j)
+      if (!mbar_wait_bounded(&full[j % kPipeStages], (j / kPipeStages) & 1)) atomicOr(a.err, kDevErrTimeout);
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Reference-antenna baselines in FP64 (mixed form).  The solve reads pol 0 of
+// the |I1| baselines through the reference antenna with weight one (cal1 =
+// Ad1 * arg(avg[I1, 0])) and then multiplies cal1 by 2*pi, so an FP32 phase
+// error on one of them reaches every antenna's cal phase ~7x amplified; on
+// nearly cancelling sums FP32 products leave errors of 1e-6..1e-5 rad there.
+// These rows are therefore accumulated in FP64 (the all-FP64 recurrence of
+// rotate_average_fp64, pol 0 only), gathered by I1.  They are 1-2% of the rows
+// and use the FP64 pipe, which the FP32 bulk kernel leaves idle, so the call
+// launches this kernel on a second stream to overlap the two.
+// Output: [nslab][ndir][nI1] double2 (nslab == 1: final).
+// ---------------------------------------------------------------------------
+template <typename VisT, int DPW>
+__global__ void __launch_bounds__(128) refant_average_fp64(RotateArgs a, const int32_t* __restrict__ I1, int nI1,
+                                                          double2* __restrict__ out) {
+  constexpr int NW = 4;
+  constexpr int kSeed = 16;
+  const int lane = threadIdx.x & 31;
+  const int warp = threadIdx.x >> 5;
+  const int k = blockIdx.x * 32 + lane;
+  const int d0 = (blockIdx.y * NW + warp) * DPW;
+  const int slab = blockIdx.z;
+  const int ts = slab / a.n_cslab, cs = slab % a.n_cslab;
+  const int t_lo = ts * a.t_per_slab, t_hi = min(a.timesteps, t_lo + a.t_per_slab);
+  const int c_lo = cs * a.c_per_slab, c_hi = min(a.channels, c_lo + a.c_per_slab);
+  if (d0 >= a.ndir || k >= nI1) return;
+  int b = __ldg(I1 + k);
+  if (b < 0) b += a.nbl;  // VectorRangeSelect wrap-around (LA/math/cpu/vector.h:97-104)
+
+  double dd2[DPW][3];
+#pragma unroll
+  for (int j = 0; j < DPW; ++j) {
+    const int d = min(d0 + j, a.ndir - 1);
+    dd2[j][0] = __ldg(a.dd + 9 * d + 6);
+    dd2[j][1] = __ldg(a.dd + 9 * d + 7);
+    dd2[j][2] = __ldg(a.dd + 9 * d + 8);
+  }
+  double accr[DPW], acci[DPW];
+#pragma unroll
+  for (int j = 0; j < DPW; ++j) accr[j] = acci[j] = 0.0;
+  const double inv_c = 1.0 / kSpeedOfLight;
+  const VisT* vis = static_cast<const VisT*>(a.vis);
+  for (int t = t_lo; t < t_hi; ++t) {
+    const int64_t r = static_cast<int64_t>(t) * a.nbl + b;
+    const double u = __ldg(a.uvw + 3 * r), v = __ldg(a.uvw + 3 * r + 1), w = __ldg(a.uvw + 3 * r + 2);
+    double sf[DPW], wr[DPW], wi[DPW];
+#pragma unroll
+    for (int j = 0; j < DPW; ++j) {
+      const double wrot = dd2[j][0] * u + dd2[j][1] * v + dd2[j][2] * w;
+      sf[j] = -kTwoPi * (wrot - w);
+      sincos(sf[j] * (a.df * inv_c), &wi[j], &wr[j]);
+    }
+    for (int cb = c_lo; cb < c_hi; cb += kSeed) {
+      const int ce = min(c_hi, cb + kSeed);
+      double zr[DPW], zi[DPW];
+#pragma unroll
+      for (int j = 0; j < DPW; ++j) sincos(sf[j] / __ldg(a.lambda + cb), &zi[j], &zr[j]);
+      for (int c = cb; c < ce; ++c) {
+        double vr, vi;
+        load_sample(vis + (static_cast<int64_t>(c) * a.rows + r) * a.pols, vr, vi);
+#pragma unroll
+        for (int j = 0; j < DPW; ++j) {
+          accr[j] += vr * zr[j] - vi * zi[j];
+          acci[j] += vr * zi[j] + vi * zr[j];
+          const double nr = zr[j] * wr[j] - zi[j] * wi[j];
+          zi[j] = zr[j] * wi[j] + zi[j] * wr[j];
+          zr[j] = nr;
+        }
+      }
+    }
+  }
+  const int64_t slab_off = static_cast<int64_t>(slab) * a.ndir * nI1;
+#pragma unroll
+  for (int j = 0; j < DPW; ++j) {
+    const int d = d0 + j;
+    if (d < a.ndir) out[slab_off + static_cast<int64_t>(d) * nI1 + k] = make_double2(accr[j], acci[j]);
   }
 }
 

@@ -29,19 +29,27 @@ struct SolveArgs {
   int32_t Kpad;             // padded length of dphi rows
   double* cal1;             // [ndir][S]
   void* dphi;               // [ndir][Kpad] double (FP64) or float (mixed)
+  const double2* avg_i1;    // optional [ndir][A1rows-1]: FP64 pol-0 sums of the I1 baselines
 };
 
-// K3 + K4: phi1 and cal1 = Ad1 * phi1, one block per direction.
+// K3 + K4: phi1 and cal1 = Ad1 * phi1, one block per direction.  With FP64
+// sums of the I1 baselines (mixed form) those replace pol 0 of avgData first.
 __global__ void solve_cal1(SolveArgs a) {
   extern __shared__ double sphi[];
   const int d = blockIdx.x;
-  const double2* avg0 = a.avg + static_cast<int64_t>(d) * a.pols * a.nbl;  // pol 0 column
+  double2* avg0 = const_cast<double2*>(a.avg) + static_cast<int64_t>(d) * a.pols * a.nbl;  // pol 0 column
   for (int k = threadIdx.x; k < a.A1rows; k += blockDim.x) {
     double v = 0.0;
     if (k < a.A1rows - 1) {
       int idx = a.I1[k];
       if (idx < 0) idx += a.nbl;  // VectorRangeSelect wrap-around (LA/math/cpu/vector.h:97-104)
-      const double2 z = avg0[idx];
+      double2 z;
+      if (a.avg_i1) {
+        z = a.avg_i1[static_cast<int64_t>(d) * (a.A1rows - 1) + k];
+        avg0[idx] = z;  // duplicate I1 entries carry the same value
+      } else {
+        z = avg0[idx];
+      }
       v = atan2(z.y, z.x);
     }
     sphi[k] = v;

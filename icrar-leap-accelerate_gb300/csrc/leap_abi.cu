@@ -10,6 +10,8 @@
 #include <string>
 #include <vector>
 
+#include <cudaTypedefs.h>
+
 #include "leap_gb300.h"
 #include "host_math.h"
 #include "kernels_rotate.cuh"
@@ -47,7 +49,22 @@ struct Integration {
   int32_t vis_type = LEAP_VIS_C64;
   int64_t rows = 0;
   int32_t channels = 0, pols = 0;
+  bool has_map = false;
+  CUtensorMap vis_map;  // [channel][row*8 floats] view of a 4-pol complex<float> integration
 };
+
+// cuTensorMapEncodeTiled through the runtime's driver entry point (no libcuda link).
+PFN_cuTensorMapEncodeTiled_v12000 tensor_map_encoder() {
+  static PFN_cuTensorMapEncodeTiled_v12000 fn = [] {
+    void* f = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &f, 12000, cudaEnableDefault, &q) != cudaSuccess ||
+        q != cudaDriverEntryPointSuccess)
+      f = nullptr;
+    return reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(f);
+  }();
+  return fn;
+}
 
 struct Metadata {
   bool set = false;
@@ -60,12 +77,16 @@ struct Metadata {
 
 struct leap_ctx {
   int device = 0;
+  int sms = 152;
+  bool pipe_attr_set = false;
   cudaStream_t stream = nullptr;
   std::string err;
   Metadata md;
   std::map<int32_t, Integration> integ;
   // scratch, shared by calls on this context
-  DeviceBuffer partial, avg, cal1, dphi, gemm_partial, dd, cal, dev_err, lambda;
+  DeviceBuffer partial, avg, cal1, dphi, gemm_partial, dd, cal, dev_err, lambda, twiddle, partial_i1, avg_i1;
+  cudaStream_t aux = nullptr;           // second stream for the FP64 reference-antenna pass
+  cudaEvent_t fork = nullptr, join = nullptr;
   int last_ndir = 0, last_pols = 0, last_nbl = 0;
   std::vector<double> lambda_host;
   double lambda_f0 = 0.0, lambda_df = 0.0;
@@ -108,14 +129,18 @@ struct DeviceGuard {
   }
 };
 
+constexpr int kPipeNC = 8;  // consumer warps of the pipelined kernel (4 directions each)
+constexpr int kPipeSmem = kPipeStages * kPipeStageBytes + kTwiddleSize * sizeof(float2) +
+                          2 * kPipeStages * sizeof(uint64_t);
+
 int grid_1d(int64_t n, int threads) {
   int64_t b = (n + threads - 1) / threads;
   return static_cast<int>(std::min<int64_t>(std::max<int64_t>(b, 1), 152 * 32));
 }
 
-// Slab split of (timestep, channel) space so the grid covers the GPU.
-void choose_slabs(int timesteps, int channels, int64_t base_blocks, int& t_per, int& c_per, int& nts, int& ncs) {
-  const int64_t target = 152 * 8;
+// Slab split of (timestep, channel) space so that the grid reaches `target` blocks.
+void choose_slabs_target(int timesteps, int channels, int64_t base_blocks, int64_t target, int& t_per, int& c_per,
+                         int& nts, int& ncs) {
   int64_t want = std::max<int64_t>(1, (target + base_blocks - 1) / base_blocks);
   // Keep at least 64 (timestep, channel) pairs per slab.
   const int64_t max_slabs = std::max<int64_t>(1, (static_cast<int64_t>(timesteps) * channels) / 64);
@@ -127,6 +152,31 @@ void choose_slabs(int timesteps, int channels, int64_t base_blocks, int& t_per, 
   ncs = static_cast<int>(std::min<int64_t>(rest, std::max(1, channels / 16)));
   c_per = (channels + ncs - 1) / ncs;
   ncs = (channels + c_per - 1) / c_per;
+}
+
+// Slab split for the direct-load kernels: about 8 blocks per SM.
+void choose_slabs(int timesteps, int channels, int64_t base_blocks, int& t_per, int& c_per, int& nts, int& ncs) {
+  choose_slabs_target(timesteps, channels, base_blocks, 152 * 8, t_per, c_per, nts, ncs);
+}
+
+// Timestep slabs for the persistent pipelined kernel: the smallest split whose
+// unit count fills the persistent grid to >= 95% on the last round.
+void choose_pipe_slabs(int timesteps, int64_t base_units, int grid, int& t_per, int& nts) {
+  int best = 1;
+  double best_eff = 0.0;
+  for (int n = 1; n <= std::min(timesteps, 16); ++n) {
+    const int tp = (timesteps + n - 1) / n;
+    const int nn = (timesteps + tp - 1) / tp;
+    const int64_t u = base_units * nn;
+    const double eff = static_cast<double>(u) / (static_cast<double>(grid) * ((u + grid - 1) / grid));
+    if (eff > best_eff + 1e-9) {
+      best_eff = eff;
+      best = nn;
+    }
+    if (eff >= 0.95) break;
+  }
+  t_per = (timesteps + best - 1) / best;
+  nts = (timesteps + t_per - 1) / t_per;
 }
 
 template <typename VisT, int P>
@@ -165,12 +215,22 @@ int calibrate_impl(leap_ctx* ctx, int32_t slot, const double* d_dd, int32_t ndir
   const int32_t T = static_cast<int32_t>(in.rows / nbl);
   const int32_t C = in.channels;
 
-  // Launch shape: 32 baselines per warp, 4 warps per block.
+  // Launch shape: 32 baselines per warp.  The pipelined persistent kernel takes
+  // the 4-pol complex<float> mixed case; the direct-load kernels (4 warps per
+  // block) take every other shape.
+  const bool pipe = precision == LEAP_PRECISION_MIXED && P == 4 && in.vis_type == LEAP_VIS_C64 && in.has_map;
   const int dpw = precision == LEAP_PRECISION_FP64 ? 2 : 4;
   const int tiles = (nbl + 31) / 32;
   const int dgroups = (ndir + 4 * dpw - 1) / (4 * dpw);
+  const int pipe_dgroups = (ndir + kPipeNC * 4 - 1) / (kPipeNC * 4);
   int t_per, c_per, nts, ncs;
-  choose_slabs(T, C, static_cast<int64_t>(tiles) * dgroups, t_per, c_per, nts, ncs);
+  if (pipe) {
+    choose_pipe_slabs(T, static_cast<int64_t>(tiles) * pipe_dgroups, ctx->sms, t_per, nts);
+    c_per = C;
+    ncs = 1;
+  } else {
+    choose_slabs(T, C, static_cast<int64_t>(tiles) * dgroups, t_per, c_per, nts, ncs);
+  }
   const int nslab = nts * ncs;
   const int64_t avg_elems = static_cast<int64_t>(ndir) * P * nbl;
 
@@ -200,6 +260,7 @@ int calibrate_impl(leap_ctx* ctx, int32_t slot, const double* d_dd, int32_t ndir
   ra.uvw = in.uvw.as<double>();
   ra.dd = d_dd;
   ra.lambda = ctx->lambda.as<double>();
+  ra.twiddle = ctx->twiddle.as<float2>();
   ra.rows = in.rows;
   ra.channels = C;
   ra.pols = P;
@@ -218,11 +279,64 @@ int calibrate_impl(leap_ctx* ctx, int32_t slot, const double* d_dd, int32_t ndir
   int kernels = 0;
   cudaEvent_t* ev = ctx->ring[ctx->ring_count % leap_ctx::kRing];
   cudaEventRecord(ev[0], s);
-  const dim3 grid(tiles, dgroups, nslab);
-  int rc = in.vis_type == LEAP_VIS_C64 ? dispatch_pols<float2>(ra, grid, precision, s)
-                                       : dispatch_pols<double2>(ra, grid, precision, s);
-  if (rc != 0) return fail(ctx, LEAP_ERR_INVALID_ARGUMENT, "unsupported polarisation count (1, 2 or 4)");
+
+  const int nI1 = md.A1rows - 1;
+  const bool refant = precision == LEAP_PRECISION_MIXED && nI1 > 0;
+  if (refant) LEAP_CUDA(cudaEventRecord(ctx->fork, s), "fork");
+  if (pipe) {
+    PipeArgs pa{};
+    pa.a = ra;
+    pa.tiles = tiles;
+    pa.dgroups = pipe_dgroups;
+    pa.nslab = nslab;
+    const int units = tiles * pipe_dgroups * nslab;
+    const int grid = std::min(units, ctx->sms);
+    if (!ctx->pipe_attr_set) {
+      LEAP_CUDA(cudaFuncSetAttribute(rotate_average_mixed_pipe<kPipeNC, 4>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                     kPipeSmem), "set shared memory size");
+      ctx->pipe_attr_set = true;
+    }
+    rotate_average_mixed_pipe<kPipeNC, 4><<<grid, kPipeNC * 32, kPipeSmem, s>>>(in.vis_map, pa);
+  } else {
+    const dim3 grid(tiles, dgroups, nslab);
+    int rc = in.vis_type == LEAP_VIS_C64 ? dispatch_pols<float2>(ra, grid, precision, s)
+                                         : dispatch_pols<double2>(ra, grid, precision, s);
+    if (rc != 0) return fail(ctx, LEAP_ERR_INVALID_ARGUMENT, "unsupported polarisation count (1, 2 or 4)");
+  }
   ++kernels;
+  // Mixed form: FP64 sums of pol 0 of the reference-antenna baselines, on the
+  // aux stream so that the FP64 pipe works while the FP32 bulk kernel runs.
+  if (refant) {
+    // About one block per SM: launched after the persistent bulk kernel, each
+    // block fits beside a bulk block (registers) and keeps the FP64 pipe busy.
+    int rt_per, rc_per, rnts, rncs;
+    const int rtiles = (nI1 + 31) / 32;
+    const int rdg = (ndir + 4 * 2 - 1) / (4 * 2);
+    choose_slabs_target(T, C, static_cast<int64_t>(rtiles) * rdg, ctx->sms, rt_per, rc_per, rnts, rncs);
+    const int rslab = rnts * rncs;
+    const int64_t n_i1 = static_cast<int64_t>(ndir) * nI1;
+    LEAP_CUDA(ctx->avg_i1.ensure(sizeof(double2) * n_i1), "alloc I1 sums");
+    if (rslab > 1) LEAP_CUDA(ctx->partial_i1.ensure(sizeof(double2) * n_i1 * rslab), "alloc I1 partials");
+    RotateArgs rr = ra;
+    rr.t_per_slab = rt_per;
+    rr.c_per_slab = rc_per;
+    rr.n_tslab = rnts;
+    rr.n_cslab = rncs;
+    LEAP_CUDA(cudaStreamWaitEvent(ctx->aux, ctx->fork, 0), "fork");
+    double2* dst = rslab > 1 ? ctx->partial_i1.as<double2>() : ctx->avg_i1.as<double2>();
+    const dim3 rgrid(rtiles, rdg, rslab);
+    if (in.vis_type == LEAP_VIS_C64)
+      refant_average_fp64<float2, 2><<<rgrid, 128, 0, ctx->aux>>>(rr, md.I1.as<int32_t>(), nI1, dst);
+    else
+      refant_average_fp64<double2, 2><<<rgrid, 128, 0, ctx->aux>>>(rr, md.I1.as<int32_t>(), nI1, dst);
+    ++kernels;
+    if (rslab > 1) {
+      reduce_slabs<<<grid_1d(n_i1, 256), 256, 0, ctx->aux>>>(ctx->partial_i1.as<double2>(), rslab, n_i1,
+                                                             ctx->avg_i1.as<double2>());
+      ++kernels;
+    }
+    LEAP_CUDA(cudaEventRecord(ctx->join, ctx->aux), "join");
+  }
   if (nslab > 1) {
     reduce_slabs<<<grid_1d(avg_elems, 256), 256, 0, s>>>(ctx->partial.as<double2>(), nslab, avg_elems,
                                                             ctx->avg.as<double2>());
@@ -245,6 +359,8 @@ int calibrate_impl(leap_ctx* ctx, int32_t slot, const double* d_dd, int32_t ndir
   sa.Kpad = md.Kpad;
   sa.cal1 = ctx->cal1.as<double>();
   sa.dphi = ctx->dphi.ptr;
+  sa.avg_i1 = refant ? ctx->avg_i1.as<double2>() : nullptr;
+  if (refant) LEAP_CUDA(cudaStreamWaitEvent(s, ctx->join, 0), "join");
   solve_cal1<<<ndir, 256, sizeof(double) * md.A1rows, s>>>(sa);
   ++kernels;
   const dim3 gd((md.Kpad + 255) / 256, ndir);
@@ -315,11 +431,24 @@ int32_t leap_create(int32_t device, leap_ctx** out) {
   ctx->device = device;
   int rc = [&]() -> int {
     DeviceGuard g(device);
+    LEAP_CUDA(cudaDeviceGetAttribute(&ctx->sms, cudaDevAttrMultiProcessorCount, device), "query SM count");
     LEAP_CUDA(cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking), "create stream");
+    LEAP_CUDA(cudaStreamCreateWithFlags(&ctx->aux, cudaStreamNonBlocking), "create aux stream");
+    LEAP_CUDA(cudaEventCreateWithFlags(&ctx->fork, cudaEventDisableTiming), "create event");
+    LEAP_CUDA(cudaEventCreateWithFlags(&ctx->join, cudaEventDisableTiming), "create event");
     for (auto& tri : ctx->ring)
       for (auto& ev : tri) LEAP_CUDA(cudaEventCreate(&ev), "create event");
     LEAP_CUDA(ctx->dev_err.ensure(sizeof(int)), "alloc error word");
     LEAP_CUDA(cudaMemset(ctx->dev_err.ptr, 0, sizeof(int)), "clear error word");
+    // (cos, sin) of 2*pi*i/kTwiddleSize, FP64 rounded once to FP32.
+    std::vector<float2> tw(kTwiddleSize);
+    for (int i = 0; i < kTwiddleSize; ++i) {
+      const double ang = kTwoPi * static_cast<double>(i) / kTwiddleSize;
+      tw[i] = make_float2(static_cast<float>(std::cos(ang)), static_cast<float>(std::sin(ang)));
+    }
+    LEAP_CUDA(ctx->twiddle.ensure(sizeof(float2) * kTwiddleSize), "alloc twiddle table");
+    LEAP_CUDA(cudaMemcpy(ctx->twiddle.ptr, tw.data(), sizeof(float2) * kTwiddleSize, cudaMemcpyHostToDevice),
+              "upload twiddle table");
     return LEAP_OK;
   }();
   if (rc != LEAP_OK) {
@@ -344,10 +473,16 @@ void leap_destroy(leap_ctx* ctx) {
     md.I1.release(); md.Ad1.release(); md.Ad.release(); md.Ad_f32.release(); md.arow.release(); md.arow_val.release();
     ctx->partial.release(); ctx->avg.release(); ctx->cal1.release(); ctx->dphi.release();
     ctx->gemm_partial.release(); ctx->dd.release(); ctx->cal.release(); ctx->dev_err.release(); ctx->lambda.release();
+    ctx->twiddle.release();
     for (auto& tri : ctx->ring)
       for (auto& ev : tri)
         if (ev) cudaEventDestroy(ev);
     if (ctx->stream) cudaStreamDestroy(ctx->stream);
+    if (ctx->aux) cudaStreamDestroy(ctx->aux);
+    if (ctx->fork) cudaEventDestroy(ctx->fork);
+    if (ctx->join) cudaEventDestroy(ctx->join);
+    ctx->partial_i1.release();
+    ctx->avg_i1.release();
   }
   delete ctx;
 }
@@ -448,6 +583,21 @@ int32_t leap_set_integration(leap_ctx* ctx, int32_t slot, int32_t vis_type, cons
   in.rows = rows;
   in.channels = channels;
   in.pols = pols;
+  in.has_map = false;
+  if (vis_type == LEAP_VIS_C64 && pols == 4 && rows * 8 < (int64_t(1) << 31)) {
+    // The pipelined kernel's view: 2-D floats [channels][rows*8], box 256 x kPipeChunk.
+    auto enc = tensor_map_encoder();
+    if (!enc) return fail(ctx, LEAP_ERR_CUDA, "cuTensorMapEncodeTiled unavailable");
+    cuuint64_t dims[2] = {static_cast<cuuint64_t>(rows) * 8, static_cast<cuuint64_t>(channels)};
+    cuuint64_t strides[1] = {static_cast<cuuint64_t>(rows) * 32};
+    cuuint32_t box[2] = {256, static_cast<cuuint32_t>(kPipeChunk)};
+    cuuint32_t estr[2] = {1, 1};
+    CUresult r = enc(&in.vis_map, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 2, in.vis.ptr, dims, strides, box, estr,
+                     CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+                     CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+    if (r != CUDA_SUCCESS) return fail(ctx, LEAP_ERR_CUDA, "cuTensorMapEncodeTiled failed: " + std::to_string(r));
+    in.has_map = true;
+  }
   return LEAP_OK;
 }
 

@@ -2,6 +2,7 @@
 #pragma once
 
 #include <cstdint>
+#include <cuda.h>
 #include <cuda_runtime.h>
 
 namespace leapgb {
@@ -61,6 +62,17 @@ __device__ __forceinline__ bool mbar_wait_bounded(uint64_t* bar, uint32_t parity
   return false;
 }
 
+// Two-dimensional tiled TMA load global -> shared through a tensor map,
+// completing on an mbarrier.  x (the inner coordinate, in elements) times the
+// element size must be a multiple of 16 bytes.
+__device__ __forceinline__ void tma_load_2d(void* smem_dst, const CUtensorMap* map, int x, int y, uint64_t* bar) {
+  asm volatile(
+      "cp.async.bulk.tensor.2d.shared::cluster.global.tile.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3}], [%4];" ::"r"(
+          smem_u32(smem_dst)),
+      "l"(map), "r"(x), "r"(y), "r"(smem_u32(bar))
+      : "memory");
+}
+
 // One-dimensional bulk copy global -> shared, completing on an mbarrier
 // (cp.async.bulk; both addresses 16-byte aligned, size a multiple of 16).
 __device__ __forceinline__ void bulk_copy_g2s(void* smem_dst, const void* gmem_src, uint32_t bytes,
@@ -72,28 +84,26 @@ __device__ __forceinline__ void bulk_copy_g2s(void* smem_dst, const void* gmem_s
       : "memory");
 }
 
-// ---- packed FP32x2 arithmetic (sm_100+) ----
-__device__ __forceinline__ unsigned long long pack2(float lo, float hi) {
-  unsigned long long r;
-  asm("mov.b64 %0, {%1, %2};" : "=l"(r) : "f"(lo), "f"(hi));
-  return r;
-}
-__device__ __forceinline__ void unpack2(unsigned long long v, float& lo, float& hi) {
-  asm("mov.b64 {%0, %1}, %2;" : "=f"(lo), "=f"(hi) : "l"(v));
-}
-__device__ __forceinline__ unsigned long long ffma2(unsigned long long a, unsigned long long b,
-                                                    unsigned long long c) {
-  unsigned long long d;
-  asm("fma.rn.f32x2 %0, %1, %2, %3;" : "=l"(d) : "l"(a), "l"(b), "l"(c));
-  return d;
-}
+// Twiddle table: kTwiddleBits-bit index of a turn -> (cos, sin) of 2*pi*i/2^kTwiddleBits,
+// rounded to FP32 from FP64 values on the host.
+constexpr int kTwiddleBits = 10;
+constexpr int kTwiddleSize = 1 << kTwiddleBits;
 
-// Phase in turns held as an unsigned 32-bit fraction of a turn -> angle in [-pi, pi).
-// The top 23 bits (with the sign bit flipped, i.e. +half a turn) become the
-// mantissa of a float in [1, 2); 2*pi*(f - 1.5) is then the angle.
-__device__ __forceinline__ float turns_u32_to_angle(uint32_t turns) {
-  const uint32_t bits = ((turns >> 9) ^ 0x00400000u) | 0x3F800000u;
-  return fmaf(__uint_as_float(bits), 6.28318530717958647692f, -9.42477796076937971538f);
+// exp(2*pi*i*turns) for a 32-bit fixed-point fraction of a turn, to about 1e-7
+// absolute: the top kTwiddleBits bits pick a table entry; the remaining 22 bits
+// are an angle delta in [0, 2*pi/1024) (exact in a float mantissa), whose sine
+// and cosine are the first Taylor terms (truncation below 6e-11); the table
+// entry is then rotated by delta.  The table lives in shared memory.
+__device__ __forceinline__ void twiddle_turns(uint32_t turns, const float2* __restrict__ tab, float& c, float& s) {
+  constexpr float kStep = 6.28318530717958647692f / kTwiddleSize;
+  const float2 t = tab[turns >> (32 - kTwiddleBits)];
+  const uint32_t fbits = ((turns << kTwiddleBits) >> 9) | 0x3F800000u;
+  const float d = fmaf(__uint_as_float(fbits), kStep, -kStep);
+  const float d2 = d * d;
+  const float cd = fmaf(d2, -0.5f, 1.0f);
+  const float sd = d * fmaf(d2, -0.16666667f, 1.0f);
+  c = fmaf(t.x, cd, -t.y * sd);
+  s = fmaf(t.y, cd, t.x * sd);
 }
 
 // Fractional part of x (turns) as a rounded 2^-32 fixed-point value.

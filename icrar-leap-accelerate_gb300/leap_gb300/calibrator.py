@@ -226,7 +226,7 @@ class Context:
     def calibrate(self, slot: int, dds: np.ndarray, precision: int = _abi.LEAP_PRECISION_FP64) -> np.ndarray:
         dds = np.ascontiguousarray(dds, dtype=np.float64).reshape(-1, 9)
         D = dds.shape[0]
-        S = self.md.A.shape[1]
+        S = self.md.A.shape[1] if self.md is not None else 1
         cal = np.zeros((D, S), dtype=np.float64)
         self._check(lib.leap_calibrate(self._h, slot, _ptr(dds), D, precision, _ptr(cal)))
         self._last_slot = slot

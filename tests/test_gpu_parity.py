@@ -172,3 +172,18 @@ def test_error_paths(ctx):
     with pytest.raises(lg.InvalidArgument):
         fresh.calibrate(0, np.eye(3)[None], 7)  # unknown precision
     fresh.close()
+
+
+@pytest.mark.parametrize("stations,timesteps,channels,ndir", [(64, 9, 23, 40), (33, 5, 5, 3), (12, 20, 48, 70)])
+def test_mixed_pipelined_edges(ctx, stations, timesteps, channels, ndir):
+    """4-pol complex<float> shapes that hit partial 32-baseline tiles, partial
+    16-channel chunks, several direction groups and several timestep slabs."""
+    obs, dirs = synth.small_case(stations=stations, timesteps=timesteps, channels=channels, directions=ndir,
+                                 vis_dtype=np.complex64, seed_shift=stations)
+    md, mdo, dds, cal, cal_o, avg_o = run_case(ctx, obs, dirs, lg.LEAP_PRECISION_MIXED)
+    assert_cal_close(cal, cal_o, avg_o, mdo, MIXED_CAL_TOL, 1e-4)
+    # avgData of the bulk kernel (all pols) against the oracle, relative to the sum of |terms|
+    scale = np.abs(obs.vis).sum(axis=0).reshape(timesteps, obs.nbaselines, 4).sum(axis=0)
+    for d in range(0, ndir, max(1, ndir // 4)):
+        err = np.abs(ctx.avgdata(d) - avg_o[d]) / np.maximum(scale, 1e-30)
+        assert err.max() < 2e-6
