@@ -64,7 +64,9 @@ __device__ __forceinline__ void load_sample_f(const VisT* __restrict__ p, float&
 // kSeed channels (drift below 1e-14 rad).  FP64 sincos runs at about 1/25 of
 // the DFMA rate on GB300, so this removes it from the inner loop.
 // ---------------------------------------------------------------------------
-template <typename VisT, int P, int DPW>
+// kCheckNan: skip (row, channel) groups with a NaN in any pol inside the kernel
+// (for callers whose visibilities did not go through the ingestion sanitiser).
+template <typename VisT, int P, int DPW, bool kCheckNan = false>
 __global__ void __launch_bounds__(128) rotate_average_fp64(RotateArgs a) {
   constexpr int NW = 4;
   constexpr int kSeed = 16;
@@ -116,6 +118,15 @@ __global__ void __launch_bounds__(128) rotate_average_fp64(RotateArgs a) {
           double vr[P], vi[P];
 #pragma unroll
           for (int p = 0; p < P; ++p) load_sample(src + p, vr[p], vi[p]);
+          if (kCheckNan) {
+            bool nan = false;
+#pragma unroll
+            for (int p = 0; p < P; ++p) nan |= isnan(vr[p]) || isnan(vi[p]);
+            if (nan) {
+#pragma unroll
+              for (int p = 0; p < P; ++p) vr[p] = vi[p] = 0.0;
+            }
+          }
 #pragma unroll
           for (int j = 0; j < DPW; ++j) {
 #pragma unroll
@@ -584,7 +595,7 @@ __global__ void __launch_bounds__(128) refant_average_fp64(RotateArgs a, const i
 }
 
 // Sum of slab partials in slab order: avg[i] = sum_s partial[s][i].
-__global__ void reduce_slabs(const double2* __restrict__ partial, int nslab, int64_t n, double2* __restrict__ avg) {
+static __global__ void reduce_slabs(const double2* __restrict__ partial, int nslab, int64_t n, double2* __restrict__ avg) {
   for (int64_t i = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x; i < n;
        i += static_cast<int64_t>(gridDim.x) * blockDim.x) {
     double re = 0.0, im = 0.0;
@@ -642,7 +653,7 @@ __global__ void sanitize_nan_groups_generic(const VisT* __restrict__ src, VisT* 
 
 // K1: rotated[d][r] = dd[d] * uvw[r]  (MetaData::CalcUVW, LA/model/cpu/MetaData.cc:220-229;
 // g_RotateUVW, LA/algorithm/cuda/CudaLeapCalibrator.cu:271-282).
-__global__ void rotate_uvw(const double* __restrict__ dd, const double* __restrict__ uvw, int64_t rows, int ndir,
+static __global__ void rotate_uvw(const double* __restrict__ dd, const double* __restrict__ uvw, int64_t rows, int ndir,
                            double* __restrict__ out) {
   const int64_t total = rows * ndir;
   for (int64_t i = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x; i < total;

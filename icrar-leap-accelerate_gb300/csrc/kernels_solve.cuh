@@ -34,7 +34,7 @@ struct SolveArgs {
 
 // K3 + K4: phi1 and cal1 = Ad1 * phi1, one block per direction.  With FP64
 // sums of the I1 baselines (mixed form) those replace pol 0 of avgData first.
-__global__ void solve_cal1(SolveArgs a) {
+static __global__ void solve_cal1(SolveArgs a) {
   extern __shared__ double sphi[];
   const int d = blockIdx.x;
   double2* avg0 = const_cast<double2*>(a.avg) + static_cast<int64_t>(d) * a.pols * a.nbl;  // pol 0 column
@@ -63,7 +63,7 @@ __global__ void solve_cal1(SolveArgs a) {
 }
 
 // K5 + K6-prep: dphi[d][n] for n < Kpad (zero past |I|).  FP64 form.
-__global__ void solve_dint_fp64(SolveArgs a) {
+static __global__ void solve_dint_fp64(SolveArgs a) {
   const int d = blockIdx.y;
   const int n = blockIdx.x * blockDim.x + threadIdx.x;
   if (n >= a.Kpad) return;
@@ -84,7 +84,7 @@ __global__ void solve_dint_fp64(SolveArgs a) {
 }
 
 // Mixed form: the same in FP32 after the FP64 reduction of A*cal1's argument.
-__global__ void solve_dint_mixed(SolveArgs a) {
+static __global__ void solve_dint_mixed(SolveArgs a) {
   const int d = blockIdx.y;
   const int n = blockIdx.x * blockDim.x + threadIdx.x;
   if (n >= a.Kpad) return;
@@ -109,7 +109,7 @@ __global__ void solve_dint_mixed(SolveArgs a) {
 // K6: partial[kc][d][s] = sum_{k in chunk kc} Ad[s, k] * dphi[d][k].
 // Block tile: 64 stations x 16 directions, 256 threads, 4 outputs per thread.
 template <typename T>
-__global__ void __launch_bounds__(256) gemm_ad_partial(const T* __restrict__ Ad, int S, int Arows,
+static __global__ void __launch_bounds__(256) gemm_ad_partial(const T* __restrict__ Ad, int S, int Arows,
                                                        const T* __restrict__ dphi, int Kpad, int ndir,
                                                        int kchunk, double* __restrict__ partial) {
   constexpr int TS = 64, TD = 16, TK = 32;
@@ -150,7 +150,7 @@ __global__ void __launch_bounds__(256) gemm_ad_partial(const T* __restrict__ Ad,
 }
 
 // cal[d][s] = sum_kc partial[kc][d][s] (fixed order) + cal1[d][s].
-__global__ void gemm_ad_finish(const double* __restrict__ partial, int nk, int ndir, int S,
+static __global__ void gemm_ad_finish(const double* __restrict__ partial, int nk, int ndir, int S,
                                const double* __restrict__ cal1, double* __restrict__ cal) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   const int n = ndir * S;

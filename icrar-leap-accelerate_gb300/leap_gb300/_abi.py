@@ -26,6 +26,7 @@ LEAP_PRECISION_FP64 = 0
 LEAP_PRECISION_MIXED = 1
 LEAP_MEMORY_HOST = 0
 LEAP_MEMORY_DEVICE = 1
+LEAP_NOALLOC_SCRATCH_BYTES = 16 * 1024 * 1024
 
 # Every entry point include/leap_gb300.h declares, with its ctypes signature.
 i32, i64, f64, vp = ctypes.c_int32, ctypes.c_int64, ctypes.c_double, ctypes.c_void_p
@@ -63,6 +64,8 @@ SIGNATURES = {
     "leap_get_timings": ([vp, ctypes.POINTER(LeapTimings)], i32),
     "leap_timing_reset": ([vp], i32),
     "leap_synchronize": ([vp], i32),
+    "leap_rotate_average_noalloc": ([i32, vp, vp, i64, i32, i32, i32, f64, f64, vp, i32, vp, vp], i32),
+    "leap_noalloc_last_error": ([], ctypes.c_char_p),
     "leap_dd_matrix": ([f64, f64, f64, f64, vp], None),
     "leap_phase_matrix": ([vp, vp, vp, i32, i32, vp, vp, ctypes.POINTER(i32), ctypes.POINTER(i32)], i32),
     "leap_pseudo_inverse": ([vp, i32, i32, vp], i32),

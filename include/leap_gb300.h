@@ -153,6 +153,44 @@ int32_t leap_timing_reset(leap_ctx* ctx);
 /* Block until the context's stream is idle and report any device-side error. */
 int32_t leap_synchronize(leap_ctx* ctx);
 
+/* ---- entry point that allocates no device memory ---- */
+
+/* Size of the library's built-in scratch array (16 MiB), held on every GPU that
+ * loads the library until the process exits. */
+#define LEAP_NOALLOC_SCRATCH_BYTES (16u * 1024u * 1024u)
+
+/* This entry point has no counterpart in the reference.  It is for callers that
+ * must not allocate device memory while they run: code that builds or replays a
+ * CUDA graph (cudaMalloc is not allowed between stream-capture begin and end),
+ * hosts whose device memory is owned by another runtime's pool or arena and
+ * hands this library only pre-allocated buffers, and real-time pipelines that
+ * cannot take the latency or fragmentation of an allocation.
+ *
+ * It computes the all-FP64 rotate + average stage (RotateVisibilities,
+ * LA/algorithm/cpu/CpuLeapCalibrator.cc:181-217) of one integration for
+ * ndirections directions into avg_out, [ndirections][pols][nbl] complex
+ * doubles (the layout of leap_get_avgdata).  vis, uvw, dd and avg_out are
+ * DEVICE pointers on the current device, in the layouts above; (row, channel)
+ * groups with a NaN in any pol are skipped inside the kernel.  The call only
+ * launches kernels on `stream` (NULL: the default stream) and does not wait.
+ *
+ * Its scratch (wavelength table and partial sums) is one array of
+ * LEAP_NOALLOC_SCRATCH_BYTES per device; sizes that cannot fit (more than
+ * about two million channels) are rejected with LEAP_ERR_INVALID_ARGUMENT, and
+ * large workloads use fewer partial-sum slabs.  All calls on a device share the
+ * array, so calls that overlap on the GPU (different streams, or several host
+ * threads) race and must be serialised by the caller.  The first call on each
+ * device, with that device current, looks up the array's device address
+ * (cudaGetSymbolAddress); make that first call before any stream capture.
+ * Error text: leap_noalloc_last_error(). */
+int32_t leap_rotate_average_noalloc(int32_t vis_type, const void* vis, const double* uvw, int64_t rows,
+                                    int32_t channels, int32_t pols, int32_t nbl, double freq_start_hz,
+                                    double freq_inc_hz, const double* dd, int32_t ndirections, double* avg_out,
+                                    void* stream);
+
+/* Message of the last failure of leap_rotate_average_noalloc on this thread. */
+const char* leap_noalloc_last_error(void);
+
 /* ---- host helpers (FP64, no device needed) ---- */
 
 /* MetaData::GenerateDDMatrix (LA/model/cpu/MetaData.cc:166-203). */
