@@ -594,6 +594,122 @@ __global__ void __launch_bounds__(128) refant_average_fp64(RotateArgs a, const i
   }
 }
 
+// ---------------------------------------------------------------------------
+// Reference-antenna baselines in compensated FP32 (mixed form, complex<float>
+// input).  Same sums as refant_average_fp64, at about 1e-9 relative per term,
+// on the FP32 pipe (GB300's FP64 rate is ~1/70 of FP32):
+//  * phase: 64-bit fixed-point turns  pa + c*pb  (from FP64 A, B per timestep);
+//  * twiddle: the top 10 bits pick a (cos, sin) entry held as (hi, lo) float
+//    pairs (df_tab), the next 24 bits give delta < 2*pi/1024, and
+//    z = entry * (1 - delta^2/2 + i*(delta - delta^3/6)) is formed as entry_hi
+//    plus a correction (absolute error ~5e-10) and renormalised with TwoSum so
+//    that the low part is below one FP32 ulp;
+//  * product v*z_hi is exact (TwoProd), v*z_lo is rounded (error <= 4e-10 |v|),
+//    and the running sum is a TwoSum pair, so the sum carries no FP32 rounding.
+// ---------------------------------------------------------------------------
+struct DfAcc {
+  float s, c;  // value = s + c
+};
+
+// Knuth's TwoSum: a + b = s + e exactly.
+__device__ __forceinline__ void two_sum(float a, float b, float& s, float& e) {
+  s = a + b;
+  const float bb = s - a;
+  e = (a - (s - bb)) + (b - bb);
+}
+
+__device__ __forceinline__ void df_add_product(DfAcc& acc, float x, float yh, float yl) {
+  const float p = x * yh;
+  const float e = fmaf(x, yh, -p);       // x*yh = p + e exactly
+  const float sum = acc.s + p;           // TwoSum(acc.s, p)
+  const float bb = sum - acc.s;
+  const float err = (acc.s - (sum - bb)) + (p - bb);
+  acc.s = sum;
+  acc.c += err + fmaf(x, yl, e);
+}
+
+__device__ __forceinline__ void df_twiddle(uint64_t turns, const float4* __restrict__ tab, float& zrh, float& zrl,
+                                           float& zih, float& zil) {
+  const float4 t = tab[turns >> 54];                                   // (cos_hi, cos_lo, sin_hi, sin_lo)
+  const uint32_t r24 = static_cast<uint32_t>(turns >> 30) & 0xFFFFFFu;
+  const float d = __uint2float_rn(r24) * 3.657295198167899e-10f;     // 2*pi / 2^34
+  const float d2 = d * d;
+  const float c2 = 0.5f * d2;                                          // 1 - cos(d) (d^4/24 < 6e-11 dropped)
+  const float sd = d * fmaf(d2, -0.16666667f, 1.0f);                   // sin(d)
+  const float lr = fmaf(-t.x, c2, fmaf(-t.z, sd, t.y));  // z_re - entry_hi
+  const float li = fmaf(-t.z, c2, fmaf(t.x, sd, t.w));   // z_im - entry_hi
+  two_sum(t.x, lr, zrh, zrl);
+  two_sum(t.z, li, zih, zil);
+}
+
+// Fractional part of x (turns) as a 2^-64 fixed-point value.
+__device__ __forceinline__ uint64_t frac_turns_u64(double x) {
+  const double f = x - rint(x);  // in [-0.5, 0.5]
+  return static_cast<uint64_t>(static_cast<long long>(rint(f * 9223372036854775808.0))) << 1;
+}
+
+template <int DPW>
+__global__ void __launch_bounds__(128) refant_average_df(RotateArgs a, const int32_t* __restrict__ I1, int nI1,
+                                                        const float4* __restrict__ df_tab, double2* __restrict__ out) {
+  __shared__ float4 tab[kTwiddleSize];
+  for (int i = threadIdx.x; i < kTwiddleSize; i += blockDim.x) tab[i] = __ldg(df_tab + i);
+  __syncthreads();
+  constexpr int NW = 4;
+  const int lane = threadIdx.x & 31;
+  const int warp = threadIdx.x >> 5;
+  const int k = blockIdx.x * 32 + lane;
+  const int d0 = (blockIdx.y * NW + warp) * DPW;
+  const int slab = blockIdx.z;
+  const int ts = slab / a.n_cslab, cs = slab % a.n_cslab;
+  const int t_lo = ts * a.t_per_slab, t_hi = min(a.timesteps, t_lo + a.t_per_slab);
+  const int c_lo = cs * a.c_per_slab, c_hi = min(a.channels, c_lo + a.c_per_slab);
+  if (d0 >= a.ndir || k >= nI1) return;
+  int b = __ldg(I1 + k);
+  if (b < 0) b += a.nbl;  // VectorRangeSelect wrap-around (LA/math/cpu/vector.h:97-104)
+
+  const double kA = a.f0 / kSpeedOfLight, kB = a.df / kSpeedOfLight;
+  DfAcc re[DPW], im[DPW];
+#pragma unroll
+  for (int j = 0; j < DPW; ++j) re[j] = im[j] = DfAcc{0.f, 0.f};
+  const float2* vis = static_cast<const float2*>(a.vis);
+  for (int t = t_lo; t < t_hi; ++t) {
+    const int64_t r = static_cast<int64_t>(t) * a.nbl + b;
+    const double uu = __ldg(a.uvw + 3 * r), vv = __ldg(a.uvw + 3 * r + 1), ww = __ldg(a.uvw + 3 * r + 2);
+    uint64_t pa[DPW], pb[DPW];
+#pragma unroll
+    for (int j = 0; j < DPW; ++j) {
+      const int d = min(d0 + j, a.ndir - 1);
+      const double wrot = __ldg(a.dd + 9 * d + 6) * uu + __ldg(a.dd + 9 * d + 7) * vv + __ldg(a.dd + 9 * d + 8) * ww;
+      const double dw = wrot - ww;
+      pa[j] = frac_turns_u64(-dw * kA);
+      pb[j] = frac_turns_u64(-dw * kB);
+    }
+    const float2* src = vis + r * a.pols;
+#pragma unroll 4
+    for (int c = c_lo; c < c_hi; ++c) {
+      const float2 v = __ldg(src + static_cast<int64_t>(c) * a.rows * a.pols);
+#pragma unroll
+      for (int j = 0; j < DPW; ++j) {
+        float zrh, zrl, zih, zil;
+        df_twiddle(pa[j] + static_cast<uint64_t>(c) * pb[j], tab, zrh, zrl, zih, zil);
+        df_add_product(re[j], v.x, zrh, zrl);
+        df_add_product(re[j], -v.y, zih, zil);
+        df_add_product(im[j], v.x, zih, zil);
+        df_add_product(im[j], v.y, zrh, zrl);
+      }
+    }
+  }
+  const int64_t slab_off = static_cast<int64_t>(slab) * a.ndir * nI1;
+#pragma unroll
+  for (int j = 0; j < DPW; ++j) {
+    const int d = d0 + j;
+    if (d < a.ndir)
+      out[slab_off + static_cast<int64_t>(d) * nI1 + k] =
+          make_double2(static_cast<double>(re[j].s) + static_cast<double>(re[j].c),
+                       static_cast<double>(im[j].s) + static_cast<double>(im[j].c));
+  }
+}
+
 // Sum of slab partials in slab order: avg[i] = sum_s partial[s][i].
 static __global__ void reduce_slabs(const double2* __restrict__ partial, int nslab, int64_t n, double2* __restrict__ avg) {
   for (int64_t i = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x; i < n;

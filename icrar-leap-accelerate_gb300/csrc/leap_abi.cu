@@ -84,7 +84,7 @@ struct leap_ctx {
   Metadata md;
   std::map<int32_t, Integration> integ;
   // scratch, shared by calls on this context
-  DeviceBuffer partial, avg, cal1, dphi, gemm_partial, dd, cal, dev_err, lambda, twiddle, partial_i1, avg_i1;
+  DeviceBuffer partial, avg, cal1, dphi, gemm_partial, dd, cal, dev_err, lambda, twiddle, twiddle_df, partial_i1, avg_i1;
   cudaStream_t aux = nullptr;           // second stream for the FP64 reference-antenna pass
   cudaEvent_t fork = nullptr, join = nullptr;
   int last_ndir = 0, last_pols = 0, last_nbl = 0;
@@ -307,12 +307,22 @@ int calibrate_impl(leap_ctx* ctx, int32_t slot, const double* d_dd, int32_t ndir
   // Mixed form: FP64 sums of pol 0 of the reference-antenna baselines, on the
   // aux stream so that the FP64 pipe works while the FP32 bulk kernel runs.
   if (refant) {
-    // About one block per SM: launched after the persistent bulk kernel, each
-    // block fits beside a bulk block (registers) and keeps the FP64 pipe busy.
+    // complex<float> input: compensated FP32 kernel, about 4 blocks per SM over
+    // timestep slabs.  complex<double> input keeps the FP64 kernel.
+    const bool df = in.vis_type == LEAP_VIS_C64;
+    const int rdpw = df ? 4 : 2;
     int rt_per, rc_per, rnts, rncs;
     const int rtiles = (nI1 + 31) / 32;
-    const int rdg = (ndir + 4 * 2 - 1) / (4 * 2);
-    choose_slabs_target(T, C, static_cast<int64_t>(rtiles) * rdg, ctx->sms, rt_per, rc_per, rnts, rncs);
+    const int rdg = (ndir + 4 * rdpw - 1) / (4 * rdpw);
+    if (df) {
+      rnts = static_cast<int>(std::min<int64_t>(T, std::max<int64_t>(1, (4 * ctx->sms) / (rtiles * rdg))));
+      rt_per = (T + rnts - 1) / rnts;
+      rnts = (T + rt_per - 1) / rt_per;
+      rc_per = C;
+      rncs = 1;
+    } else {
+      choose_slabs_target(T, C, static_cast<int64_t>(rtiles) * rdg, ctx->sms, rt_per, rc_per, rnts, rncs);
+    }
     const int rslab = rnts * rncs;
     const int64_t n_i1 = static_cast<int64_t>(ndir) * nI1;
     LEAP_CUDA(ctx->avg_i1.ensure(sizeof(double2) * n_i1), "alloc I1 sums");
@@ -325,8 +335,8 @@ int calibrate_impl(leap_ctx* ctx, int32_t slot, const double* d_dd, int32_t ndir
     LEAP_CUDA(cudaStreamWaitEvent(ctx->aux, ctx->fork, 0), "fork");
     double2* dst = rslab > 1 ? ctx->partial_i1.as<double2>() : ctx->avg_i1.as<double2>();
     const dim3 rgrid(rtiles, rdg, rslab);
-    if (in.vis_type == LEAP_VIS_C64)
-      refant_average_fp64<float2, 2><<<rgrid, 128, 0, ctx->aux>>>(rr, md.I1.as<int32_t>(), nI1, dst);
+    if (df)
+      refant_average_df<4><<<rgrid, 128, 0, ctx->aux>>>(rr, md.I1.as<int32_t>(), nI1, ctx->twiddle_df.as<float4>(), dst);
     else
       refant_average_fp64<double2, 2><<<rgrid, 128, 0, ctx->aux>>>(rr, md.I1.as<int32_t>(), nI1, dst);
     ++kernels;
@@ -446,6 +456,17 @@ int32_t leap_create(int32_t device, leap_ctx** out) {
       const double ang = kTwoPi * static_cast<double>(i) / kTwiddleSize;
       tw[i] = make_float2(static_cast<float>(std::cos(ang)), static_cast<float>(std::sin(ang)));
     }
+    // The same angles as (hi, lo) float pairs of cos and sin for the compensated kernel.
+    std::vector<float4> twd(kTwiddleSize);
+    for (int i = 0; i < kTwiddleSize; ++i) {
+      const double ang = kTwoPi * static_cast<double>(i) / kTwiddleSize;
+      const double c = std::cos(ang), sn = std::sin(ang);
+      const float ch = static_cast<float>(c), sh = static_cast<float>(sn);
+      twd[i] = make_float4(ch, static_cast<float>(c - ch), sh, static_cast<float>(sn - sh));
+    }
+    LEAP_CUDA(ctx->twiddle_df.ensure(sizeof(float4) * kTwiddleSize), "alloc twiddle table");
+    LEAP_CUDA(cudaMemcpy(ctx->twiddle_df.ptr, twd.data(), sizeof(float4) * kTwiddleSize, cudaMemcpyHostToDevice),
+              "upload twiddle table");
     LEAP_CUDA(ctx->twiddle.ensure(sizeof(float2) * kTwiddleSize), "alloc twiddle table");
     LEAP_CUDA(cudaMemcpy(ctx->twiddle.ptr, tw.data(), sizeof(float2) * kTwiddleSize, cudaMemcpyHostToDevice),
               "upload twiddle table");
@@ -474,6 +495,7 @@ void leap_destroy(leap_ctx* ctx) {
     ctx->partial.release(); ctx->avg.release(); ctx->cal1.release(); ctx->dphi.release();
     ctx->gemm_partial.release(); ctx->dd.release(); ctx->cal.release(); ctx->dev_err.release(); ctx->lambda.release();
     ctx->twiddle.release();
+    ctx->twiddle_df.release();
     for (auto& tri : ctx->ring)
       for (auto& ev : tri)
         if (ev) cudaEventDestroy(ev);

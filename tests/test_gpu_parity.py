@@ -187,3 +187,17 @@ def test_mixed_pipelined_edges(ctx, stations, timesteps, channels, ndir):
     for d in range(0, ndir, max(1, ndir // 4)):
         err = np.abs(ctx.avgdata(d) - avg_o[d]) / np.maximum(scale, 1e-30)
         assert err.max() < 2e-6
+
+
+@pytest.mark.parametrize("dtype", [np.complex64, np.complex128])
+def test_mixed_reference_antenna_rows_are_near_fp64(ctx, dtype):
+    """The reference-antenna baselines (pol 0), which the solve reads with weight
+    one, are summed with compensated arithmetic: within 1e-9 of the FP64 sums,
+    relative to the sum of |terms|."""
+    obs, dirs = synth.small_case(stations=40, timesteps=6, channels=70, directions=9, vis_dtype=dtype, seed_shift=2)
+    md, mdo, dds, cal, cal_o, avg_o = run_case(ctx, obs, dirs, lg.LEAP_PRECISION_MIXED)
+    scale = np.abs(obs.vis[:, :, 0]).sum(axis=0).reshape(obs.timesteps, obs.nbaselines).sum(axis=0)
+    for d in range(len(dirs)):
+        got = ctx.avgdata(d)[mdo.I1, 0]
+        err = np.abs(got - avg_o[d][mdo.I1, 0]) / scale[mdo.I1]
+        assert err.max() < 1e-9, (d, err.max())
