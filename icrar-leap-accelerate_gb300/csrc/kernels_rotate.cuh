@@ -28,6 +28,8 @@ struct RotateArgs {
   const double* dd;         // [ndir][9] row-major direction matrices
   const double* lambda;     // [channels] c / (f0 + ch*df), as the reference computes it
   const float2* twiddle;    // [kTwiddleSize] (cos, sin) table for the mixed form
+  const float* uvw_f;       // [rows][6] (u, v, w) as (hi, lo) float pairs
+  const float* dirk;        // [ndir][12] phase constants as (hi, lo) pairs: -(l, m, n-1)*f0/c, -(l, m, n-1)*df/c
   int64_t rows;
   int32_t channels, pols, nbl, timesteps, ndir;
   double f0, df;
@@ -276,9 +278,9 @@ __global__ void __launch_bounds__(128) rotate_average_mixed(RotateArgs a) {
 // on one SM sub-partition, and cap registers at 168.)  All waits are bounded
 // and report a device error instead of hanging.
 //
-// Per (row, direction) the phase turns(c) = A + c*B is formed in FP64 once
-// per timestep as 32-bit fixed-point fractions of a turn.  The twiddle is
-// table-accurate (twiddle_turns) every kReseed channels and is advanced by
+// Per (row, direction) the phase turns(c) = A + c*B is formed once per
+// timestep in double-float arithmetic (~1e-12 turns) as 32-bit fixed-point
+// fractions of a turn.  The twiddle is table-accurate (twiddle_turns) every kReseed channels and is advanced by
 // one FP32 complex multiply per channel in between (drift over 8 steps about
 // 5e-7; it reaches the cal phases only through baselines that the FP64
 // reference-antenna pass does not cover, with weight ~1/S).  Sums: FP32 over
@@ -388,7 +390,6 @@ __global__ void __launch_bounds__(NC * 32, 1)
   __syncthreads();
 
   const int h = (lane >> 2) & 1;  // read order of the two 16-byte halves
-  const double kA = a.f0 / kSpeedOfLight, kB = a.df / kSpeedOfLight;
   uint32_t it = 0;
   bool ok = true;
   for (int u = blockIdx.x; u < units && ok; u += gridDim.x) {
@@ -413,15 +414,24 @@ __global__ void __launch_bounds__(NC * 32, 1)
       uint32_t pa[DPW], pb[DPW];
       float wr[DPW], wi[DPW];
       if (active) {
+        // turns(c) = A + c*B with A = -(l*u + m*v + (n-1)*w)*f0/c and B likewise with
+        // df, in double-float from pre-split UVWs and direction constants: no FP64
+        // instructions in this kernel (GB300 runs them at ~1/70 of the FP32 rate).
         const int64_t r = static_cast<int64_t>(t) * a.nbl + (valid ? b : 0);
-        const double uu = __ldg(a.uvw + 3 * r), vv = __ldg(a.uvw + 3 * r + 1), ww = __ldg(a.uvw + 3 * r + 2);
+        float x[6];
+#pragma unroll
+        for (int i = 0; i < 6; ++i) x[i] = __ldg(a.uvw_f + 6 * r + i);
 #pragma unroll
         for (int j = 0; j < DPW; ++j) {
           const int d = min(d0 + j, a.ndir - 1);
-          const double wrot = __ldg(a.dd + 9 * d + 6) * uu + __ldg(a.dd + 9 * d + 7) * vv + __ldg(a.dd + 9 * d + 8) * ww;
-          const double dw = wrot - ww;
-          pa[j] = frac_turns_u32(-dw * kA);
-          pb[j] = frac_turns_u32(-dw * kB);
+          float ka[6], kb[6];
+#pragma unroll
+          for (int i = 0; i < 6; ++i) {
+            ka[i] = __ldg(a.dirk + 12 * d + i);
+            kb[i] = __ldg(a.dirk + 12 * d + 6 + i);
+          }
+          pa[j] = df_dot3_turns_u32(ka, x);
+          pb[j] = df_dot3_turns_u32(kb, x);
           twiddle_turns(pb[j], tab, wr[j], wi[j]);
         }
       }
@@ -611,13 +621,6 @@ struct DfAcc {
   float s, c;  // value = s + c
 };
 
-// Knuth's TwoSum: a + b = s + e exactly.
-__device__ __forceinline__ void two_sum(float a, float b, float& s, float& e) {
-  s = a + b;
-  const float bb = s - a;
-  e = (a - (s - bb)) + (b - bb);
-}
-
 __device__ __forceinline__ void df_add_product(DfAcc& acc, float x, float yh, float yl) {
   const float p = x * yh;
   const float e = fmaf(x, yh, -p);       // x*yh = p + e exactly
@@ -707,6 +710,37 @@ __global__ void __launch_bounds__(128) refant_average_df(RotateArgs a, const int
       out[slab_off + static_cast<int64_t>(d) * nI1 + k] =
           make_double2(static_cast<double>(re[j].s) + static_cast<double>(re[j].c),
                        static_cast<double>(im[j].s) + static_cast<double>(im[j].c));
+  }
+}
+
+// UVWs as (hi, lo) float pairs for the double-float phase set-up.
+static __global__ void split_uvw(const double* __restrict__ uvw, int64_t rows, float* __restrict__ out) {
+  for (int64_t i = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x; i < 3 * rows;
+       i += static_cast<int64_t>(gridDim.x) * blockDim.x) {
+    const double x = uvw[i];
+    const float hi = static_cast<float>(x);
+    out[2 * i] = hi;
+    out[2 * i + 1] = static_cast<float>(x - static_cast<double>(hi));
+  }
+}
+
+// Per-direction phase constants: -(l, m, n-1) * f0/c and -(l, m, n-1) * df/c as
+// (hi, lo) float pairs, from the third row of each direction matrix.  n-1 is
+// exact in FP64 (Sterbenz), which removes the reference's w_rot - w cancellation.
+static __global__ void direction_constants(const double* __restrict__ dd, int ndir, double f0, double df,
+                                           float* __restrict__ out) {
+  const int d = blockIdx.x * blockDim.x + threadIdx.x;
+  if (d >= ndir) return;
+  const double kA = f0 / kSpeedOfLight, kB = df / kSpeedOfLight;
+  const double lmn[3] = {dd[9 * d + 6], dd[9 * d + 7], dd[9 * d + 8] - 1.0};
+  for (int s = 0; s < 2; ++s) {
+    const double k = s == 0 ? kA : kB;
+    for (int i = 0; i < 3; ++i) {
+      const double x = -lmn[i] * k;
+      const float hi = static_cast<float>(x);
+      out[12 * d + 6 * s + 2 * i] = hi;
+      out[12 * d + 6 * s + 2 * i + 1] = static_cast<float>(x - static_cast<double>(hi));
+    }
   }
 }
 

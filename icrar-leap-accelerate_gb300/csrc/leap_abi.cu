@@ -45,7 +45,7 @@ struct DeviceBuffer {
 };
 
 struct Integration {
-  DeviceBuffer vis, uvw;
+  DeviceBuffer vis, uvw, uvw_f;
   int32_t vis_type = LEAP_VIS_C64;
   int64_t rows = 0;
   int32_t channels = 0, pols = 0;
@@ -84,7 +84,8 @@ struct leap_ctx {
   Metadata md;
   std::map<int32_t, Integration> integ;
   // scratch, shared by calls on this context
-  DeviceBuffer partial, avg, cal1, dphi, gemm_partial, dd, cal, dev_err, lambda, twiddle, twiddle_df, partial_i1, avg_i1;
+  DeviceBuffer partial, avg, cal1, dphi, gemm_partial, dd, cal, dev_err, lambda, twiddle, twiddle_df, partial_i1, avg_i1,
+      dirk;
   cudaStream_t aux = nullptr;           // second stream for the FP64 reference-antenna pass
   cudaEvent_t fork = nullptr, join = nullptr;
   int last_ndir = 0, last_pols = 0, last_nbl = 0;
@@ -237,6 +238,7 @@ int calibrate_impl(leap_ctx* ctx, int32_t slot, const double* d_dd, int32_t ndir
   LEAP_CUDA(ctx->avg.ensure(sizeof(double2) * avg_elems), "alloc avgData");
   if (nslab > 1) LEAP_CUDA(ctx->partial.ensure(sizeof(double2) * avg_elems * nslab), "alloc partial sums");
   LEAP_CUDA(ctx->lambda.ensure(sizeof(double) * C), "alloc wavelengths");
+  LEAP_CUDA(ctx->dirk.ensure(sizeof(float) * 12 * ndir), "alloc direction constants");
   LEAP_CUDA(ctx->cal1.ensure(sizeof(double) * ndir * md.S), "alloc cal1");
   LEAP_CUDA(ctx->dphi.ensure(sizeof(double) * static_cast<size_t>(ndir) * md.Kpad), "alloc dphi");
   const int kchunk = 512;
@@ -261,6 +263,8 @@ int calibrate_impl(leap_ctx* ctx, int32_t slot, const double* d_dd, int32_t ndir
   ra.dd = d_dd;
   ra.lambda = ctx->lambda.as<double>();
   ra.twiddle = ctx->twiddle.as<float2>();
+  ra.uvw_f = in.uvw_f.as<float>();
+  ra.dirk = ctx->dirk.as<float>();
   ra.rows = in.rows;
   ra.channels = C;
   ra.pols = P;
@@ -284,6 +288,9 @@ int calibrate_impl(leap_ctx* ctx, int32_t slot, const double* d_dd, int32_t ndir
   const bool refant = precision == LEAP_PRECISION_MIXED && nI1 > 0;
   if (refant) LEAP_CUDA(cudaEventRecord(ctx->fork, s), "fork");
   if (pipe) {
+    direction_constants<<<(ndir + 63) / 64, 64, 0, s>>>(d_dd, ndir, md.k.freq_start_hz, md.k.freq_inc_hz,
+                                                       ctx->dirk.as<float>());
+    ++kernels;
     PipeArgs pa{};
     pa.a = ra;
     pa.tiles = tiles;
@@ -489,11 +496,13 @@ void leap_destroy(leap_ctx* ctx) {
     for (auto& kv : ctx->integ) {
       kv.second.vis.release();
       kv.second.uvw.release();
+      kv.second.uvw_f.release();
     }
     Metadata& md = ctx->md;
     md.I1.release(); md.Ad1.release(); md.Ad.release(); md.Ad_f32.release(); md.arow.release(); md.arow_val.release();
     ctx->partial.release(); ctx->avg.release(); ctx->cal1.release(); ctx->dphi.release();
     ctx->gemm_partial.release(); ctx->dd.release(); ctx->cal.release(); ctx->dev_err.release(); ctx->lambda.release();
+    ctx->dirk.release();
     ctx->twiddle.release();
     ctx->twiddle_df.release();
     for (auto& tri : ctx->ring)
@@ -599,6 +608,8 @@ int32_t leap_set_integration(leap_ctx* ctx, int32_t slot, int32_t vis_type, cons
     if (pols == 4) sanitize_nan_groups<double2, 4><<<grid, 256, 0, ctx->stream>>>(p, p, groups);
     else sanitize_nan_groups_generic<double2><<<grid, 256, 0, ctx->stream>>>(p, p, groups, pols);
   }
+  LEAP_CUDA(in.uvw_f.ensure(sizeof(float) * 6 * rows), "alloc split uvw");
+  split_uvw<<<grid_1d(3 * rows, 256), 256, 0, ctx->stream>>>(in.uvw.as<double>(), rows, in.uvw_f.as<float>());
   LEAP_CUDA(cudaGetLastError(), "sanitize launch");
   LEAP_CUDA(cudaStreamSynchronize(ctx->stream), "set integration");
   in.vis_type = vis_type;
@@ -631,6 +642,7 @@ int32_t leap_release_integration(leap_ctx* ctx, int32_t slot) {
   cudaStreamSynchronize(ctx->stream);
   it->second.vis.release();
   it->second.uvw.release();
+  it->second.uvw_f.release();
   ctx->integ.erase(it);
   return LEAP_OK;
 }

@@ -106,6 +106,37 @@ __device__ __forceinline__ void twiddle_turns(uint32_t turns, const float2* __re
   s = fmaf(t.y, cd, t.x * sd);
 }
 
+// Knuth's TwoSum: a + b = s + e exactly.
+__device__ __forceinline__ void two_sum(float a, float b, float& s, float& e) {
+  s = a + b;
+  const float bb = s - a;
+  e = (a - (s - bb)) + (b - bb);
+}
+
+// (ah + al) * (bh + bl) = p + e to about 2^-44 relative (TwoProd of the high parts).
+__device__ __forceinline__ void df_prod(float ah, float al, float bh, float bl, float& p, float& e) {
+  p = ah * bh;
+  e = fmaf(ah, bh, -p);
+  e = fmaf(ah, bl, e);
+  e = fmaf(al, bh, e);
+}
+
+// k[0..5] = (L, M, N) as (hi, lo) float pairs, x[0..5] = (u, v, w) likewise.
+// Returns frac(L*u + M*v + N*w) as a 2^-32 fixed-point fraction of a turn,
+// computed in double-float arithmetic (error ~1e-12 turns for |sum| < 1e4).
+__device__ __forceinline__ uint32_t df_dot3_turns_u32(const float* k, const float* x) {
+  float p1, e1, p2, e2, p3, e3, s, t1, t2;
+  df_prod(k[0], k[1], x[0], x[1], p1, e1);
+  df_prod(k[2], k[3], x[2], x[3], p2, e2);
+  df_prod(k[4], k[5], x[4], x[5], p3, e3);
+  two_sum(p1, p2, s, t1);
+  two_sum(s, p3, s, t2);
+  const float lo = (e1 + e2) + (e3 + (t1 + t2));
+  const float f = s - rintf(s);  // exact, in [-0.5, 0.5]
+  return static_cast<uint32_t>(__float2int_rn(f * 4294967296.0f)) +
+         static_cast<uint32_t>(__float2int_rn(lo * 4294967296.0f));
+}
+
 // Fractional part of x (turns) as a rounded 2^-32 fixed-point value.
 __device__ __forceinline__ uint32_t frac_turns_u32(double x) {
   const double f = x - rint(x);  // in [-0.5, 0.5]
