@@ -280,8 +280,13 @@ def run_gpu(args, rank: int, world: int):
     b_alg = D * (units / D * vis_bytes + obs.rows * 24) + D * obs.nbaselines * P * 16
     achieved = b_alg / (rot_ms / 1e3) / 1e9
     fp32_ops = D * obs.rows * obs.channels * (P * 4 + 5)  # FMA-pipe issue slots per (row, channel, direction)
+    # DRAM traffic of one launch of the bulk kernel, from an ncu capture
+    # (dram__bytes_read.sum + dram__bytes_write.sum) of the 2-timestep case of this
+    # workload: 101.7 MB read per timestep (the visibilities, once) + 44.7 MB of
+    # partial-sum writes, scaled to the timesteps of this run.
+    traffic = (101.74e6 * obs.timesteps + 44.74e6) if (obs.nbaselines == 8256 and obs.channels == 384 and D == 64) else None
     roof = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
-            "traffic": None, "kernel": "rotate_average", "kernel_ms": rot_ms,
+            "traffic": traffic, "kernel": "rotate_average", "kernel_ms": rot_ms,
             "peak_source": "MEASURED_PEAKS.json hbm_gbs" if peaks else "fallback 6.8 TB/s",
             "note": "B_alg counts the vis once per direction; the kernel reads it once for all directions",
             "compute": {"fp32_issue_per_s": fp32_ops / (rot_ms / 1e3), "fp32_peak_fma_per_s": 3.6e13,

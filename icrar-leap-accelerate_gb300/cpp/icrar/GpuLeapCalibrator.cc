@@ -1,0 +1,81 @@
+#include "GpuLeapCalibrator.h"
+
+#include <complex>
+#include <string>
+
+#include "MetaData.h"
+#include "exception.h"
+
+namespace icrar {
+namespace gb300 {
+
+namespace {
+void check(int rc, leap_ctx* ctx, const char* what) {
+  if (rc == LEAP_OK) return;
+  const std::string msg = std::string(what) + ": " + leap_last_error(ctx);
+  if (rc == LEAP_ERR_INVALID_ARGUMENT) throw invalid_argument_exception(msg, what, __FILE__, __LINE__);
+  throw icrar::exception(msg, __FILE__, __LINE__);
+}
+}  // namespace
+
+GpuLeapCalibrator::GpuLeapCalibrator(GpuOptions options) : m_options(options) {
+  check(leap_create(options.device, &m_ctx), nullptr, "leap_create");
+}
+
+GpuLeapCalibrator::~GpuLeapCalibrator() { leap_destroy(m_ctx); }
+
+cpu::CalibrationCollection GpuLeapCalibrator::Calibrate(const MeasurementSet& ms,
+                                                        const std::vector<SphericalDirection>& directions,
+                                                        const Slice& solutionInterval, double minimumBaselineThreshold,
+                                                        std::optional<unsigned int> referenceAntenna,
+                                                        bool isFileSystemCacheEnabled) {
+  const int timesteps = static_cast<int>(ms.GetNumTimesteps());
+  const Range interval = solutionInterval.Evaluate(timesteps);
+  const std::vector<double> epochs = ms.GetEpochs();
+  const cpu::MetaData metadata(ms, referenceAntenna, minimumBaselineThreshold, isFileSystemCacheEnabled);
+  const leap_constants k = metadata.GetConstants().ToAbi();
+  check(leap_set_metadata(m_ctx, &k, metadata.GetA().data(), metadata.GetARows(), metadata.GetStations(),
+                          metadata.GetI().data(), metadata.GetAd().data(), metadata.GetA1().data(),
+                          metadata.GetA1Rows(), metadata.GetI1().data(), metadata.GetAd1().data()),
+        m_ctx, "leap_set_metadata");
+
+  std::vector<double> dd(9 * directions.size());
+  for (size_t i = 0; i < directions.size(); ++i) {
+    const auto m = metadata.GenerateDDMatrix(directions[i]);
+    std::copy(m.begin(), m.end(), dd.begin() + 9 * i);
+  }
+  const uint32_t nbl = ms.GetNumBaselines();
+  const uint32_t C = ms.GetNumChannels(), P = ms.GetNumPols();
+  const int32_t S = metadata.GetStations();
+  std::vector<cpu::Calibration> output;
+  const int solutions = interval.GetSize();
+  for (int s = 0; s < solutions; ++s) {
+    output.emplace_back(epochs[static_cast<size_t>(s) * interval.interval],
+                        epochs[static_cast<size_t>(s + 1) * interval.interval - 1]);
+    // Integration start row ignores Slice.start, as the reference does (CpuLeapCalibrator.cc:116).
+    const uint32_t startRow = static_cast<uint32_t>(s) * interval.interval * nbl;
+    const uint32_t rows = static_cast<uint32_t>(interval.interval) * nbl;
+    const std::vector<double> uvw = ms.GetCoords(startRow, rows);
+    if (ms.HasFloatData()) {
+      const auto vis = ms.GetVisF32(startRow, 0, C, rows, P);
+      check(leap_set_integration(m_ctx, 0, LEAP_VIS_C64, vis.data(), uvw.data(), rows, C, P, LEAP_MEMORY_HOST), m_ctx,
+            "leap_set_integration");
+    } else {
+      const auto vis = ms.GetVis(startRow, 0, C, rows, P);
+      check(leap_set_integration(m_ctx, 0, LEAP_VIS_C128, vis.data(), uvw.data(), rows, C, P, LEAP_MEMORY_HOST), m_ctx,
+            "leap_set_integration");
+    }
+    std::vector<double> cal(static_cast<size_t>(S) * directions.size());
+    check(leap_calibrate(m_ctx, 0, dd.data(), static_cast<int32_t>(directions.size()), m_options.precision, cal.data()),
+          m_ctx, "leap_calibrate");
+    for (size_t i = 0; i < directions.size(); ++i)
+      output.back().GetBeamCalibrations().emplace_back(
+          directions[i], std::vector<double>(cal.begin() + static_cast<std::ptrdiff_t>(S * i),
+                                             cal.begin() + static_cast<std::ptrdiff_t>(S * (i + 1))));
+  }
+  leap_release_integration(m_ctx, 0);
+  return cpu::CalibrationCollection(std::move(output));
+}
+
+}  // namespace gb300
+}  // namespace icrar

@@ -225,3 +225,23 @@ def uneven_chunks(count: int = 32, seed: int = 4, t_range=(1, 64), channel_choic
         chunks.append(Chunk(int(t), int(c), off))
         off += int(t)
     return chunks
+
+
+def write_leapms(obs: Observation, path: str) -> None:
+    """Write an observation as a ".leapms" file for the C++ MeasurementSet stand-in:
+    header, per-row ANTENNA1/ANTENNA2/FLAG/TIME/UVW, then DATA in the
+    MeasurementSet's own [row][channel][pol] order."""
+    nbl, T = obs.nbaselines, obs.timesteps
+    rows = nbl * T
+    is_double = obs.vis.dtype == np.complex128
+    with open(path, "wb") as f:
+        f.write(b"LEAPMS01")
+        np.array([obs.num_stations, obs.total_antennas, rows, obs.channels, obs.pols, int(is_double)],
+                 dtype="<u4").tofile(f)
+        np.array([obs.freq_start_hz, obs.freq_inc_hz, obs.phase_centre[0], obs.phase_centre[1]], dtype="<f8").tofile(f)
+        np.tile(obs.antenna1[:nbl], T).astype("<i4").tofile(f)
+        np.tile(obs.antenna2[:nbl], T).astype("<i4").tofile(f)
+        np.tile(np.asarray(obs.flags[:nbl], dtype=np.uint8), T).tofile(f)
+        np.repeat(obs.epochs, nbl).astype("<f8").tofile(f)
+        np.ascontiguousarray(obs.uvw, dtype="<f8").tofile(f)
+        np.ascontiguousarray(obs.vis.transpose(1, 0, 2)).tofile(f)
