@@ -19,6 +19,7 @@
 #pragma once
 
 #include "leap_common.cuh"
+#include "kernels_pipe.cuh"
 
 namespace leapgb {
 
@@ -262,270 +263,6 @@ __global__ void __launch_bounds__(128) rotate_average_mixed(RotateArgs a) {
 }
 
 // ---------------------------------------------------------------------------
-// Mixed-precision form, pipelined (4 pols, complex<float>): the hot kernel.
-//
-// Persistent blocks of NC warps.  Work units are (32-baseline tile, direction
-// group of NC*DPW, timestep slab), visited round-robin by the blocks.  Each
-// unit is a sequence of chunks = (timestep, 16 channels).  The visibility
-// tensor is viewed as a 2-D array [channel][row*8 floats]; a chunk of the tile
-// is one TMA box of 256 floats (32 baselines x 4 pols x complex) by 16 channels
-// (16 KB), loaded with cp.async.bulk.tensor into a shared-memory stage and
-// completing on the stage's "full" mbarrier.  Boxes past the last channel or
-// row are zero-filled by the TMA unit; rows of a partial tile that belong to
-// the next timestep are loaded but not used.  Every warp releases a stage
-// through its "empty" mbarrier; lane 0 of warp 0 then refills it with the
-// chunk kPipeStages ahead.  (A separate producer warp would make 9 warps, 3
-// on one SM sub-partition, and cap registers at 168.)  All waits are bounded
-// and report a device error instead of hanging.
-//
-// Per (row, direction) the phase turns(c) = A + c*B is formed once per
-// timestep in double-float arithmetic (~1e-12 turns) as 32-bit fixed-point
-// fractions of a turn.  The twiddle is table-accurate (twiddle_turns) every kReseed channels and is advanced by
-// one FP32 complex multiply per channel in between (drift over 8 steps about
-// 5e-7; it reaches the cal phases only through baselines that the FP64
-// reference-antenna pass does not cover, with weight ~1/S).  Sums: FP32 over
-// each chunk, folded into Kahan pairs.
-//
-// Shared-memory reads: lane i reads its 32 bytes as two 16-byte halves; lanes
-// with bit 2 set read the upper half first so that each quarter-warp covers
-// all 32 banks (conflict-free).  Those lanes hold pols (2,3,0,1) in register
-// slots (0,1,2,3) and swap back when writing out.
-// ---------------------------------------------------------------------------
-struct PipeArgs {
-  RotateArgs a;
-  int tiles, dgroups, nslab;   // unit grid
-};
-
-constexpr int kPipeChunk = 16;    // channels per stage (TMA box height)
-constexpr int kPipeReseed = 8;    // channels between table-accurate twiddles
-constexpr int kPipeStages = 4;
-constexpr int kPipeItemBytes = 32 * 4 * 8;  // 32 baselines x 4 pols x complex<float>
-constexpr int kPipeStageBytes = kPipeChunk * kPipeItemBytes;
-
-// Position in a block's chunk sequence (unit, timestep, first channel).
-struct ChunkCursor {
-  int u, t, cb;
-  int t_lo, t_hi, c_lo, c_hi;
-};
-
-__device__ __forceinline__ void cursor_unit(ChunkCursor& k, const PipeArgs& p) {
-  const RotateArgs& a = p.a;
-  const int slab = k.u % p.nslab;
-  const int ts = slab / a.n_cslab, cs = slab % a.n_cslab;
-  k.t_lo = ts * a.t_per_slab;
-  k.t_hi = min(a.timesteps, k.t_lo + a.t_per_slab);
-  k.c_lo = cs * a.c_per_slab;
-  k.c_hi = min(a.channels, k.c_lo + a.c_per_slab);
-  k.t = k.t_lo;
-  k.cb = k.c_lo;
-}
-
-__device__ __forceinline__ void cursor_next(ChunkCursor& k, const PipeArgs& p, int units) {
-  k.cb += kPipeChunk;
-  if (k.cb < k.c_hi) return;
-  k.cb = k.c_lo;
-  if (++k.t < k.t_hi) return;
-  k.u += gridDim.x;
-  if (k.u < units) cursor_unit(k, p);
-}
-
-// Issue the TMA load of the chunk at cursor k into stage st.
-__device__ __forceinline__ void issue_chunk(const ChunkCursor& k, const PipeArgs& p, const CUtensorMap* map,
-                                           unsigned char* stage_mem, uint64_t* full, int st) {
-  const int tile = k.u / (p.dgroups * p.nslab);
-  mbar_arrive_expect_tx(&full[st], kPipeStageBytes);
-  tma_load_2d(stage_mem + st * kPipeStageBytes, map, (k.t * p.a.nbl + tile * 32) * 8, k.cb, &full[st]);
-}
-
-template <int DPW>
-__device__ __forceinline__ void mac_channel(const unsigned char* src, int h, float (&pr)[DPW][4], float (&pi)[DPW][4],
-                                            float (&zr)[DPW], float (&zi)[DPW], const float (&wr)[DPW],
-                                            const float (&wi)[DPW]) {
-  const float4 x0 = *reinterpret_cast<const float4*>(src + 16 * h);
-  const float4 x1 = *reinterpret_cast<const float4*>(src + 16 * (1 - h));
-  const float vr[4] = {x0.x, x0.z, x1.x, x1.z};
-  const float vi[4] = {x0.y, x0.w, x1.y, x1.w};
-#pragma unroll
-  for (int j = 0; j < DPW; ++j) {
-#pragma unroll
-    for (int q = 0; q < 4; ++q) {
-      pr[j][q] = fmaf(vr[q], zr[j], fmaf(-vi[q], zi[j], pr[j][q]));
-      pi[j][q] = fmaf(vr[q], zi[j], fmaf(vi[q], zr[j], pi[j][q]));
-    }
-    const float nr = fmaf(zr[j], wr[j], -zi[j] * wi[j]);
-    zi[j] = fmaf(zr[j], wi[j], zi[j] * wr[j]);
-    zr[j] = nr;
-  }
-}
-
-template <int NC, int DPW>
-__global__ void __launch_bounds__(NC * 32, 1)
-    rotate_average_mixed_pipe(const __grid_constant__ CUtensorMap vis_map, PipeArgs pa_) {
-  const RotateArgs& a = pa_.a;
-  extern __shared__ __align__(128) unsigned char smem[];
-  unsigned char* stage_mem = smem;
-  float2* tab = reinterpret_cast<float2*>(smem + kPipeStages * kPipeStageBytes);
-  uint64_t* full = reinterpret_cast<uint64_t*>(tab + kTwiddleSize);
-  uint64_t* empty = full + kPipeStages;
-
-  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const bool producer = threadIdx.x == 0;
-  for (int i = threadIdx.x; i < kTwiddleSize; i += blockDim.x) tab[i] = __ldg(a.twiddle + i);
-  const int units = pa_.tiles * pa_.dgroups * pa_.nslab;
-  ChunkCursor pc{};  // producer cursor, kPipeStages chunks ahead of the consumers
-  uint32_t issued = 0;
-  if (producer) {
-    for (int i = 0; i < kPipeStages; ++i) {
-      mbar_init(&full[i], 1);
-      mbar_init(&empty[i], NC);
-    }
-    fence_mbar_init();
-    pc.u = blockIdx.x;
-    if (pc.u < units) cursor_unit(pc, pa_);
-    for (; issued < kPipeStages && pc.u < units; ++issued) {
-      issue_chunk(pc, pa_, &vis_map, stage_mem, full, issued);
-      cursor_next(pc, pa_, units);
-    }
-  }
-  __syncthreads();
-
-  const int h = (lane >> 2) & 1;  // read order of the two 16-byte halves
-  uint32_t it = 0;
-  bool ok = true;
-  for (int u = blockIdx.x; u < units && ok; u += gridDim.x) {
-    const int tile = u / (pa_.dgroups * pa_.nslab);
-    const int dg = (u / pa_.nslab) % pa_.dgroups;
-    const int slab = u % pa_.nslab;
-    const int ts = slab / a.n_cslab, cs = slab % a.n_cslab;
-    const int t_lo = ts * a.t_per_slab, t_hi = min(a.timesteps, t_lo + a.t_per_slab);
-    const int c_lo = cs * a.c_per_slab, c_hi = min(a.channels, c_lo + a.c_per_slab);
-    const int b = tile * 32 + lane;
-    const bool valid = b < a.nbl;
-    const int d0 = (dg * NC + warp) * DPW;
-    const bool active = d0 < a.ndir;
-
-    float sr[DPW][4], si[DPW][4], cr[DPW][4], ci[DPW][4];
-#pragma unroll
-    for (int j = 0; j < DPW; ++j)
-#pragma unroll
-      for (int q = 0; q < 4; ++q) sr[j][q] = si[j][q] = cr[j][q] = ci[j][q] = 0.f;
-
-    for (int t = t_lo; t < t_hi && ok; ++t) {
-      uint32_t pa[DPW], pb[DPW];
-      float wr[DPW], wi[DPW];
-      if (active) {
-        // turns(c) = A + c*B with A = -(l*u + m*v + (n-1)*w)*f0/c and B likewise with
-        // df, in double-float from pre-split UVWs and direction constants: no FP64
-        // instructions in this kernel (GB300 runs them at ~1/70 of the FP32 rate).
-        const int64_t r = static_cast<int64_t>(t) * a.nbl + (valid ? b : 0);
-        float x[6];
-#pragma unroll
-        for (int i = 0; i < 6; ++i) x[i] = __ldg(a.uvw_f + 6 * r + i);
-#pragma unroll
-        for (int j = 0; j < DPW; ++j) {
-          const int d = min(d0 + j, a.ndir - 1);
-          float ka[6], kb[6];
-#pragma unroll
-          for (int i = 0; i < 6; ++i) {
-            ka[i] = __ldg(a.dirk + 12 * d + i);
-            kb[i] = __ldg(a.dirk + 12 * d + 6 + i);
-          }
-          pa[j] = df_dot3_turns_u32(ka, x);
-          pb[j] = df_dot3_turns_u32(kb, x);
-          twiddle_turns(pb[j], tab, wr[j], wi[j]);
-        }
-      }
-      for (int cb = c_lo; cb < c_hi; cb += kPipeChunk, ++it) {
-        const int n = min(kPipeChunk, c_hi - cb);
-        const int st = it % kPipeStages;
-        if (!mbar_wait_bounded(&full[st], (it / kPipeStages) & 1)) {
-          atomicOr(a.err, kDevErrTimeout);
-          ok = false;
-          break;
-        }
-        if (active) {
-          float pr[DPW][4], pi[DPW][4];
-          float zr[DPW], zi[DPW];
-#pragma unroll
-          for (int j = 0; j < DPW; ++j)
-#pragma unroll
-            for (int q = 0; q < 4; ++q) pr[j][q] = pi[j][q] = 0.f;
-          const unsigned char* src = stage_mem + st * kPipeStageBytes + lane * 32;
-          if (n == kPipeChunk) {
-#pragma unroll
-            for (int sub = 0; sub < kPipeChunk; sub += kPipeReseed) {
-#pragma unroll
-              for (int j = 0; j < DPW; ++j)
-                twiddle_turns(pa[j] + static_cast<uint32_t>(cb + sub) * pb[j], tab, zr[j], zi[j]);
-#pragma unroll
-              for (int k = 0; k < kPipeReseed; ++k)
-                mac_channel<DPW>(src + (sub + k) * kPipeItemBytes, h, pr, pi, zr, zi, wr, wi);
-            }
-          } else {
-            for (int k = 0; k < n; ++k) {
-              if (k % kPipeReseed == 0) {
-#pragma unroll
-                for (int j = 0; j < DPW; ++j)
-                  twiddle_turns(pa[j] + static_cast<uint32_t>(cb + k) * pb[j], tab, zr[j], zi[j]);
-              }
-              mac_channel<DPW>(src + k * kPipeItemBytes, h, pr, pi, zr, zi, wr, wi);
-            }
-          }
-#pragma unroll
-          for (int j = 0; j < DPW; ++j)
-#pragma unroll
-            for (int q = 0; q < 4; ++q) {
-              float y = pr[j][q] - cr[j][q];
-              float tt = sr[j][q] + y;
-              cr[j][q] = (tt - sr[j][q]) - y;
-              sr[j][q] = tt;
-              y = pi[j][q] - ci[j][q];
-              tt = si[j][q] + y;
-              ci[j][q] = (tt - si[j][q]) - y;
-              si[j][q] = tt;
-            }
-        }
-        __syncwarp();
-        if (lane == 0) mbar_arrive(&empty[st]);
-        if (producer && pc.u < units) {
-          // Refill this stage with the chunk kPipeStages ahead once every warp released it.
-          if (!mbar_wait_bounded(&empty[st], (it / kPipeStages) & 1)) {
-            atomicOr(a.err, kDevErrTimeout);
-            ok = false;
-          } else {
-            issue_chunk(pc, pa_, &vis_map, stage_mem, full, st);
-            cursor_next(pc, pa_, units);
-            ++issued;
-          }
-        }
-        __syncwarp();
-      }
-    }
-    if (ok && active && valid) {
-      const int64_t slab_off = static_cast<int64_t>(slab) * a.ndir * 4 * a.nbl;
-#pragma unroll
-      for (int j = 0; j < DPW; ++j) {
-        const int d = d0 + j;
-        if (d < a.ndir) {
-#pragma unroll
-          for (int q = 0; q < 4; ++q) {
-            const int p = q ^ (2 * h);
-            a.out[slab_off + (static_cast<int64_t>(d) * 4 + p) * a.nbl + b] =
-                make_double2(static_cast<double>(sr[j][q]) - static_cast<double>(cr[j][q]),
-                             static_cast<double>(si[j][q]) - static_cast<double>(ci[j][q]));
-          }
-        }
-      }
-    }
-  }
-  if (producer) {
-    // Do not leave while copies issued by this block may still land in shared memory.
-    for (uint32_t j = (issued > kPipeStages ? issued - kPipeStages : 0); j < issued; ++j)
-      if (!mbar_wait_bounded(&full[j % kPipeStages], (j / kPipeStages) & 1)) atomicOr(a.err, kDevErrTimeout);
-  }
-}
-
-// ---------------------------------------------------------------------------
 // Reference-antenna baselines in FP64 (mixed form).  The solve reads pol 0 of
 // the |I1| baselines through the reference antenna with weight one (cal1 =
 // Ad1 * arg(avg[I1, 0])) and then multiplies cal1 by 2*pi, so an FP32 phase
@@ -741,6 +478,86 @@ static __global__ void direction_constants(const double* __restrict__ dd, int nd
       out[12 * d + 6 * s + 2 * i] = hi;
       out[12 * d + 6 * s + 2 * i + 1] = static_cast<float>(x - static_cast<double>(hi));
     }
+  }
+}
+
+// One work item of the compensated reference-antenna pass (batched calls:
+// one per integration chunk).  Blocks are numbered across items.
+struct RefantItem {
+  const float2* vis;       // [C][rows][pols]
+  const double* uvw;       // [rows][3]
+  const double* dd;        // the item's first direction matrix
+  double2* out;            // [nslab][ndir][nI1]
+  int64_t rows;
+  int32_t T, C, pols, ndir;
+  int32_t t_per_slab, c_per_slab, n_tslab, n_cslab;
+  int32_t dgroups, block_begin, pad_[2];
+};
+
+template <int DPW>
+__global__ void __launch_bounds__(128) refant_average_df_items(const RefantItem* __restrict__ items, int nitems,
+                                                              int nbl, double f0, double df,
+                                                              const int32_t* __restrict__ I1, int nI1,
+                                                              const float4* __restrict__ df_tab) {
+  __shared__ float4 tab[kTwiddleSize];
+  for (int i = threadIdx.x; i < kTwiddleSize; i += blockDim.x) tab[i] = __ldg(df_tab + i);
+  __syncthreads();
+  int ii = 0;
+  while (ii + 1 < nitems && items[ii + 1].block_begin <= static_cast<int>(blockIdx.x)) ++ii;
+  const RefantItem it = items[ii];
+  constexpr int NW = 4;
+  const int nslab = it.n_tslab * it.n_cslab;
+  const int local = blockIdx.x - it.block_begin;
+  const int ktile = local / (it.dgroups * nslab);
+  const int dg = (local / nslab) % it.dgroups;
+  const int slab = local % nslab;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const int k = ktile * 32 + lane;
+  const int j0 = (dg * NW + warp) * DPW;
+  const int ts = slab / it.n_cslab, cs = slab % it.n_cslab;
+  const int t_lo = ts * it.t_per_slab, t_hi = min(it.T, t_lo + it.t_per_slab);
+  const int c_lo = cs * it.c_per_slab, c_hi = min(it.C, c_lo + it.c_per_slab);
+  if (j0 >= it.ndir || k >= nI1) return;
+  int b = __ldg(I1 + k);
+  if (b < 0) b += nbl;  // VectorRangeSelect wrap-around (LA/math/cpu/vector.h:97-104)
+  const double kA = f0 / kSpeedOfLight, kB = df / kSpeedOfLight;
+  DfAcc re[DPW], im[DPW];
+#pragma unroll
+  for (int j = 0; j < DPW; ++j) re[j] = im[j] = DfAcc{0.f, 0.f};
+  for (int t = t_lo; t < t_hi; ++t) {
+    const int64_t r = static_cast<int64_t>(t) * nbl + b;
+    const double uu = __ldg(it.uvw + 3 * r), vv = __ldg(it.uvw + 3 * r + 1), ww = __ldg(it.uvw + 3 * r + 2);
+    uint64_t pa[DPW], pb[DPW];
+#pragma unroll
+    for (int j = 0; j < DPW; ++j) {
+      const int d = min(j0 + j, it.ndir - 1);
+      const double wrot = __ldg(it.dd + 9 * d + 6) * uu + __ldg(it.dd + 9 * d + 7) * vv + __ldg(it.dd + 9 * d + 8) * ww;
+      const double dw = wrot - ww;
+      pa[j] = frac_turns_u64(-dw * kA);
+      pb[j] = frac_turns_u64(-dw * kB);
+    }
+    const float2* src = it.vis + r * it.pols;
+#pragma unroll 4
+    for (int c = c_lo; c < c_hi; ++c) {
+      const float2 v = __ldg(src + static_cast<int64_t>(c) * it.rows * it.pols);
+#pragma unroll
+      for (int j = 0; j < DPW; ++j) {
+        float zrh, zrl, zih, zil;
+        df_twiddle(pa[j] + static_cast<uint64_t>(c) * pb[j], tab, zrh, zrl, zih, zil);
+        df_add_product(re[j], v.x, zrh, zrl);
+        df_add_product(re[j], -v.y, zih, zil);
+        df_add_product(im[j], v.x, zih, zil);
+        df_add_product(im[j], v.y, zrh, zrl);
+      }
+    }
+  }
+  double2* out = it.out + static_cast<int64_t>(slab) * it.ndir * nI1;
+#pragma unroll
+  for (int j = 0; j < DPW; ++j) {
+    const int jd = j0 + j;
+    if (jd < it.ndir)
+      out[static_cast<int64_t>(jd) * nI1 + k] = make_double2(static_cast<double>(re[j].s) + static_cast<double>(re[j].c),
+                                                             static_cast<double>(im[j].s) + static_cast<double>(im[j].c));
   }
 }
 

@@ -23,12 +23,17 @@ namespace {
 
 thread_local std::string g_last_error;
 
+// Bumped whenever any device buffer is (re)allocated: captured CUDA graphs
+// hold raw pointers, so a graph recorded before the bump is stale.
+uint64_t g_alloc_epoch = 0;
+
 // Grow-only device buffer: steady-state calls reuse it and never allocate.
 struct DeviceBuffer {
   void* ptr = nullptr;
   size_t bytes = 0;
   cudaError_t ensure(size_t need) {
     if (need <= bytes) return cudaSuccess;
+    ++g_alloc_epoch;
     if (ptr) cudaFree(ptr);
     ptr = nullptr;
     bytes = 0;
@@ -37,7 +42,10 @@ struct DeviceBuffer {
     return e;
   }
   void release() {
-    if (ptr) cudaFree(ptr);
+    if (ptr) {
+      cudaFree(ptr);
+      ++g_alloc_epoch;
+    }
     ptr = nullptr;
     bytes = 0;
   }
@@ -50,7 +58,7 @@ struct Integration {
   int64_t rows = 0;
   int32_t channels = 0, pols = 0;
   bool has_map = false;
-  CUtensorMap vis_map;  // [channel][row*8 floats] view of a 4-pol complex<float> integration
+  CUtensorMap map16, map8;  // [channel][row*8 floats] views of a 4-pol complex<float> integration, box heights 16 / 8
 };
 
 // cuTensorMapEncodeTiled through the runtime's driver entry point (no libcuda link).
@@ -75,10 +83,27 @@ struct Metadata {
 
 }  // namespace
 
+// Launch choices the autotuner may set (0 = built-in heuristic).
+struct TuneChoice {
+  int tpb = 0;    // tiles per block of the pipelined kernel (1 or 4)
+  int waves = 0;  // target rounds of the persistent grid when planning slabs
+};
+
 struct leap_ctx {
   int device = 0;
   int sms = 152;
-  bool pipe_attr_set = false;
+  bool pipe_attr_set = false, pipe_attr_set4 = false;
+  TuneChoice tune;
+  bool capturing = false;             // recording a CUDA graph: skip host-side uploads and timing events
+  bool autotune = true;               // tune new batched shapes on first use
+  std::map<std::string, TuneChoice> tuned;
+  std::string graph_key;
+  cudaGraphExec_t graph_exec = nullptr;
+  uint64_t graph_epoch = 0;
+  std::vector<PipeItem> pipe_items_host;
+  std::vector<ReduceItem> reduce_items_host, refant_reduce_host;
+  std::vector<RefantItem> refant_items_host;
+  DeviceBuffer pipe_items, reduce_items, refant_items, refant_reduce;
   cudaStream_t stream = nullptr;
   std::string err;
   Metadata md;
@@ -130,9 +155,8 @@ struct DeviceGuard {
   }
 };
 
-constexpr int kPipeNC = 8;  // consumer warps of the pipelined kernel (4 directions each)
-constexpr int kPipeSmem = kPipeStages * kPipeStageBytes + kTwiddleSize * sizeof(float2) +
-                          2 * kPipeStages * sizeof(uint64_t);
+constexpr int kPipeNC = 8;   // warps of the pipelined kernel
+constexpr int kPipeDPW = 4;  // directions per warp
 
 int grid_1d(int64_t n, int threads) {
   int64_t b = (n + threads - 1) / threads;
@@ -199,173 +223,326 @@ int dispatch_pols(const RotateArgs& a, dim3 grid, int precision, cudaStream_t s)
   }
 }
 
-int calibrate_impl(leap_ctx* ctx, int32_t slot, const double* d_dd, int32_t ndir, int32_t precision,
-                   double* d_cal, cudaStream_t s) {
-  if (!ctx->md.set) return fail(ctx, LEAP_ERR_NOT_READY, "metadata not set");
-  auto it = ctx->integ.find(slot);
-  if (it == ctx->integ.end()) return fail(ctx, LEAP_ERR_NOT_READY, "integration slot not set");
-  if (ndir <= 0) return fail(ctx, LEAP_ERR_INVALID_ARGUMENT, "ndirections must be positive");
-  if (precision != LEAP_PRECISION_FP64 && precision != LEAP_PRECISION_MIXED)
-    return fail(ctx, LEAP_ERR_INVALID_ARGUMENT, "unknown precision");
-  Integration& in = it->second;
+// A unit of a calibrate call: directions [dir0, dir0 + ndir) against integration `slot`.
+struct WorkItem {
+  int32_t slot, dir0, ndir;
+};
+
+// Rotate + average of every item into ctx->avg ([D][P][nbl]).
+int rotate_stage(leap_ctx* ctx, const std::vector<WorkItem>& items, const double* d_dd, int32_t D, int32_t precision,
+                 int P, cudaStream_t s, int& kernels) {
   Metadata& md = ctx->md;
   const int32_t nbl = static_cast<int32_t>(md.k.nbaselines);
-  const int32_t P = in.pols;
-  if (in.rows % nbl != 0)
-    return fail(ctx, LEAP_ERR_INVALID_ARGUMENT, "integration rows not a multiple of the baseline count");
-  const int32_t T = static_cast<int32_t>(in.rows / nbl);
-  const int32_t C = in.channels;
-
-  // Launch shape: 32 baselines per warp.  The pipelined persistent kernel takes
-  // the 4-pol complex<float> mixed case; the direct-load kernels (4 warps per
-  // block) take every other shape.
-  const bool pipe = precision == LEAP_PRECISION_MIXED && P == 4 && in.vis_type == LEAP_VIS_C64 && in.has_map;
-  const int dpw = precision == LEAP_PRECISION_FP64 ? 2 : 4;
   const int tiles = (nbl + 31) / 32;
-  const int dgroups = (ndir + 4 * dpw - 1) / (4 * dpw);
-  const int pipe_dgroups = (ndir + kPipeNC * 4 - 1) / (kPipeNC * 4);
-  int t_per, c_per, nts, ncs;
-  if (pipe) {
-    choose_pipe_slabs(T, static_cast<int64_t>(tiles) * pipe_dgroups, ctx->sms, t_per, nts);
-    c_per = C;
-    ncs = 1;
-  } else {
-    choose_slabs(T, C, static_cast<int64_t>(tiles) * dgroups, t_per, c_per, nts, ncs);
+  bool all_pipe = precision == LEAP_PRECISION_MIXED && P == 4;
+  int maxC = 0;
+  int min_ndir = D;
+  for (const auto& w : items) {
+    const Integration& in = ctx->integ.at(w.slot);
+    all_pipe = all_pipe && in.vis_type == LEAP_VIS_C64 && in.has_map;
+    maxC = std::max(maxC, in.channels);
+    min_ndir = std::min(min_ndir, w.ndir);
   }
-  const int nslab = nts * ncs;
-  const int64_t avg_elems = static_cast<int64_t>(ndir) * P * nbl;
-
-  LEAP_CUDA(ctx->avg.ensure(sizeof(double2) * avg_elems), "alloc avgData");
-  if (nslab > 1) LEAP_CUDA(ctx->partial.ensure(sizeof(double2) * avg_elems * nslab), "alloc partial sums");
-  LEAP_CUDA(ctx->lambda.ensure(sizeof(double) * C), "alloc wavelengths");
-  LEAP_CUDA(ctx->dirk.ensure(sizeof(float) * 12 * ndir), "alloc direction constants");
-  LEAP_CUDA(ctx->cal1.ensure(sizeof(double) * ndir * md.S), "alloc cal1");
-  LEAP_CUDA(ctx->dphi.ensure(sizeof(double) * static_cast<size_t>(ndir) * md.Kpad), "alloc dphi");
-  const int kchunk = 512;
-  const int nk = (md.Arows + kchunk - 1) / kchunk;
-  LEAP_CUDA(ctx->gemm_partial.ensure(sizeof(double) * static_cast<size_t>(nk) * ndir * md.S), "alloc gemm partial");
-
   // Channel wavelengths, computed exactly as Constants::GetChannelWavelength does;
   // uploaded only when the channel count or the spectral window changes.
-  if (ctx->lambda_host.size() != static_cast<size_t>(C) || ctx->lambda_f0 != md.k.freq_start_hz ||
+  LEAP_CUDA(ctx->lambda.ensure(sizeof(double) * maxC), "alloc wavelengths");
+  if (ctx->lambda_host.size() != static_cast<size_t>(maxC) || ctx->lambda_f0 != md.k.freq_start_hz ||
       ctx->lambda_df != md.k.freq_inc_hz) {
-    ctx->lambda_host.resize(C);
-    for (int c = 0; c < C; ++c) ctx->lambda_host[c] = kSpeedOfLight / (md.k.freq_start_hz + c * md.k.freq_inc_hz);
+    ctx->lambda_host.resize(maxC);
+    for (int c = 0; c < maxC; ++c) ctx->lambda_host[c] = kSpeedOfLight / (md.k.freq_start_hz + c * md.k.freq_inc_hz);
     ctx->lambda_f0 = md.k.freq_start_hz;
     ctx->lambda_df = md.k.freq_inc_hz;
-    LEAP_CUDA(cudaMemcpyAsync(ctx->lambda.ptr, ctx->lambda_host.data(), sizeof(double) * C, cudaMemcpyHostToDevice, s),
+    LEAP_CUDA(cudaMemcpyAsync(ctx->lambda.ptr, ctx->lambda_host.data(), sizeof(double) * maxC, cudaMemcpyHostToDevice, s),
               "upload wavelengths");
   }
 
-  RotateArgs ra{};
-  ra.vis = in.vis.ptr;
-  ra.uvw = in.uvw.as<double>();
-  ra.dd = d_dd;
-  ra.lambda = ctx->lambda.as<double>();
-  ra.twiddle = ctx->twiddle.as<float2>();
-  ra.uvw_f = in.uvw_f.as<float>();
-  ra.dirk = ctx->dirk.as<float>();
-  ra.rows = in.rows;
-  ra.channels = C;
-  ra.pols = P;
-  ra.nbl = nbl;
-  ra.timesteps = T;
-  ra.ndir = ndir;
-  ra.f0 = md.k.freq_start_hz;
-  ra.df = md.k.freq_inc_hz;
-  ra.t_per_slab = t_per;
-  ra.c_per_slab = c_per;
-  ra.n_tslab = nts;
-  ra.n_cslab = ncs;
-  ra.out = nslab > 1 ? ctx->partial.as<double2>() : ctx->avg.as<double2>();
-  ra.err = ctx->dev_err.as<int>();
-
-  int kernels = 0;
-  cudaEvent_t* ev = ctx->ring[ctx->ring_count % leap_ctx::kRing];
-  cudaEventRecord(ev[0], s);
-
-  const int nI1 = md.A1rows - 1;
-  const bool refant = precision == LEAP_PRECISION_MIXED && nI1 > 0;
-  if (refant) LEAP_CUDA(cudaEventRecord(ctx->fork, s), "fork");
-  if (pipe) {
-    direction_constants<<<(ndir + 63) / 64, 64, 0, s>>>(d_dd, ndir, md.k.freq_start_hz, md.k.freq_inc_hz,
-                                                       ctx->dirk.as<float>());
-    ++kernels;
-    PipeArgs pa{};
-    pa.a = ra;
-    pa.tiles = tiles;
-    pa.dgroups = pipe_dgroups;
-    pa.nslab = nslab;
-    const int units = tiles * pipe_dgroups * nslab;
-    const int grid = std::min(units, ctx->sms);
-    if (!ctx->pipe_attr_set) {
-      LEAP_CUDA(cudaFuncSetAttribute(rotate_average_mixed_pipe<kPipeNC, 4>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                     kPipeSmem), "set shared memory size");
-      ctx->pipe_attr_set = true;
+  if (all_pipe) {
+    // Tiles per block: 4 when items hold at most 8 directions (one block covers
+    // 128 baselines x 8 directions), else 1 (32 baselines x 32 directions).
+    const int tpb = (ctx->tune.tpb > 0) ? ctx->tune.tpb : (min_ndir <= 8 ? 4 : 1);
+    const int wpt = kPipeNC / tpb;
+    const int tgroups = (tiles + tpb - 1) / tpb;
+    int64_t work = 0;  // timestep-channels x unit multiplicity, for the slab plan
+    for (const auto& w : items) {
+      const Integration& in = ctx->integ.at(w.slot);
+      work += (in.rows / nbl) * in.channels * static_cast<int64_t>(tgroups) * ((w.ndir + wpt * kPipeDPW - 1) / (wpt * kPipeDPW));
     }
-    rotate_average_mixed_pipe<kPipeNC, 4><<<grid, kPipeNC * 32, kPipeSmem, s>>>(in.vis_map, pa);
-  } else {
+    // Target work per unit: enough units for ~target_waves rounds of the persistent grid.
+    const int waves = ctx->tune.waves > 0 ? ctx->tune.waves : 4;
+    const int64_t per_unit = std::max<int64_t>(1, work / (static_cast<int64_t>(ctx->sms) * waves));
+    std::vector<PipeItem>& pit = ctx->pipe_items_host;
+    std::vector<ReduceItem>& red = ctx->reduce_items_host;
+    pit.assign(items.size(), PipeItem{});
+    red.clear();
+    int units = 0;
+    int64_t partial_elems = 0;
+    std::vector<int64_t> partial_off(items.size(), -1);
+    for (size_t i = 0; i < items.size(); ++i) {
+      const WorkItem& w = items[i];
+      Integration& in = ctx->integ.at(w.slot);
+      const int T = static_cast<int>(in.rows / nbl);
+      const int C = in.channels;
+      PipeItem& it = pit[i];
+      it.map = tpb == 4 ? in.map8 : in.map16;
+      it.uvw_f = in.uvw_f.as<float>();
+      it.rows = in.rows;
+      it.T = T;
+      it.C = C;
+      int tps;
+      if (items.size() == 1 && ctx->tune.waves <= 0) {
+        int nts;
+        choose_pipe_slabs(T, static_cast<int64_t>(tgroups) * ((w.ndir + wpt * kPipeDPW - 1) / (wpt * kPipeDPW)),
+                          ctx->sms, tps, nts);
+      } else {
+        tps = static_cast<int>(std::max<int64_t>(1, std::min<int64_t>(T, (per_unit + C - 1) / C)));
+      }
+      it.t_per_slab = tps;
+      it.nslab = (T + tps - 1) / tps;
+      it.tgroups = tgroups;
+      it.dgroups = (w.ndir + wpt * kPipeDPW - 1) / (wpt * kPipeDPW);
+      it.dir0 = w.dir0;
+      it.ndir = w.ndir;
+      it.unit_begin = units;
+      units += it.tgroups * it.dgroups * it.nslab;
+      if (it.nslab > 1) {
+        partial_off[i] = partial_elems;
+        partial_elems += static_cast<int64_t>(it.nslab) * w.ndir * 4 * nbl;
+      }
+    }
+    if (units == 0) return LEAP_OK;
+    if (partial_elems) LEAP_CUDA(ctx->partial.ensure(sizeof(double2) * partial_elems), "alloc partial sums");
+    for (size_t i = 0; i < items.size(); ++i) {
+      PipeItem& it = pit[i];
+      if (it.nslab > 1) {
+        it.out = ctx->partial.as<double2>() + partial_off[i];
+        red.push_back(ReduceItem{it.out, static_cast<int64_t>(it.dir0) * 4 * nbl, it.nslab, it.ndir});
+      } else {
+        it.out = ctx->avg.as<double2>() + static_cast<int64_t>(it.dir0) * 4 * nbl;
+      }
+    }
+    LEAP_CUDA(ctx->pipe_items.ensure(sizeof(PipeItem) * pit.size()), "alloc item table");
+    if (!ctx->capturing)
+      LEAP_CUDA(cudaMemcpyAsync(ctx->pipe_items.ptr, pit.data(), sizeof(PipeItem) * pit.size(), cudaMemcpyHostToDevice, s),
+                "upload item table");
+    if (!red.empty() && !ctx->capturing) {
+      LEAP_CUDA(ctx->reduce_items.ensure(sizeof(ReduceItem) * red.size()), "alloc reduce table");
+      LEAP_CUDA(cudaMemcpyAsync(ctx->reduce_items.ptr, red.data(), sizeof(ReduceItem) * red.size(),
+                                cudaMemcpyHostToDevice, s),
+                "upload reduce table");
+    }
+    direction_constants<<<(D + 63) / 64, 64, 0, s>>>(d_dd, D, md.k.freq_start_hz, md.k.freq_inc_hz,
+                                                     ctx->dirk.as<float>());
+    ++kernels;
+    PipeParams pp{};
+    pp.items = ctx->pipe_items.as<PipeItem>();
+    pp.nitems = static_cast<int32_t>(pit.size());
+    pp.units = units;
+    pp.nbl = nbl;
+    pp.dirk = ctx->dirk.as<float>();
+    pp.twiddle = ctx->twiddle.as<float2>();
+    pp.err = ctx->dev_err.as<int>();
+    const int grid = std::min(units, ctx->sms);
+    if (tpb == 4) {
+      if (!ctx->pipe_attr_set4) {
+        LEAP_CUDA(cudaFuncSetAttribute(rotate_average_mixed_pipe<kPipeNC, kPipeDPW, 4>,
+                                       cudaFuncAttributeMaxDynamicSharedMemorySize, pipe_smem_bytes<4>()),
+                  "set shared memory size");
+        ctx->pipe_attr_set4 = true;
+      }
+      rotate_average_mixed_pipe<kPipeNC, kPipeDPW, 4><<<grid, kPipeNC * 32, pipe_smem_bytes<4>(), s>>>(pp);
+    } else {
+      if (!ctx->pipe_attr_set) {
+        LEAP_CUDA(cudaFuncSetAttribute(rotate_average_mixed_pipe<kPipeNC, kPipeDPW, 1>,
+                                       cudaFuncAttributeMaxDynamicSharedMemorySize, pipe_smem_bytes<1>()),
+                  "set shared memory size");
+        ctx->pipe_attr_set = true;
+      }
+      rotate_average_mixed_pipe<kPipeNC, kPipeDPW, 1><<<grid, kPipeNC * 32, pipe_smem_bytes<1>(), s>>>(pp);
+    }
+    ++kernels;
+    if (!red.empty()) {
+      int64_t maxn = 0;
+      for (const auto& r : red) maxn = std::max<int64_t>(maxn, static_cast<int64_t>(r.ndir) * 4 * nbl);
+      const dim3 rg(static_cast<unsigned>(std::min<int64_t>((maxn + 255) / 256, 1024)), static_cast<unsigned>(red.size()));
+      reduce_item_slabs<<<rg, 256, 0, s>>>(ctx->reduce_items.as<ReduceItem>(), static_cast<int>(red.size()), 4 * nbl,
+                                            ctx->avg.as<double2>());
+      ++kernels;
+    }
+    return LEAP_OK;
+  }
+
+  // Direct-load kernels, one launch per item.
+  for (const auto& w : items) {
+    Integration& in = ctx->integ.at(w.slot);
+    const int T = static_cast<int>(in.rows / nbl);
+    const int C = in.channels;
+    const int dpw = precision == LEAP_PRECISION_FP64 ? 2 : 4;
+    const int dgroups = (w.ndir + 4 * dpw - 1) / (4 * dpw);
+    int t_per, c_per, nts, ncs;
+    choose_slabs(T, C, static_cast<int64_t>(tiles) * dgroups, t_per, c_per, nts, ncs);
+    const int nslab = nts * ncs;
+    const int64_t n = static_cast<int64_t>(w.ndir) * P * nbl;
+    if (nslab > 1) LEAP_CUDA(ctx->partial.ensure(sizeof(double2) * n * nslab), "alloc partial sums");
+    RotateArgs ra{};
+    ra.vis = in.vis.ptr;
+    ra.uvw = in.uvw.as<double>();
+    ra.dd = d_dd + 9 * static_cast<int64_t>(w.dir0);
+    ra.lambda = ctx->lambda.as<double>();
+    ra.twiddle = ctx->twiddle.as<float2>();
+    ra.rows = in.rows;
+    ra.channels = C;
+    ra.pols = P;
+    ra.nbl = nbl;
+    ra.timesteps = T;
+    ra.ndir = w.ndir;
+    ra.f0 = md.k.freq_start_hz;
+    ra.df = md.k.freq_inc_hz;
+    ra.t_per_slab = t_per;
+    ra.c_per_slab = c_per;
+    ra.n_tslab = nts;
+    ra.n_cslab = ncs;
+    double2* avg_item = ctx->avg.as<double2>() + static_cast<int64_t>(w.dir0) * P * nbl;
+    ra.out = nslab > 1 ? ctx->partial.as<double2>() : avg_item;
+    ra.err = ctx->dev_err.as<int>();
     const dim3 grid(tiles, dgroups, nslab);
     int rc = in.vis_type == LEAP_VIS_C64 ? dispatch_pols<float2>(ra, grid, precision, s)
                                          : dispatch_pols<double2>(ra, grid, precision, s);
     if (rc != 0) return fail(ctx, LEAP_ERR_INVALID_ARGUMENT, "unsupported polarisation count (1, 2 or 4)");
-  }
-  ++kernels;
-  // Mixed form: FP64 sums of pol 0 of the reference-antenna baselines, on the
-  // aux stream so that the FP64 pipe works while the FP32 bulk kernel runs.
-  if (refant) {
-    // complex<float> input: compensated FP32 kernel, about 4 blocks per SM over
-    // timestep slabs.  complex<double> input keeps the FP64 kernel.
-    const bool df = in.vis_type == LEAP_VIS_C64;
-    const int rdpw = df ? 4 : 2;
-    int rt_per, rc_per, rnts, rncs;
-    const int rtiles = (nI1 + 31) / 32;
-    const int rdg = (ndir + 4 * rdpw - 1) / (4 * rdpw);
-    if (df) {
-      rnts = static_cast<int>(std::min<int64_t>(T, std::max<int64_t>(1, (4 * ctx->sms) / (rtiles * rdg))));
-      rt_per = (T + rnts - 1) / rnts;
-      rnts = (T + rt_per - 1) / rt_per;
-      rc_per = C;
-      rncs = 1;
-    } else {
-      choose_slabs_target(T, C, static_cast<int64_t>(rtiles) * rdg, ctx->sms, rt_per, rc_per, rnts, rncs);
-    }
-    const int rslab = rnts * rncs;
-    const int64_t n_i1 = static_cast<int64_t>(ndir) * nI1;
-    LEAP_CUDA(ctx->avg_i1.ensure(sizeof(double2) * n_i1), "alloc I1 sums");
-    if (rslab > 1) LEAP_CUDA(ctx->partial_i1.ensure(sizeof(double2) * n_i1 * rslab), "alloc I1 partials");
-    RotateArgs rr = ra;
-    rr.t_per_slab = rt_per;
-    rr.c_per_slab = rc_per;
-    rr.n_tslab = rnts;
-    rr.n_cslab = rncs;
-    LEAP_CUDA(cudaStreamWaitEvent(ctx->aux, ctx->fork, 0), "fork");
-    double2* dst = rslab > 1 ? ctx->partial_i1.as<double2>() : ctx->avg_i1.as<double2>();
-    const dim3 rgrid(rtiles, rdg, rslab);
-    if (df)
-      refant_average_df<4><<<rgrid, 128, 0, ctx->aux>>>(rr, md.I1.as<int32_t>(), nI1, ctx->twiddle_df.as<float4>(), dst);
-    else
-      refant_average_fp64<double2, 2><<<rgrid, 128, 0, ctx->aux>>>(rr, md.I1.as<int32_t>(), nI1, dst);
     ++kernels;
-    if (rslab > 1) {
-      reduce_slabs<<<grid_1d(n_i1, 256), 256, 0, ctx->aux>>>(ctx->partial_i1.as<double2>(), rslab, n_i1,
-                                                             ctx->avg_i1.as<double2>());
+    if (nslab > 1) {
+      reduce_slabs<<<grid_1d(n, 256), 256, 0, s>>>(ctx->partial.as<double2>(), nslab, n, avg_item);
       ++kernels;
     }
-    LEAP_CUDA(cudaEventRecord(ctx->join, ctx->aux), "join");
   }
-  if (nslab > 1) {
-    reduce_slabs<<<grid_1d(avg_elems, 256), 256, 0, s>>>(ctx->partial.as<double2>(), nslab, avg_elems,
-                                                            ctx->avg.as<double2>());
-    ++kernels;
-  }
-  cudaEventRecord(ev[1], s);
+  return LEAP_OK;
+}
 
+// Mixed form: compensated sums of pol 0 of the reference-antenna baselines into
+// ctx->avg_i1 ([D][nI1]), on the aux stream.  complex<float> items go through
+// one item-table launch; complex<double> items keep the FP64 kernel.
+int refant_stage(leap_ctx* ctx, const std::vector<WorkItem>& items, const double* d_dd, int32_t D, int& kernels) {
+  Metadata& md = ctx->md;
+  const int32_t nbl = static_cast<int32_t>(md.k.nbaselines);
+  const int nI1 = md.A1rows - 1;
+  const int rtiles = (nI1 + 31) / 32;
+  cudaStream_t a = ctx->aux;
+  LEAP_CUDA(ctx->avg_i1.ensure(sizeof(double2) * static_cast<int64_t>(D) * nI1), "alloc I1 sums");
+  std::vector<RefantItem>& rit = ctx->refant_items_host;
+  std::vector<ReduceItem>& red = ctx->refant_reduce_host;
+  rit.clear();
+  red.clear();
+  int64_t partial_elems = 0;
+  std::vector<int64_t> off;
+  int blocks = 0;
+  // Each block sums <= 4*DPW directions of 32 reference baselines over a slab;
+  // about 8 blocks per SM in total.
+  int64_t base_total = 0;
+  for (const auto& w : items) base_total += static_cast<int64_t>(rtiles) * ((w.ndir + 7) / 8);
+  for (const auto& w : items) {
+    Integration& in = ctx->integ.at(w.slot);
+    const int T = static_cast<int>(in.rows / nbl);
+    if (in.vis_type != LEAP_VIS_C64) {
+      // FP64 kernel for complex<double> input, one launch per item.
+      int rt_per, rc_per, rnts, rncs;
+      const int rdg = (w.ndir + 7) / 8;
+      choose_slabs_target(T, in.channels, static_cast<int64_t>(rtiles) * rdg, ctx->sms, rt_per, rc_per, rnts, rncs);
+      const int rslab = rnts * rncs;
+      const int64_t n = static_cast<int64_t>(w.ndir) * nI1;
+      LEAP_CUDA(ctx->partial_i1.ensure(sizeof(double2) * n * rslab), "alloc I1 partials");
+      RotateArgs rr{};
+      rr.vis = in.vis.ptr;
+      rr.uvw = in.uvw.as<double>();
+      rr.dd = d_dd + 9 * static_cast<int64_t>(w.dir0);
+      rr.lambda = ctx->lambda.as<double>();
+      rr.rows = in.rows;
+      rr.channels = in.channels;
+      rr.pols = in.pols;
+      rr.nbl = nbl;
+      rr.timesteps = T;
+      rr.ndir = w.ndir;
+      rr.f0 = md.k.freq_start_hz;
+      rr.df = md.k.freq_inc_hz;
+      rr.t_per_slab = rt_per;
+      rr.c_per_slab = rc_per;
+      rr.n_tslab = rnts;
+      rr.n_cslab = rncs;
+      double2* dst = ctx->avg_i1.as<double2>() + static_cast<int64_t>(w.dir0) * nI1;
+      const dim3 rgrid(rtiles, rdg, rslab);
+      refant_average_fp64<double2, 2><<<rgrid, 128, 0, a>>>(rr, md.I1.as<int32_t>(), nI1,
+                                                             rslab > 1 ? ctx->partial_i1.as<double2>() : dst);
+      ++kernels;
+      if (rslab > 1) {
+        reduce_slabs<<<grid_1d(n, 256), 256, 0, a>>>(ctx->partial_i1.as<double2>(), rslab, n, dst);
+        ++kernels;
+      }
+      continue;
+    }
+    RefantItem r{};
+    r.vis = in.vis.as<float2>();
+    r.uvw = in.uvw.as<double>();
+    r.dd = d_dd + 9 * static_cast<int64_t>(w.dir0);
+    r.rows = in.rows;
+    r.T = T;
+    r.C = in.channels;
+    r.pols = in.pols;
+    r.ndir = w.ndir;
+    r.dgroups = (w.ndir + 7) / 8;  // 4 warps x 2 directions
+    const int64_t want = std::max<int64_t>(1, (8 * static_cast<int64_t>(ctx->sms) + base_total - 1) / base_total);
+    r.n_tslab = static_cast<int>(std::min<int64_t>(T, want));
+    r.t_per_slab = (T + r.n_tslab - 1) / r.n_tslab;
+    r.n_tslab = (T + r.t_per_slab - 1) / r.t_per_slab;
+    const int64_t rest = (want + r.n_tslab - 1) / r.n_tslab;
+    r.n_cslab = static_cast<int>(std::min<int64_t>(rest, std::max(1, in.channels / 16)));
+    r.c_per_slab = (in.channels + r.n_cslab - 1) / r.n_cslab;
+    r.n_cslab = (in.channels + r.c_per_slab - 1) / r.c_per_slab;
+    r.block_begin = blocks;
+    blocks += rtiles * r.dgroups * r.n_tslab * r.n_cslab;
+    off.push_back(partial_elems);
+    partial_elems += static_cast<int64_t>(r.n_tslab) * r.n_cslab * w.ndir * nI1;
+    rit.push_back(r);
+    red.push_back(ReduceItem{nullptr, static_cast<int64_t>(w.dir0) * nI1, r.n_tslab * r.n_cslab, w.ndir});
+  }
+  if (rit.empty()) return LEAP_OK;
+  LEAP_CUDA(ctx->partial_i1.ensure(sizeof(double2) * partial_elems), "alloc I1 partials");
+  for (size_t i = 0; i < rit.size(); ++i) {
+    rit[i].out = ctx->partial_i1.as<double2>() + off[i];
+    red[i].partial = rit[i].out;
+  }
+  LEAP_CUDA(ctx->refant_items.ensure(sizeof(RefantItem) * rit.size()), "alloc refant table");
+  LEAP_CUDA(ctx->refant_reduce.ensure(sizeof(ReduceItem) * red.size()), "alloc refant reduce table");
+  if (!ctx->capturing) {
+    LEAP_CUDA(cudaMemcpyAsync(ctx->refant_items.ptr, rit.data(), sizeof(RefantItem) * rit.size(), cudaMemcpyHostToDevice,
+                              a),
+              "upload refant table");
+    LEAP_CUDA(cudaMemcpyAsync(ctx->refant_reduce.ptr, red.data(), sizeof(ReduceItem) * red.size(),
+                              cudaMemcpyHostToDevice, a),
+              "upload refant reduce table");
+  }
+  refant_average_df_items<2><<<blocks, 128, 0, a>>>(ctx->refant_items.as<RefantItem>(), static_cast<int>(rit.size()), nbl,
+                                                    md.k.freq_start_hz, md.k.freq_inc_hz, md.I1.as<int32_t>(), nI1,
+                                                    ctx->twiddle_df.as<float4>());
+  ++kernels;
+  int64_t maxn = 0;
+  for (const auto& r : red) maxn = std::max<int64_t>(maxn, static_cast<int64_t>(r.ndir) * nI1);
+  const dim3 rg(static_cast<unsigned>(std::min<int64_t>((maxn + 255) / 256, 1024)), static_cast<unsigned>(red.size()));
+  reduce_item_slabs<<<rg, 256, 0, a>>>(ctx->refant_reduce.as<ReduceItem>(), static_cast<int>(red.size()), nI1,
+                                        ctx->avg_i1.as<double2>());
+  ++kernels;
+  return LEAP_OK;
+}
+
+// Phase angles + both contractions for all D directions: avg -> cal.
+int solve_stage(leap_ctx* ctx, int32_t D, int32_t precision, int P, bool refant, double* d_cal, cudaStream_t s,
+                int& kernels) {
+  Metadata& md = ctx->md;
+  const int32_t nbl = static_cast<int32_t>(md.k.nbaselines);
+  const int kchunk = 512;
+  const int nk = (md.Arows + kchunk - 1) / kchunk;
   SolveArgs sa{};
   sa.avg = ctx->avg.as<double2>();
   sa.nbl = nbl;
   sa.pols = P;
-  sa.ndir = ndir;
+  sa.ndir = D;
   sa.S = md.S;
   sa.I1 = md.I1.as<int32_t>();
   sa.Ad1 = md.Ad1.as<double>();
@@ -377,30 +554,185 @@ int calibrate_impl(leap_ctx* ctx, int32_t slot, const double* d_dd, int32_t ndir
   sa.cal1 = ctx->cal1.as<double>();
   sa.dphi = ctx->dphi.ptr;
   sa.avg_i1 = refant ? ctx->avg_i1.as<double2>() : nullptr;
-  if (refant) LEAP_CUDA(cudaStreamWaitEvent(s, ctx->join, 0), "join");
-  solve_cal1<<<ndir, 256, sizeof(double) * md.A1rows, s>>>(sa);
+  solve_cal1<<<D, 256, sizeof(double) * md.A1rows, s>>>(sa);
   ++kernels;
-  const dim3 gd((md.Kpad + 255) / 256, ndir);
-  const dim3 gg((md.S + 63) / 64, (ndir + 15) / 16, nk);
+  const dim3 gd((md.Kpad + 255) / 256, D);
+  const dim3 gg((md.S + 63) / 64, (D + 15) / 16, nk);
   if (precision == LEAP_PRECISION_FP64) {
     solve_dint_fp64<<<gd, 256, 0, s>>>(sa);
-    gemm_ad_partial<double><<<gg, 256, 0, s>>>(md.Ad.as<double>(), md.S, md.Arows, static_cast<double*>(sa.dphi),
-                                                md.Kpad, ndir, kchunk, ctx->gemm_partial.as<double>());
+    gemm_ad_partial<double><<<gg, 256, 0, s>>>(md.Ad.as<double>(), md.S, md.Arows, static_cast<double*>(sa.dphi), md.Kpad,
+                                                D, kchunk, ctx->gemm_partial.as<double>());
   } else {
     solve_dint_mixed<<<gd, 256, 0, s>>>(sa);
     gemm_ad_partial<float><<<gg, 256, 0, s>>>(md.Ad_f32.as<float>(), md.S, md.Arows, static_cast<float*>(sa.dphi),
-                                               md.Kpad, ndir, kchunk, ctx->gemm_partial.as<double>());
+                                               md.Kpad, D, kchunk, ctx->gemm_partial.as<double>());
   }
-  gemm_ad_finish<<<(ndir * md.S + 255) / 256, 256, 0, s>>>(ctx->gemm_partial.as<double>(), nk, ndir, md.S,
-                                                           ctx->cal1.as<double>(), d_cal);
+  gemm_ad_finish<<<(D * md.S + 255) / 256, 256, 0, s>>>(ctx->gemm_partial.as<double>(), nk, D, md.S,
+                                                        ctx->cal1.as<double>(), d_cal);
   kernels += 3;
-  cudaEventRecord(ev[2], s);
-  ctx->ring_count++;
+  return LEAP_OK;
+}
+
+// The whole calibration of a list of work items with D directions in total.
+int calibrate_items(leap_ctx* ctx, const std::vector<WorkItem>& items, const double* d_dd, int32_t D, int32_t precision,
+                    double* d_cal, cudaStream_t s) {
+  if (!ctx->md.set) return fail(ctx, LEAP_ERR_NOT_READY, "metadata not set");
+  if (D <= 0 || items.empty()) return fail(ctx, LEAP_ERR_INVALID_ARGUMENT, "ndirections must be positive");
+  if (precision != LEAP_PRECISION_FP64 && precision != LEAP_PRECISION_MIXED)
+    return fail(ctx, LEAP_ERR_INVALID_ARGUMENT, "unknown precision");
+  Metadata& md = ctx->md;
+  const int32_t nbl = static_cast<int32_t>(md.k.nbaselines);
+  int P = -1;
+  for (const auto& w : items) {
+    auto it = ctx->integ.find(w.slot);
+    if (it == ctx->integ.end()) return fail(ctx, LEAP_ERR_NOT_READY, "integration slot not set");
+    if (w.ndir <= 0 || w.dir0 < 0 || w.dir0 + w.ndir > D)
+      return fail(ctx, LEAP_ERR_INVALID_ARGUMENT, "work item directions out of range");
+    if (it->second.rows % nbl != 0)
+      return fail(ctx, LEAP_ERR_INVALID_ARGUMENT, "integration rows not a multiple of the baseline count");
+    if (P >= 0 && it->second.pols != P) return fail(ctx, LEAP_ERR_INVALID_ARGUMENT, "work items differ in pols");
+    P = it->second.pols;
+  }
+  const int64_t avg_elems = static_cast<int64_t>(D) * P * nbl;
+  const int kchunk = 512;
+  const int nk = (md.Arows + kchunk - 1) / kchunk;
+  LEAP_CUDA(ctx->avg.ensure(sizeof(double2) * avg_elems), "alloc avgData");
+  LEAP_CUDA(ctx->dirk.ensure(sizeof(float) * 12 * D), "alloc direction constants");
+  LEAP_CUDA(ctx->cal1.ensure(sizeof(double) * D * md.S), "alloc cal1");
+  LEAP_CUDA(ctx->dphi.ensure(sizeof(double) * static_cast<size_t>(D) * md.Kpad), "alloc dphi");
+  LEAP_CUDA(ctx->gemm_partial.ensure(sizeof(double) * static_cast<size_t>(nk) * D * md.S), "alloc gemm partial");
+
+  int kernels = 0;
+  cudaEvent_t* ev = ctx->ring[ctx->ring_count % leap_ctx::kRing];
+  if (!ctx->capturing) cudaEventRecord(ev[0], s);
+  const bool refant = precision == LEAP_PRECISION_MIXED && md.A1rows > 1;
+  if (refant) {
+    LEAP_CUDA(cudaEventRecord(ctx->fork, s), "fork");
+    LEAP_CUDA(cudaStreamWaitEvent(ctx->aux, ctx->fork, 0), "fork");
+  }
+  int rc = rotate_stage(ctx, items, d_dd, D, precision, P, s, kernels);
+  if (rc != LEAP_OK) return rc;
+  if (refant) {
+    // Launched after the bulk kernel so that the persistent blocks take the SMs first.
+    rc = refant_stage(ctx, items, d_dd, D, kernels);
+    if (rc != LEAP_OK) return rc;
+    LEAP_CUDA(cudaEventRecord(ctx->join, ctx->aux), "join");
+  }
+  if (!ctx->capturing) cudaEventRecord(ev[1], s);
+  if (refant) LEAP_CUDA(cudaStreamWaitEvent(s, ctx->join, 0), "join");
+  rc = solve_stage(ctx, D, precision, P, refant, d_cal, s, kernels);
+  if (rc != LEAP_OK) return rc;
+  if (!ctx->capturing) {
+    cudaEventRecord(ev[2], s);
+    ctx->ring_count++;
+  }
   LEAP_CUDA(cudaGetLastError(), "kernel launch");
-  ctx->last_ndir = ndir;
+  ctx->last_ndir = D;
   ctx->last_pols = P;
   ctx->last_nbl = nbl;
   ctx->kernels_last = kernels;
+  return LEAP_OK;
+}
+
+int calibrate_impl(leap_ctx* ctx, int32_t slot, const double* d_dd, int32_t ndir, int32_t precision, double* d_cal,
+                   cudaStream_t s) {
+  if (ndir <= 0) return fail(ctx, LEAP_ERR_INVALID_ARGUMENT, "ndirections must be positive");
+  return calibrate_items(ctx, {WorkItem{slot, 0, ndir}}, d_dd, ndir, precision, d_cal, s);
+}
+
+std::string batch_key(const std::vector<WorkItem>& items, int32_t D, int32_t precision) {
+  std::string k = std::to_string(D) + ":" + std::to_string(precision);
+  for (const auto& w : items) k += "|" + std::to_string(w.slot) + "," + std::to_string(w.dir0) + "," + std::to_string(w.ndir);
+  return k;
+}
+
+// Autotuner: time each candidate launch plan of the batched call with CUDA
+// events (after one warm-up run) and keep the fastest for this shape.
+int autotune_batch(leap_ctx* ctx, const std::vector<WorkItem>& items, int32_t D, int32_t precision,
+                   const std::string& key) {
+  int min_ndir = D;
+  for (const auto& w : items) min_ndir = std::min(min_ndir, w.ndir);
+  std::vector<TuneChoice> cands;
+  const int tpbs[2] = {1, 4};
+  for (int tpb : tpbs) {
+    if (tpb == 4 && min_ndir > 8) continue;
+    for (int waves : {2, 4, 8}) cands.push_back(TuneChoice{tpb, waves});
+  }
+  cudaEvent_t e0, e1;
+  LEAP_CUDA(cudaEventCreate(&e0), "tuning event");
+  LEAP_CUDA(cudaEventCreate(&e1), "tuning event");
+  float best = 1e30f;
+  TuneChoice choice{};
+  for (const auto& c : cands) {
+    ctx->tune = c;
+    int rc = calibrate_items(ctx, items, ctx->dd.as<double>(), D, precision, ctx->cal.as<double>(), ctx->stream);
+    if (rc != LEAP_OK) break;
+    cudaEventRecord(e0, ctx->stream);
+    rc = calibrate_items(ctx, items, ctx->dd.as<double>(), D, precision, ctx->cal.as<double>(), ctx->stream);
+    cudaEventRecord(e1, ctx->stream);
+    if (rc != LEAP_OK) break;
+    cudaEventSynchronize(e1);
+    float ms = 0.f;
+    cudaEventElapsedTime(&ms, e0, e1);
+    if (ms < best) {
+      best = ms;
+      choice = c;
+    }
+  }
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  ctx->tune = choice;
+  ctx->tuned[key] = choice;
+  return LEAP_OK;
+}
+
+int calibrate_batched_impl(leap_ctx* ctx, const leap_work_item* witems, int32_t nitems, int32_t D, int32_t precision) {
+  if (!witems || nitems <= 0) return fail(ctx, LEAP_ERR_INVALID_ARGUMENT, "no work items");
+  std::vector<WorkItem> items(nitems);
+  for (int i = 0; i < nitems; ++i) items[i] = WorkItem{witems[i].slot, witems[i].first_direction, witems[i].ndirections};
+  const std::string key = batch_key(items, D, precision);
+  cudaStream_t s = ctx->stream;
+  if (ctx->graph_exec && ctx->graph_key == key && ctx->graph_epoch == g_alloc_epoch) {
+    cudaEvent_t* ev = ctx->ring[ctx->ring_count % leap_ctx::kRing];
+    cudaEventRecord(ev[0], s);
+    cudaEventRecord(ev[1], s);
+    LEAP_CUDA(cudaGraphLaunch(ctx->graph_exec, s), "graph launch");
+    cudaEventRecord(ev[2], s);
+    ctx->ring_count++;
+    return LEAP_OK;
+  }
+  auto t = ctx->tuned.find(key);
+  if (t != ctx->tuned.end()) {
+    ctx->tune = t->second;
+  } else if (ctx->autotune) {
+    int rc = autotune_batch(ctx, items, D, precision, key);
+    if (rc != LEAP_OK) return rc;
+  } else {
+    ctx->tune = TuneChoice{};
+  }
+  // Eager run: allocates and uploads the launch tables, produces this call's result.
+  int rc = calibrate_items(ctx, items, ctx->dd.as<double>(), D, precision, ctx->cal.as<double>(), s);
+  if (rc != LEAP_OK) return rc;
+  // Record the same launches once as a CUDA graph for the next calls of this shape.
+  if (ctx->graph_exec) {
+    cudaGraphExecDestroy(ctx->graph_exec);
+    ctx->graph_exec = nullptr;
+  }
+  cudaGraph_t graph = nullptr;
+  LEAP_CUDA(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal), "begin capture");
+  ctx->capturing = true;
+  const int kernels = ctx->kernels_last;
+  rc = calibrate_items(ctx, items, ctx->dd.as<double>(), D, precision, ctx->cal.as<double>(), s);
+  ctx->capturing = false;
+  const cudaError_t ec = cudaStreamEndCapture(s, &graph);
+  ctx->kernels_last = kernels;
+  if (rc != LEAP_OK) return rc;
+  if (ec != cudaSuccess) return cuda_fail(ctx, ec, "end capture");
+  const cudaError_t ei = cudaGraphInstantiate(&ctx->graph_exec, graph, 0);
+  cudaGraphDestroy(graph);
+  if (ei != cudaSuccess) return cuda_fail(ctx, ei, "instantiate graph");
+  ctx->graph_key = key;
+  ctx->graph_epoch = g_alloc_epoch;
   return LEAP_OK;
 }
 
@@ -510,10 +842,15 @@ void leap_destroy(leap_ctx* ctx) {
         if (ev) cudaEventDestroy(ev);
     if (ctx->stream) cudaStreamDestroy(ctx->stream);
     if (ctx->aux) cudaStreamDestroy(ctx->aux);
+    if (ctx->graph_exec) cudaGraphExecDestroy(ctx->graph_exec);
     if (ctx->fork) cudaEventDestroy(ctx->fork);
     if (ctx->join) cudaEventDestroy(ctx->join);
     ctx->partial_i1.release();
     ctx->avg_i1.release();
+    ctx->pipe_items.release();
+    ctx->reduce_items.release();
+    ctx->refant_items.release();
+    ctx->refant_reduce.release();
   }
   delete ctx;
 }
@@ -618,17 +955,19 @@ int32_t leap_set_integration(leap_ctx* ctx, int32_t slot, int32_t vis_type, cons
   in.pols = pols;
   in.has_map = false;
   if (vis_type == LEAP_VIS_C64 && pols == 4 && rows * 8 < (int64_t(1) << 31)) {
-    // The pipelined kernel's view: 2-D floats [channels][rows*8], box 256 x kPipeChunk.
+    // The pipelined kernel's view: 2-D floats [channels][rows*8], box 256 x (16 or 8) channels.
     auto enc = tensor_map_encoder();
     if (!enc) return fail(ctx, LEAP_ERR_CUDA, "cuTensorMapEncodeTiled unavailable");
     cuuint64_t dims[2] = {static_cast<cuuint64_t>(rows) * 8, static_cast<cuuint64_t>(channels)};
     cuuint64_t strides[1] = {static_cast<cuuint64_t>(rows) * 32};
-    cuuint32_t box[2] = {256, static_cast<cuuint32_t>(kPipeChunk)};
     cuuint32_t estr[2] = {1, 1};
-    CUresult r = enc(&in.vis_map, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 2, in.vis.ptr, dims, strides, box, estr,
-                     CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
-                     CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
-    if (r != CUDA_SUCCESS) return fail(ctx, LEAP_ERR_CUDA, "cuTensorMapEncodeTiled failed: " + std::to_string(r));
+    for (int which = 0; which < 2; ++which) {
+      cuuint32_t box[2] = {256, static_cast<cuuint32_t>(which == 0 ? PipeShape<1>::CH : PipeShape<4>::CH)};
+      CUresult r = enc(which == 0 ? &in.map16 : &in.map8, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 2, in.vis.ptr, dims, strides,
+                       box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
+                       CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+      if (r != CUDA_SUCCESS) return fail(ctx, LEAP_ERR_CUDA, "cuTensorMapEncodeTiled failed: " + std::to_string(r));
+    }
     in.has_map = true;
   }
   return LEAP_OK;
@@ -669,6 +1008,31 @@ int32_t leap_calibrate_async(leap_ctx* ctx, int32_t slot, const double* d_dd, in
   DeviceGuard g(ctx->device);
   cudaStream_t s = stream ? static_cast<cudaStream_t>(stream) : ctx->stream;
   return calibrate_impl(ctx, slot, d_dd, ndir, precision, d_cal_out, s);
+}
+
+int32_t leap_calibrate_batched(leap_ctx* ctx, const leap_work_item* items, int32_t nitems, const double* dd,
+                               int32_t ndirections, int32_t precision, double* cal_out) {
+  if (!ctx || !items || !dd || !cal_out) return fail(ctx, LEAP_ERR_INVALID_ARGUMENT, "NULL argument");
+  if (ndirections <= 0) return fail(ctx, LEAP_ERR_INVALID_ARGUMENT, "ndirections must be positive");
+  if (!ctx->md.set) return fail(ctx, LEAP_ERR_NOT_READY, "metadata not set");
+  DeviceGuard g(ctx->device);
+  const int S = ctx->md.S;
+  LEAP_CUDA(ctx->dd.ensure(sizeof(double) * 9 * ndirections), "alloc dd");
+  LEAP_CUDA(ctx->cal.ensure(sizeof(double) * S * ndirections), "alloc cal");
+  LEAP_CUDA(cudaMemcpyAsync(ctx->dd.ptr, dd, sizeof(double) * 9 * ndirections, cudaMemcpyHostToDevice, ctx->stream),
+            "upload dd");
+  int rc = calibrate_batched_impl(ctx, items, nitems, ndirections, precision);
+  if (rc != LEAP_OK) return rc;
+  LEAP_CUDA(cudaMemcpyAsync(cal_out, ctx->cal.ptr, sizeof(double) * S * ndirections, cudaMemcpyDeviceToHost, ctx->stream),
+            "download cal");
+  LEAP_CUDA(cudaStreamSynchronize(ctx->stream), "calibrate batched");
+  return check_device_error(ctx);
+}
+
+int32_t leap_set_autotune(leap_ctx* ctx, int32_t enable) {
+  if (!ctx) return fail(ctx, LEAP_ERR_INVALID_ARGUMENT, "NULL context");
+  ctx->autotune = enable != 0;
+  return LEAP_OK;
 }
 
 int32_t leap_get_avgdata(leap_ctx* ctx, int32_t direction, double* out) {

@@ -59,6 +59,8 @@ SIGNATURES = {
     "leap_release_integration": ([vp, i32], i32),
     "leap_calibrate": ([vp, i32, vp, i32, i32, vp], i32),
     "leap_calibrate_async": ([vp, i32, vp, i32, i32, vp, vp], i32),
+    "leap_calibrate_batched": ([vp, vp, i32, vp, i32, i32, vp], i32),
+    "leap_set_autotune": ([vp, i32], i32),
     "leap_get_avgdata": ([vp, i32, vp], i32),
     "leap_rotate_uvw": ([vp, i32, vp, i32, vp], i32),
     "leap_get_timings": ([vp, ctypes.POINTER(LeapTimings)], i32),

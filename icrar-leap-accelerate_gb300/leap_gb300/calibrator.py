@@ -232,6 +232,19 @@ class Context:
         self._last_slot = slot
         return cal
 
+    def calibrate_batched(self, items, dds: np.ndarray, precision: int = _abi.LEAP_PRECISION_MIXED) -> np.ndarray:
+        """items: sequence of (slot, first_direction, ndirections); dds: (D, 3, 3)."""
+        dds = np.ascontiguousarray(dds, dtype=np.float64).reshape(-1, 9)
+        D = dds.shape[0]
+        arr = (_abi.LeapWorkItem * len(items))(*[_abi.LeapWorkItem(int(a), int(b), int(c), 0) for a, b, c in items])
+        cal = np.zeros((D, self.md.A.shape[1]), dtype=np.float64)
+        self._check(lib.leap_calibrate_batched(self._h, arr, len(items), _ptr(dds), D, precision, _ptr(cal)))
+        self._last_slot = int(items[0][0])
+        return cal
+
+    def set_autotune(self, enable: bool):
+        self._check(lib.leap_set_autotune(self._h, int(bool(enable))))
+
     def calibrate_async(self, slot: int, dd_ptr: int, ndir: int, precision: int, cal_ptr: int, stream: int = 0):
         self._check(lib.leap_calibrate_async(self._h, slot, dd_ptr, ndir, precision, cal_ptr, stream or None))
 

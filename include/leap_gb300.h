@@ -133,6 +133,22 @@ int32_t leap_calibrate(leap_ctx* ctx, int32_t slot, const double* dd, int32_t nd
 int32_t leap_calibrate_async(leap_ctx* ctx, int32_t slot, const double* d_dd, int32_t ndirections,
                              int32_t precision, double* d_cal_out, void* stream);
 
+/* Calibrate many (integration, direction range) work items in one call, e.g.
+ * hundreds of directions spread over integration chunks of uneven timestep
+ * and channel counts.  Replaces the reference's per-interval, per-direction
+ * loop (LA/algorithm/cuda/CudaLeapCalibrator.cu:159-227) with one persistent
+ * launch over all items and one Ad contraction for all directions.  dd holds
+ * ndirections row-major 3x3 matrices (HOST), items[i] selects
+ * dd[first_direction .. first_direction + ndirections); cal_out (HOST) is
+ * [ndirections][S].  The first call of a new shape tunes the launch plan (see
+ * leap_set_autotune) and records the launches as a CUDA graph, which later
+ * calls of the same shape replay. */
+int32_t leap_calibrate_batched(leap_ctx* ctx, const leap_work_item* items, int32_t nitems, const double* dd,
+                               int32_t ndirections, int32_t precision, double* cal_out);
+
+/* Enable (default) or disable tuning of new batched shapes on first use. */
+int32_t leap_set_autotune(leap_ctx* ctx, int32_t enable);
+
 /* Copy the avgData of `direction` from the last calibrate call to host memory
  * (pols x nbl complex doubles): MetaData::GetAvgData after RotateVisibilities
  * (LA/model/cpu/MetaData.h:127; DeviceMetaData::ToHost). */
