@@ -16,6 +16,7 @@
 #include "host_math.h"
 #include "kernels_rotate.cuh"
 #include "kernels_solve.cuh"
+#include "kernels_tc.cuh"
 
 using namespace leapgb;
 
@@ -78,7 +79,8 @@ struct Metadata {
   bool set = false;
   leap_constants k{};
   int32_t S = 0, Arows = 0, A1rows = 0, Kpad = 0;
-  DeviceBuffer I1, Ad1, Ad, Ad_f32, arow, arow_val;
+  int32_t tc_mtiles = 0, tc_kblocks = 0;
+  DeviceBuffer I1, Ad1, Ad, Ad_f32, arow, arow_val, Ad_tc;
 };
 
 }  // namespace
@@ -96,6 +98,9 @@ struct leap_ctx {
   TuneChoice tune;
   bool capturing = false;             // recording a CUDA graph: skip host-side uploads and timing events
   bool autotune = true;               // tune new batched shapes on first use
+  bool tc_gemm = true;                // mixed form: Ad contraction on the tensor cores (3xTF32)
+  int tc_attr_set = 0;                // bit per N tile whose shared-memory size was raised
+  DeviceBuffer dphi_tc;               // packed dphi operand of the tensor-core contraction
   std::map<std::string, TuneChoice> tuned;
   std::string graph_key;
   cudaGraphExec_t graph_exec = nullptr;
@@ -531,6 +536,50 @@ int refant_stage(leap_ctx* ctx, const std::vector<WorkItem>& items, const double
   return LEAP_OK;
 }
 
+template <int N>
+int launch_tc_gemm(leap_ctx* ctx, int D, int ntiles, int nkc, int kb_per_cta, cudaStream_t s, int bit) {
+  Metadata& md = ctx->md;
+  if (!(ctx->tc_attr_set & bit)) {
+    LEAP_CUDA(cudaFuncSetAttribute(tc_gemm_ad<N>, cudaFuncAttributeMaxDynamicSharedMemorySize, tc_gemm_smem_bytes<N>()),
+              "set shared memory size");
+    ctx->tc_attr_set |= bit;
+  }
+  const dim3 grid(md.tc_mtiles, ntiles, nkc);
+  tc_gemm_ad<N><<<grid, 128, tc_gemm_smem_bytes<N>(), s>>>(md.Ad_tc.as<float>(), ctx->dphi_tc.as<float>(), md.S, D,
+                                                             md.tc_kblocks, kb_per_cta, ctx->gemm_partial.as<double>(),
+                                                             ctx->dev_err.as<int>());
+  return LEAP_OK;
+}
+
+// cal = Ad * dphi + cal1 for all directions on the tensor cores (3xTF32, FP32
+// accumulate in TMEM), split over K across CTAs and finished in FP64.
+int tc_contraction(leap_ctx* ctx, int32_t D, double* d_cal, cudaStream_t s, int& kernels) {
+  Metadata& md = ctx->md;
+  const int N = D <= 32 ? 32 : (D <= 64 ? 64 : (D <= 128 ? 128 : 256));
+  const int ntiles = (D + N - 1) / N;
+  const int tiles = md.tc_mtiles * ntiles;
+  const int nkc_want = std::max(1, std::min(md.tc_kblocks, (ctx->sms + tiles - 1) / tiles));
+  const int kb_per_cta = (md.tc_kblocks + nkc_want - 1) / nkc_want;
+  const int nkc = (md.tc_kblocks + kb_per_cta - 1) / kb_per_cta;
+  const size_t bbytes = static_cast<size_t>(ntiles) * md.tc_kblocks * 2 * tc_block_bytes(N);
+  LEAP_CUDA(ctx->dphi_tc.ensure(bbytes), "alloc packed dphi");
+  LEAP_CUDA(ctx->gemm_partial.ensure(sizeof(double) * static_cast<size_t>(nkc) * D * md.S), "alloc gemm partial");
+  tc_pack_operand<float><<<grid_1d(static_cast<int64_t>(ntiles) * N * md.tc_kblocks * kTcKB, 256), 256, 0, s>>>(
+      static_cast<const float*>(ctx->dphi.ptr), D, md.Kpad, md.Kpad, N, ntiles, md.tc_kblocks, ctx->dphi_tc.as<float>());
+  int rc;
+  switch (N) {
+    case 32: rc = launch_tc_gemm<32>(ctx, D, ntiles, nkc, kb_per_cta, s, 1); break;
+    case 64: rc = launch_tc_gemm<64>(ctx, D, ntiles, nkc, kb_per_cta, s, 2); break;
+    case 128: rc = launch_tc_gemm<128>(ctx, D, ntiles, nkc, kb_per_cta, s, 4); break;
+    default: rc = launch_tc_gemm<256>(ctx, D, ntiles, nkc, kb_per_cta, s, 8); break;
+  }
+  if (rc != LEAP_OK) return rc;
+  gemm_ad_finish<<<(D * md.S + 255) / 256, 256, 0, s>>>(ctx->gemm_partial.as<double>(), nkc, D, md.S,
+                                                        ctx->cal1.as<double>(), d_cal);
+  kernels += 5;  // solve_dint, pack, gemm, finish (+ solve_cal1 counted by the caller)
+  return LEAP_OK;
+}
+
 // Phase angles + both contractions for all D directions: avg -> cal.
 int solve_stage(leap_ctx* ctx, int32_t D, int32_t precision, int P, bool refant, double* d_cal, cudaStream_t s,
                 int& kernels) {
@@ -562,10 +611,13 @@ int solve_stage(leap_ctx* ctx, int32_t D, int32_t precision, int P, bool refant,
     solve_dint_fp64<<<gd, 256, 0, s>>>(sa);
     gemm_ad_partial<double><<<gg, 256, 0, s>>>(md.Ad.as<double>(), md.S, md.Arows, static_cast<double*>(sa.dphi), md.Kpad,
                                                 D, kchunk, ctx->gemm_partial.as<double>());
-  } else {
+  } else if (!ctx->tc_gemm) {
     solve_dint_mixed<<<gd, 256, 0, s>>>(sa);
     gemm_ad_partial<float><<<gg, 256, 0, s>>>(md.Ad_f32.as<float>(), md.S, md.Arows, static_cast<float*>(sa.dphi),
                                                md.Kpad, D, kchunk, ctx->gemm_partial.as<double>());
+  } else {
+    solve_dint_mixed<<<gd, 256, 0, s>>>(sa);
+    return tc_contraction(ctx, D, d_cal, s, kernels);
   }
   gemm_ad_finish<<<(D * md.S + 255) / 256, 256, 0, s>>>(ctx->gemm_partial.as<double>(), nk, D, md.S,
                                                         ctx->cal1.as<double>(), d_cal);
@@ -640,8 +692,8 @@ int calibrate_impl(leap_ctx* ctx, int32_t slot, const double* d_dd, int32_t ndir
   return calibrate_items(ctx, {WorkItem{slot, 0, ndir}}, d_dd, ndir, precision, d_cal, s);
 }
 
-std::string batch_key(const std::vector<WorkItem>& items, int32_t D, int32_t precision) {
-  std::string k = std::to_string(D) + ":" + std::to_string(precision);
+std::string batch_key(const leap_ctx* ctx, const std::vector<WorkItem>& items, int32_t D, int32_t precision) {
+  std::string k = std::to_string(D) + ":" + std::to_string(precision) + (ctx->tc_gemm ? ":tc" : ":cc");
   for (const auto& w : items) k += "|" + std::to_string(w.slot) + "," + std::to_string(w.dir0) + "," + std::to_string(w.ndir);
   return k;
 }
@@ -690,7 +742,7 @@ int calibrate_batched_impl(leap_ctx* ctx, const leap_work_item* witems, int32_t 
   if (!witems || nitems <= 0) return fail(ctx, LEAP_ERR_INVALID_ARGUMENT, "no work items");
   std::vector<WorkItem> items(nitems);
   for (int i = 0; i < nitems; ++i) items[i] = WorkItem{witems[i].slot, witems[i].first_direction, witems[i].ndirections};
-  const std::string key = batch_key(items, D, precision);
+  const std::string key = batch_key(ctx, items, D, precision);
   cudaStream_t s = ctx->stream;
   if (ctx->graph_exec && ctx->graph_key == key && ctx->graph_epoch == g_alloc_epoch) {
     cudaEvent_t* ev = ctx->ring[ctx->ring_count % leap_ctx::kRing];
@@ -832,6 +884,8 @@ void leap_destroy(leap_ctx* ctx) {
     }
     Metadata& md = ctx->md;
     md.I1.release(); md.Ad1.release(); md.Ad.release(); md.Ad_f32.release(); md.arow.release(); md.arow_val.release();
+    md.Ad_tc.release();
+    ctx->dphi_tc.release();
     ctx->partial.release(); ctx->avg.release(); ctx->cal1.release(); ctx->dphi.release();
     ctx->gemm_partial.release(); ctx->dd.release(); ctx->cal.release(); ctx->dev_err.release(); ctx->lambda.release();
     ctx->dirk.release();
@@ -913,6 +967,14 @@ int32_t leap_set_metadata(leap_ctx* ctx, const leap_constants* k, const double* 
   LEAP_CUDA(cudaMemcpy(md.Ad_f32.ptr, adf.data(), sizeof(float) * adf.size(), cudaMemcpyHostToDevice), "upload Ad f32");
   LEAP_CUDA(cudaMemcpy(md.arow.ptr, arow.data(), sizeof(int4) * A_rows, cudaMemcpyHostToDevice), "upload A rows");
   LEAP_CUDA(cudaMemcpy(md.arow_val.ptr, aval.data(), sizeof(double2) * A_rows, cudaMemcpyHostToDevice), "upload A vals");
+  // Ad split into TF32 hi/lo and packed once for the tensor-core contraction.
+  md.tc_mtiles = (A_cols + kTcM - 1) / kTcM;
+  md.tc_kblocks = md.Kpad / kTcKB;
+  LEAP_CUDA(md.Ad_tc.ensure(static_cast<size_t>(md.tc_mtiles) * md.tc_kblocks * 2 * kTcBlockBytesA), "alloc packed Ad");
+  tc_pack_ad<<<grid_1d(static_cast<int64_t>(md.tc_mtiles) * kTcM * md.tc_kblocks * kTcKB, 256), 256, 0, ctx->stream>>>(
+      md.Ad.as<double>(), A_cols, A_rows, md.tc_mtiles, md.tc_kblocks, md.Ad_tc.as<float>());
+  LEAP_CUDA(cudaGetLastError(), "pack Ad");
+  LEAP_CUDA(cudaStreamSynchronize(ctx->stream), "pack Ad");
   md.set = true;
   return LEAP_OK;
 }
@@ -1027,6 +1089,15 @@ int32_t leap_calibrate_batched(leap_ctx* ctx, const leap_work_item* items, int32
             "download cal");
   LEAP_CUDA(cudaStreamSynchronize(ctx->stream), "calibrate batched");
   return check_device_error(ctx);
+}
+
+int32_t leap_set_option(leap_ctx* ctx, int32_t option, int32_t value) {
+  if (!ctx) return fail(ctx, LEAP_ERR_INVALID_ARGUMENT, "NULL context");
+  switch (option) {
+    case LEAP_OPTION_AUTOTUNE: ctx->autotune = value != 0; return LEAP_OK;
+    case LEAP_OPTION_TENSOR_CORE_CONTRACTION: ctx->tc_gemm = value != 0; return LEAP_OK;
+    default: return fail(ctx, LEAP_ERR_INVALID_ARGUMENT, "unknown option");
+  }
 }
 
 int32_t leap_set_autotune(leap_ctx* ctx, int32_t enable) {

@@ -27,6 +27,8 @@ LEAP_PRECISION_MIXED = 1
 LEAP_MEMORY_HOST = 0
 LEAP_MEMORY_DEVICE = 1
 LEAP_NOALLOC_SCRATCH_BYTES = 16 * 1024 * 1024
+LEAP_OPTION_AUTOTUNE = 1
+LEAP_OPTION_TENSOR_CORE_CONTRACTION = 2
 
 # Every entry point include/leap_gb300.h declares, with its ctypes signature.
 i32, i64, f64, vp = ctypes.c_int32, ctypes.c_int64, ctypes.c_double, ctypes.c_void_p
@@ -61,6 +63,7 @@ SIGNATURES = {
     "leap_calibrate_async": ([vp, i32, vp, i32, i32, vp, vp], i32),
     "leap_calibrate_batched": ([vp, vp, i32, vp, i32, i32, vp], i32),
     "leap_set_autotune": ([vp, i32], i32),
+    "leap_set_option": ([vp, i32, i32], i32),
     "leap_get_avgdata": ([vp, i32, vp], i32),
     "leap_rotate_uvw": ([vp, i32, vp, i32, vp], i32),
     "leap_get_timings": ([vp, ctypes.POINTER(LeapTimings)], i32),

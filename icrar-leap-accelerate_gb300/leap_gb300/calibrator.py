@@ -245,6 +245,9 @@ class Context:
     def set_autotune(self, enable: bool):
         self._check(lib.leap_set_autotune(self._h, int(bool(enable))))
 
+    def set_option(self, option: int, value: int):
+        self._check(lib.leap_set_option(self._h, int(option), int(value)))
+
     def calibrate_async(self, slot: int, dd_ptr: int, ndir: int, precision: int, cal_ptr: int, stream: int = 0):
         self._check(lib.leap_calibrate_async(self._h, slot, dd_ptr, ndir, precision, cal_ptr, stream or None))
 

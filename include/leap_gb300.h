@@ -149,6 +149,12 @@ int32_t leap_calibrate_batched(leap_ctx* ctx, const leap_work_item* items, int32
 /* Enable (default) or disable tuning of new batched shapes on first use. */
 int32_t leap_set_autotune(leap_ctx* ctx, int32_t enable);
 
+/* Context options (value 0 = off, 1 = on). */
+#define LEAP_OPTION_AUTOTUNE 1                   /* as leap_set_autotune (default on) */
+#define LEAP_OPTION_TENSOR_CORE_CONTRACTION 2    /* mixed form: Ad contraction as 3xTF32 tcgen05 MMAs (default on);
+                                                    off: FP32 CUDA-core GEMM */
+int32_t leap_set_option(leap_ctx* ctx, int32_t option, int32_t value);
+
 /* Copy the avgData of `direction` from the last calibrate call to host memory
  * (pols x nbl complex doubles): MetaData::GetAvgData after RotateVisibilities
  * (LA/model/cpu/MetaData.h:127; DeviceMetaData::ToHost). */
