@@ -50,7 +50,8 @@ def _peaks():
 
 
 class ClockSampler:
-    """nvidia-smi clocks and throttle reasons sampled during the timed region."""
+    """nvidia-smi clocks and throttle reasons sampled every 200 ms during the timed region
+    (one `nvidia-smi -lms 200` process for the whole region)."""
     Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
          "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
          "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
@@ -58,29 +59,32 @@ class ClockSampler:
     def __init__(self, device: int):
         self.device = device
         self.samples = []
-        self._stop = threading.Event()
-        self._t = None
-
-    def _run(self):
-        while not self._stop.is_set():
-            try:
-                out = subprocess.run(["nvidia-smi", "-i", str(self.device), f"--query-gpu={self.Q}",
-                                      "--format=csv,noheader,nounits"], capture_output=True, text=True, timeout=5)
-                if out.returncode == 0 and out.stdout.strip():
-                    self.samples.append([x.strip() for x in out.stdout.strip().split(",")])
-            except Exception:
-                pass
-            self._stop.wait(0.2)
+        self._p = None
 
     def __enter__(self):
-        self._t = threading.Thread(target=self._run, daemon=True)
-        self._t.start()
+        try:
+            self._p = subprocess.Popen(["nvidia-smi", "-i", str(self.device), f"--query-gpu={self.Q}",
+                                        "--format=csv,noheader,nounits", "-lms", "200"],
+                                       stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            time.sleep(0.3)  # first sample before the timed region starts
+        except Exception:
+            self._p = None
         return self
 
     def __exit__(self, *a):
-        self._stop.set()
-        if self._t:
-            self._t.join(timeout=6)
+        if self._p is None:
+            return
+        time.sleep(0.25)
+        self._p.terminate()
+        try:
+            out, _ = self._p.communicate(timeout=5)
+        except Exception:
+            self._p.kill()
+            out, _ = self._p.communicate()
+        for line in (out or "").splitlines():
+            f = [x.strip() for x in line.split(",")]
+            if len(f) >= 9:
+                self.samples.append(f)
 
     def summary(self):
         if not self.samples:
@@ -107,16 +111,16 @@ def vis_dirs(obs, ndir: int) -> float:
     return float(obs.pols) * obs.rows * obs.channels * ndir
 
 
-def bench_cpu(obs, dirs, md_host, threads: int, budget_s: float):
-    """Oracle port on a bounded sample: the first timesteps and directions of the workload."""
+def bench_cpu(obs, dirs, vis_t0, threads: int, budget_s: float):
+    """Oracle port on a bounded sample: the first timestep (vis_t0: (channels, nbl, pols))
+    and the first directions of the workload, grown towards `budget_s` seconds."""
     sys.path.insert(0, os.path.join(ROOT, "oracle"))
     import oracle
     mdo = oracle.metadata(obs)
     nbl = obs.nbaselines
-    t_s = 1
+    vis = np.ascontiguousarray(vis_t0)
+    uvw = obs.uvw[:nbl]
     d_s = max(1, min(len(dirs), threads))
-    vis = np.ascontiguousarray(obs.vis[:, : t_s * nbl, :])
-    uvw = obs.uvw[: t_s * nbl]
     dds = np.stack([oracle.dd_matrix(*obs.phase_centre, r, d) for r, d in dirs[:d_s]])
     t0 = time.perf_counter()
     oracle.calibrate_interval(vis, uvw, dds, mdo, nthreads=threads)
@@ -131,7 +135,7 @@ def bench_cpu(obs, dirs, md_host, threads: int, budget_s: float):
         dt = time.perf_counter() - t0
         d_s = d_s2
     units = float(obs.pols) * vis.shape[1] * obs.channels * d_s
-    return units / dt, {"timesteps": t_s, "directions": d_s, "seconds": dt}
+    return units / dt, {"timesteps": 1, "directions": d_s, "seconds": dt}
 
 
 def run_reference(args, rank: int, world: int):
@@ -169,6 +173,182 @@ def run_reference(args, rank: int, world: int):
     print(json.dumps(line), flush=True)
 
 
+def wrapped_max_diff(a, b) -> float:
+    return float(np.abs(np.angle(np.exp(1j * (np.asarray(a) - np.asarray(b))))).max())
+
+
+class Workload:
+    """One benchmark workload resident on the device: `step(precision)` launches one
+    pass of the hot path; `e2e_step()` runs the same through the C ABI with host buffers."""
+    name = ""
+    config: dict = {}
+    units = 0.0           # vis-directions per step
+    b_alg = 0.0           # algorithmic HBM bytes per step (vis once per direction)
+    f_alg = 0.0           # FP32 FMA-pipe issue slots per step (compute roof)
+    traffic = None        # measured DRAM bytes per launch of the bulk kernel, if known
+    h2d = 0
+    d2h = 0
+    kernel_timing = "rotate"  # which leap_timings field times the bulk pass
+    checks: dict = {}
+
+
+def alg_bytes(samples: float, rows: float, ndir: int, nbl: int, pols: int, vis_bytes: int) -> float:
+    """Bytes of the bulk pass on the per-direction convention: every direction reads the
+    visibilities (vis_bytes each) and 24 B of UVW per row, and writes its FP64 avgData."""
+    return ndir * (samples * vis_bytes + rows * 24) + ndir * nbl * pols * 16
+
+
+def fma_slots(rows: float, channels_x_rows: float, ndir: int, pols: int) -> float:
+    return ndir * channels_x_rows * (pols * 4 + 5)
+
+
+def setup_single(args, ctx, lg, torch, local, rank, kind: str):
+    """One integration, all directions in one leap_calibrate_async call (MWA or SKA-Low)."""
+    from leap_gb300 import synth
+    dev = f"cuda:{local}"
+    w = Workload()
+    if kind == "mwa":
+        obs, dirs = make_workload(args, rank)
+        vis_host = torch.from_numpy(obs.vis).pin_memory()
+        vis_dev = vis_host.to(dev)
+        w.cpu_case = (obs, dirs, obs.vis[:, :obs.nbaselines, :])
+        w.name = (f"mwa_precision {obs.num_stations}ant/{obs.nbaselines}bl/{obs.timesteps}t/{obs.channels}ch/"
+                  f"{obs.pols}pol/{len(dirs)}dir c64")
+    else:
+        obs, dirs = synth.ska_low(with_vis=False, directions=args.directions or 128)
+        if rank:
+            _, lm = synth.random_directions(len(dirs), seed=3 + 1000 * rank)
+            dirs = synth.lm_to_radec(lm[:, 0], lm[:, 1])
+        vis_dev = synth.device_visibilities(obs, dev, seed=2)
+        w.cpu_case = (obs, dirs, vis_dev[:, :obs.nbaselines, :].cpu().numpy())
+        vis_host = None
+        if args.e2e:
+            vis_host = torch.empty(vis_dev.shape, dtype=vis_dev.dtype, pin_memory=True)
+            vis_host.copy_(vis_dev)
+        w.name = (f"ska_low {obs.num_stations}st/{obs.nbaselines}bl/{obs.timesteps}t/{obs.channels}ch/"
+                  f"{obs.pols}pol/{len(dirs)}dir c64 (visibilities generated on the device)")
+    t0 = time.perf_counter()
+    md = lg.build_metadata(obs)
+    w.metadata_s = time.perf_counter() - t0
+    ctx.set_metadata(md)
+    uvw_host = torch.from_numpy(obs.uvw).pin_memory()
+    ctx.set_integration(0, vis_dev, uvw_host.to(dev))
+    del vis_dev
+    torch.cuda.empty_cache()
+    dds = np.stack([lg.dd_matrix(md.phase_centre_ra_rad, md.phase_centre_dec_rad, r, d) for r, d in dirs])
+    D, S = len(dirs), md.A.shape[1]
+    dd_dev = torch.from_numpy(dds.reshape(-1)).to(dev)
+    cal_dev = torch.empty((D, S), dtype=torch.float64, device=dev)
+    stream = torch.cuda.current_stream().cuda_stream
+
+    def step(p):
+        ctx.calibrate_async(0, dd_dev.data_ptr(), D, p, cal_dev.data_ptr(), stream)
+
+    w.step = step
+    w.result = lambda: cal_dev.cpu().numpy().copy()
+    w.obs, w.dirs, w.md, w.D, w.S = obs, dirs, md, D, S
+    w.units = vis_dirs(obs, D)
+    w.b_alg = alg_bytes(obs.pols * obs.rows * obs.channels, obs.rows, D, obs.nbaselines, obs.pols, 8)
+    w.f_alg = fma_slots(obs.rows, obs.rows * obs.channels, D, obs.pols)
+    # DRAM traffic of one launch of the bulk kernel, from an ncu capture
+    # (dram__bytes_read.sum + dram__bytes_write.sum) of the 2-timestep case of the
+    # MWA workload: 101.7 MB read per timestep (the visibilities, once) + 44.7 MB
+    # of partial-sum writes, scaled to the timesteps of this run.
+    if kind == "mwa" and obs.nbaselines == 8256 and obs.channels == 384 and D == 64:
+        w.traffic = 101.74e6 * obs.timesteps + 44.74e6
+    w.config = {"workload": w.name, "precision": args.precision,
+                "l2": f"inputs ({obs.vis.nbytes / 1e9 if obs.vis is not None else obs.rows * obs.channels * 32 / 1e9:.2f} GB)"
+                      " larger than L2; no flush"}
+    if vis_host is not None:
+        vis_np = vis_host.numpy()
+        uvw_np = uvw_host.numpy()
+        cal_host = np.zeros((D, S), dtype=np.float64)
+        C, rows, P = vis_np.shape
+        prec = lg.LEAP_PRECISION_MIXED if args.precision == "mixed" else lg.LEAP_PRECISION_FP64
+        from leap_gb300 import _abi
+
+        def e2e_step():
+            ctx._check(_abi.lib.leap_set_integration(ctx.handle, 0, _abi.LEAP_VIS_C64, vis_np.ctypes.data,
+                                                     uvw_np.ctypes.data, rows, C, P, _abi.LEAP_MEMORY_HOST))
+            ctx._check(_abi.lib.leap_calibrate(ctx.handle, 0, dds.ctypes.data, D, prec, cal_host.ctypes.data))
+
+        w.e2e_step = e2e_step
+        w.h2d = vis_np.nbytes + uvw_np.nbytes + dds.nbytes
+        w.d2h = cal_host.nbytes
+    else:
+        w.e2e_step = None
+    return w
+
+
+def setup_batched(args, ctx, lg, torch, local, rank):
+    """32 uneven integration chunks, 256 directions, one leap_calibrate_batched call per step."""
+    from leap_gb300 import synth
+    dev = f"cuda:{local}"
+    w = Workload()
+    nd = args.directions or 256
+    obs_list, dirs, items, order = synth.batched_uneven(chunks=args.chunks, directions=nd)
+    t0 = time.perf_counter()
+    md = lg.build_metadata(obs_list[0])
+    w.metadata_s = time.perf_counter() - t0
+    ctx.set_metadata(md)
+    spot = None
+    hosts = []
+    small = min(range(len(obs_list)), key=lambda i: obs_list[i].rows * obs_list[i].channels)
+    for i, obs in enumerate(obs_list):
+        vis = synth.device_visibilities(obs, dev, seed=2000 + i)
+        ctx.set_integration(i, vis, torch.from_numpy(obs.uvw).to(dev))
+        if args.e2e:
+            vh = torch.empty(vis.shape, dtype=vis.dtype, pin_memory=True)
+            vh.copy_(vis)
+            hosts.append((vh, torch.from_numpy(obs.uvw).pin_memory()))
+        if i == small:
+            spot = vis.cpu().numpy()
+        del vis
+    torch.cuda.empty_cache()
+    dds = np.stack([lg.dd_matrix(md.phase_centre_ra_rad, md.phase_centre_dec_rad, r, d) for r, d in dirs])
+    D, S = len(dirs), md.A.shape[1]
+    holder = {}
+
+    def step(p):
+        holder["cal"] = ctx.calibrate_batched(items, dds, p)
+
+    w.step = step
+    w.result = lambda: holder["cal"].copy()
+    w.kernel_timing = "total"
+    w.obs, w.dirs, w.md, w.D, w.S, w.items, w.dds = obs_list[0], dirs, md, D, S, items, dds
+    w.units = sum(float(obs_list[sl].pols) * obs_list[sl].rows * obs_list[sl].channels * n for sl, _, n in items)
+    w.b_alg = sum(alg_bytes(4.0 * obs_list[sl].rows * obs_list[sl].channels, obs_list[sl].rows, n,
+                            obs_list[sl].nbaselines, 4, 8) for sl, _, n in items)
+    w.f_alg = sum(fma_slots(obs_list[sl].rows, obs_list[sl].rows * obs_list[sl].channels, n, 4) for sl, _, n in items)
+    samples = sum(4.0 * o.rows * o.channels for o in obs_list)
+    w.vis_bytes_resident = samples * 8
+    w.name = (f"batched_uneven 128ant/8256bl, {len(obs_list)} chunks (T 1-64, C in 48/96/384; "
+              f"{int(sum(o.timesteps for o in obs_list))} timesteps), {D} directions round-robin, 4pol c64 "
+              f"({samples * 8 / 1e9:.1f} GB, generated on the device)")
+    w.config = {"workload": w.name, "precision": args.precision, "chunks": [[o.timesteps, o.channels] for o in obs_list],
+                "l2": "inputs larger than L2; no flush"}
+    w.spot = (small, obs_list[small], spot)
+    sl, d0, nd = next(it for it in items if it[0] == small)
+    w.cpu_case = (obs_list[small], dirs, spot[:, :obs_list[small].nbaselines, :])
+    if args.e2e:
+        prec = lg.LEAP_PRECISION_MIXED if args.precision == "mixed" else lg.LEAP_PRECISION_FP64
+        from leap_gb300 import _abi
+
+        def e2e_step():
+            for i, (vh, uh) in enumerate(hosts):
+                C, rows, P = vh.shape
+                ctx._check(_abi.lib.leap_set_integration(ctx.handle, i, _abi.LEAP_VIS_C64, vh.data_ptr(),
+                                                         uh.data_ptr(), rows, C, P, _abi.LEAP_MEMORY_HOST))
+            ctx.calibrate_batched(items, dds, prec)
+
+        w.e2e_step = e2e_step
+        w.h2d = sum(vh.numel() * 8 + uh.numel() * 8 for vh, uh in hosts) + dds.nbytes
+        w.d2h = D * S * 8
+    else:
+        w.e2e_step = None
+    return w
+
+
 def run_gpu(args, rank: int, world: int):
     import torch
     import leap_gb300 as lg
@@ -181,47 +361,37 @@ def run_gpu(args, rank: int, world: int):
         import torch.distributed as dist
         dist.init_process_group("nccl")
 
-    obs, dirs = make_workload(args, rank)
-    md = lg.build_metadata(obs)
     ctx = lg.Context(local)
-    ctx.set_metadata(md)
-    dds = np.stack([lg.dd_matrix(md.phase_centre_ra_rad, md.phase_centre_dec_rad, r, d) for r, d in dirs])
-    D, S = len(dirs), md.A.shape[1]
-
-    vis_host = torch.from_numpy(obs.vis).pin_memory()
-    uvw_host = torch.from_numpy(obs.uvw).pin_memory()
-    vis_dev = vis_host.to(f"cuda:{local}")
-    uvw_dev = uvw_host.to(f"cuda:{local}")
-    ctx.set_integration(0, vis_dev, uvw_dev)
-    dd_dev = torch.from_numpy(dds.reshape(-1)).to(f"cuda:{local}")
-    cal_dev = torch.empty((D, S), dtype=torch.float64, device=f"cuda:{local}")
     # A dedicated stream: the calls and the timing events go on the same (non-null) stream.
     bstream = torch.cuda.Stream(device=f"cuda:{local}")
     torch.cuda.set_stream(bstream)
-    stream = bstream.cuda_stream
+    if args.workload == "batched":
+        w = setup_batched(args, ctx, lg, torch, local, rank)
+    else:
+        w = setup_single(args, ctx, lg, torch, local, rank, args.workload)
     prec = lg.LEAP_PRECISION_MIXED if args.precision == "mixed" else lg.LEAP_PRECISION_FP64
-
-    def step(p):
-        ctx.calibrate_async(0, dd_dev.data_ptr(), D, p, cal_dev.data_ptr(), stream)
+    lib = _abi.lib
 
     def timed(p, steps, warmup):
         for _ in range(warmup):
-            step(p)
+            w.step(p)
         torch.cuda.synchronize()
         if dist:
             dist.barrier()
         torch.cuda.synchronize()
         e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-        lib = _abi.lib
         lib.leap_timing_reset(ctx.handle)
         e0.record()
         for _ in range(steps):
-            step(p)
+            w.step(p)
         e1.record()
         torch.cuda.synchronize()
         ms = e0.elapsed_time(e1) / steps
         t = _abi.LeapTimings()
-        lib.leap_get_timings(ctx.handle, t)
+        ctx._check(lib.leap_get_timings(ctx.handle, t))
+        if w.kernel_timing == "total":
+            # blocking host calls: the device time of each call, from its own events
+            ms = t.total_ms / max(1, t.calls)
         if dist:
             tt = torch.tensor([ms], device=f"cuda:{local}")
             dist.all_reduce(tt, op=dist.ReduceOp.MAX)
@@ -232,91 +402,91 @@ def run_gpu(args, rank: int, world: int):
     with ClockSampler(local) as clk:
         ms, tim = timed(prec, args.steps, args.warmup)
     clocks = clk.summary()
-    units = vis_dirs(obs, D)
-    value = units * world / (ms / 1e3)
-    cal_mixed = cal_dev.cpu().numpy().copy()
+    value = w.units * world / (ms / 1e3)
+    cal_main = w.result()
+    gpu_launches = int(tim.kernels) * args.steps
 
-    # plain FP64 on the same workload
+    checks = {}
     plain = None
     if not args.skip_plain and prec == lg.LEAP_PRECISION_MIXED:
         ms64, _ = timed(lg.LEAP_PRECISION_FP64, max(1, min(args.steps, 3)), 1)
-        cal64 = cal_dev.cpu().numpy().copy()
-        err = float(np.abs(np.angle(np.exp(1j * (cal_mixed - cal64)))).max())
-        plain = {"value": units * world / (ms64 / 1e3), "ms_per_step": ms64, "dtype": "f64",
-                 "mixed_vs_fp64_max_cal_err_rad": err}
+        cal64 = w.result()
+        plain = {"value": w.units * world / (ms64 / 1e3), "ms_per_step": ms64, "dtype": "f64",
+                 "mixed_vs_fp64_max_cal_err_rad": wrapped_max_diff(cal_main, cal64),
+                 "speedup_mixed_over_fp64": ms64 / ms}
 
-    # e2e through the C ABI with host buffers
-    cal_host = np.zeros((D, S), dtype=np.float64)
-    vis_np = vis_host.numpy()
-    uvw_np = uvw_host.numpy()
-    C, rows, P = obs.vis.shape
+    if rank == 0 and getattr(w, "spot", None) is not None and not args.skip_cpu:
+        # Full-size spot check: the smallest chunk's directions against the oracle.
+        sys.path.insert(0, os.path.join(ROOT, "oracle"))
+        import oracle
+        slot, obs_s, vis_s = w.spot
+        sl, d0, nd = next(it for it in w.items if it[0] == slot)
+        exp = oracle.calibrate_interval(vis_s, obs_s.uvw, w.dds[d0:d0 + nd], oracle.metadata(obs_s),
+                                        nthreads=oracle.max_threads())
+        checks["oracle_chunk"] = {"slot": slot, "timesteps": obs_s.timesteps, "channels": obs_s.channels,
+                                  "directions": nd, "max_cal_err_rad": wrapped_max_diff(cal_main[d0:d0 + nd], exp)}
 
-    def e2e_step():
-        ctx._check(_abi.lib.leap_set_integration(ctx.handle, 0, _abi.LEAP_VIS_C64, vis_np.ctypes.data, uvw_np.ctypes.data,
-                                                 rows, C, P, _abi.LEAP_MEMORY_HOST))
-        ctx._check(_abi.lib.leap_calibrate(ctx.handle, 0, dds.ctypes.data, D, prec, cal_host.ctypes.data))
+    e2e = None
+    if w.e2e_step is not None:
+        for _ in range(max(1, min(args.warmup, 2))):
+            w.e2e_step()
+        if dist:
+            dist.barrier()
+        e2e_steps = args.steps if args.workload == "mwa" else max(1, min(args.steps, 3))
+        t0 = time.perf_counter()
+        for _ in range(e2e_steps):
+            w.e2e_step()
+        e2e_s = (time.perf_counter() - t0) / e2e_steps
+        if dist:
+            tt = torch.tensor([e2e_s], device=f"cuda:{local}")
+            dist.all_reduce(tt, op=dist.ReduceOp.MAX)
+            e2e_s = float(tt.item())
+        e2e = {"value": w.units * world / e2e_s, "unit": "vis-directions/s", "h2d_bytes_per_step": int(w.h2d),
+               "d2h_bytes_per_step": int(w.d2h), "ms_per_step": e2e_s * 1e3, "steps": e2e_steps}
 
-    for _ in range(max(1, args.warmup)):
-        e2e_step()
-    if dist:
-        dist.barrier()
-    t0 = time.perf_counter()
-    for _ in range(args.steps):
-        e2e_step()
-    e2e_s = (time.perf_counter() - t0) / args.steps
-    if dist:
-        tt = torch.tensor([e2e_s], device=f"cuda:{local}")
-        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
-        e2e_s = float(tt.item())
-    h2d = obs.vis.nbytes + obs.uvw.nbytes + dds.nbytes
-    d2h = cal_host.nbytes
-
-    # roofline of the rotate+average kernel (SURVEY convention: s_vis bytes per vis-direction
-    # + 24 B of UVW per row and direction + the FP64 avgData write)
     peaks = _peaks()
     peak = peaks["hbm_gbs"] if peaks else 6800.0
-    rot_ms = tim.rotate_ms / max(1, tim.calls)
-    vis_bytes = obs.vis.itemsize
-    b_alg = D * (units / D * vis_bytes + obs.rows * 24) + D * obs.nbaselines * P * 16
-    achieved = b_alg / (rot_ms / 1e3) / 1e9
-    fp32_ops = D * obs.rows * obs.channels * (P * 4 + 5)  # FMA-pipe issue slots per (row, channel, direction)
-    # DRAM traffic of one launch of the bulk kernel, from an ncu capture
-    # (dram__bytes_read.sum + dram__bytes_write.sum) of the 2-timestep case of this
-    # workload: 101.7 MB read per timestep (the visibilities, once) + 44.7 MB of
-    # partial-sum writes, scaled to the timesteps of this run.
-    traffic = (101.74e6 * obs.timesteps + 44.74e6) if (obs.nbaselines == 8256 and obs.channels == 384 and D == 64) else None
+    if w.kernel_timing == "rotate":
+        k_ms = tim.rotate_ms / max(1, tim.calls)
+        k_name = "rotate_average (mixed: persistent TMA-pipelined kernel + compensated reference-antenna pass)"
+    else:
+        k_ms = ms
+        k_name = "whole batched call (graph replay)"
+    achieved = w.b_alg / (k_ms / 1e3) / 1e9
     roof = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
-            "traffic": traffic, "kernel": "rotate_average", "kernel_ms": rot_ms,
-            "peak_source": "MEASURED_PEAKS.json hbm_gbs" if peaks else "fallback 6.8 TB/s",
-            "note": "B_alg counts the vis once per direction; the kernel reads it once for all directions",
-            "compute": {"fp32_issue_per_s": fp32_ops / (rot_ms / 1e3), "fp32_peak_fma_per_s": 3.6e13,
-                        "frac": fp32_ops / (rot_ms / 1e3) / 3.6e13}}
+            "traffic": w.traffic, "kernel": k_name, "kernel_ms": k_ms,
+            "peak_source": "MEASURED_PEAKS.json hbm_gbs (of measured)" if peaks else "fallback 6.8 TB/s (of fallback)",
+            "note": "B_alg counts the visibilities once per direction; the kernel reads them once for all directions",
+            "compute": {"fp32_issue_per_s": w.f_alg / (k_ms / 1e3), "fp32_peak_fma_per_s": 3.6e13,
+                        "frac": w.f_alg / (k_ms / 1e3) / 3.6e13}}
+    if hasattr(w, "vis_bytes_resident"):
+        roof["hbm_read_once_frac"] = w.vis_bytes_resident / (k_ms / 1e3) / 1e9 / peak
 
     cpu = None
     if rank == 0 and world == 1 and not args.skip_cpu:
         sys.path.insert(0, os.path.join(ROOT, "oracle"))
         import oracle
         thr = oracle.max_threads()
-        v, samp = bench_cpu(obs, dirs, md, thr, args.cpu_budget)
+        c_obs, c_dirs, c_vis = w.cpu_case
+        v, samp = bench_cpu(c_obs, c_dirs, c_vis, thr, args.cpu_budget)
         cpu = {"value": v, "unit": "vis-directions/s", "cores": thr, "kind": "port",
-               "sample": f"{samp['timesteps']} of {obs.timesteps} timesteps x {samp['directions']} of {D} directions, "
-                         f"{samp['seconds']:.1f} s"}
+               "sample": f"1 timestep ({c_obs.nbaselines} baselines x {c_obs.channels} channels) x "
+                         f"{samp['directions']} of {w.D} directions, {samp['seconds']:.1f} s"}
 
     if rank == 0:
         line = {
             "metric": "vis-directions/s", "value": value, "unit": "vis-directions/s", "n_gpus": world,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True,
-            "scaling": "weak", "vs_baseline": None, "dtype": "f32 rotation + f64 phase arguments" if prec else "f64",
-            "data": "synthetic",
-            "config": {"workload": f"mwa_precision {obs.num_stations}ant/{obs.nbaselines}bl/{obs.timesteps}t/"
-                                   f"{obs.channels}ch/{P}pol/{D}dir c64",
-                       "precision": args.precision, "l2": "inputs (1.42 GB) larger than L2; no flush"},
-            "e2e": {"value": units * world / e2e_s, "unit": "vis-directions/s", "h2d_bytes_per_step": h2d,
-                    "d2h_bytes_per_step": d2h, "ms_per_step": e2e_s * 1e3},
-            "gpu_launches": int(tim.kernels) * args.steps,
+            "scaling": "weak", "vs_baseline": None,
+            "dtype": "f32 rotation + f64 phase arguments" if prec else "f64", "data": "synthetic",
+            "config": w.config,
+            "e2e": e2e,
+            "gpu_launches": gpu_launches,
             "roofline": roof,
             "cpu_baseline": cpu,
             "plain_fp64": plain,
+            "checks": checks or None,
+            "metadata_build_s": round(getattr(w, "metadata_s", 0.0), 2),
             "clocks": clocks,
         }
         print(json.dumps(line), flush=True)
@@ -332,13 +502,22 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--precision", default="mixed", choices=["mixed", "fp64"])
+    ap.add_argument("--workload", default="mwa", choices=["mwa", "batched", "ska_low"],
+                    help="mwa: 128 antennas, 14 t, 384 ch, 64 directions (default); batched: 32 uneven chunks, "
+                         "256 directions; ska_low: 512 stations, 16 t, 384 ch, 128 directions")
     ap.add_argument("--timesteps", type=int, default=14)
     ap.add_argument("--channels", type=int, default=384)
-    ap.add_argument("--directions", type=int, default=64)
+    ap.add_argument("--directions", type=int, default=0, help="0: the workload's own count")
+    ap.add_argument("--chunks", type=int, default=32)
+    ap.add_argument("--e2e", type=int, default=-1, help="1/0: force the host-buffer end-to-end timing on/off")
     ap.add_argument("--cpu-budget", type=float, default=15.0)
     ap.add_argument("--skip-cpu", action="store_true")
     ap.add_argument("--skip-plain", action="store_true")
     args = ap.parse_args()
+    if args.directions == 0 and args.workload == "mwa":
+        args.directions = 64
+    if args.e2e < 0:
+        args.e2e = 1 if args.workload == "mwa" else 0
     rank = int(os.environ.get("RANK", "0"))
     world = int(os.environ.get("WORLD_SIZE", "1"))
     if args.impl == "reference":

@@ -21,6 +21,7 @@ INCLUDE = os.path.join(ROOT, "include")
 OUT_DIR = os.path.join(HERE, "leap_gb300", "_lib")
 OBJ_DIR = os.path.join(HERE, "_build")
 LIB = os.path.join(OUT_DIR, "libleap_gb300.so")
+SYNTH_LIB = os.path.join(OUT_DIR, "libleap_synth.so")
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
@@ -95,6 +96,11 @@ def build(verbose: bool = False, force: bool = False) -> str:
         objs.append(o)
         if force or _newer(o, [s] + headers):
             jobs.append(["g++", "-O2", "-fPIC", "-std=c++17", "-Wall", *inc, "-c", s, "-o", o])
+    synth_src = os.path.join(CSRC, "synth_vis.cu")
+    synth_obj = os.path.join(OBJ_DIR, "synth_vis.cu.o")
+    if force or _newer(synth_obj, [synth_src] + headers):
+        jobs.append([nvcc, *ARCH, "-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", *inc, "-c", synth_src,
+                     "-o", synth_obj])
     with cf.ThreadPoolExecutor(max_workers=min(8, os.cpu_count() or 4)) as ex:
         outs = list(ex.map(_run, jobs))
     if verbose:
@@ -103,6 +109,8 @@ def build(verbose: bool = False, force: bool = False) -> str:
                 print(o)
     if force or jobs or not os.path.exists(LIB):
         _run([nvcc, *ARCH, "-shared", "-o", LIB, *objs, "-lcudart"])
+    if force or _newer(SYNTH_LIB, [synth_obj]):
+        _run([nvcc, *ARCH, "-shared", "-o", SYNTH_LIB, synth_obj, "-lcudart"])
     driver_src = os.path.join(CPP, "tools", "leap_calibrate_driver.cc")
     driver = os.path.join(OUT_DIR, "leap_calibrate_driver")
     if os.path.exists(driver_src) and (force or _newer(driver, [driver_src, LIB] + headers)):

@@ -25,6 +25,8 @@ Seeds: positions 0, gains 1, noise 2, directions 3, chunk shapes 4.
 """
 from __future__ import annotations
 
+import ctypes
+import os
 from dataclasses import dataclass, field
 from typing import List, Optional
 
@@ -245,3 +247,93 @@ def write_leapms(obs: Observation, path: str) -> None:
         np.repeat(obs.epochs, nbl).astype("<f8").tofile(f)
         np.ascontiguousarray(obs.uvw, dtype="<f8").tofile(f)
         np.ascontiguousarray(obs.vis.transpose(1, 0, 2)).tofile(f)
+
+
+# ---------------------------------------------------------------------------
+# Device-side generation (benchmark sizes: tens of GB of visibilities)
+# ---------------------------------------------------------------------------
+
+_SYNTH_LIB = None
+
+
+def _synth_lib():
+    global _SYNTH_LIB
+    if _SYNTH_LIB is None:
+        path = os.path.join(os.path.dirname(os.path.abspath(__file__)), "_lib", "libleap_synth.so")
+        if not os.path.exists(path):
+            raise RuntimeError(f"{path} is not built (run the package build first)")
+        lib = ctypes.CDLL(path)
+        lib.leap_synth_fill_c64.restype = ctypes.c_int32
+        lib.leap_synth_fill_c64.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int64,
+                                            ctypes.c_int32, ctypes.c_int32, ctypes.c_int32, ctypes.c_double,
+                                            ctypes.c_double, ctypes.c_double, ctypes.c_uint64, ctypes.c_void_p]
+        _SYNTH_LIB = lib
+    return _SYNTH_LIB
+
+
+def model_delay_and_gains(obs: Observation):
+    """Per-row delay u l0 + v m0 + w (n0 - 1) (metres) and per-baseline g_a conj(g_b)."""
+    l0, m0, n0 = obs.source_lmn
+    delay = obs.uvw[:, 0] * l0 + obs.uvw[:, 1] * m0 + obs.uvw[:, 2] * (n0 - 1.0)
+    nbl = obs.nbaselines
+    gg = obs.gains[obs.antenna1[:nbl]] * np.conj(obs.gains[obs.antenna2[:nbl]])
+    return np.ascontiguousarray(delay), np.ascontiguousarray(gg.astype(np.complex128))
+
+
+def device_visibilities(obs: Observation, device, seed: int = 2, stream=None):
+    """The observation's complex<float> visibility cube (channels, rows, pols),
+    generated on the GPU by the same model as make_observation (a different
+    noise stream): returns a torch tensor on `device`."""
+    import torch
+    delay, gg = model_delay_and_gains(obs)
+    dev = torch.device(device)
+    d_delay = torch.from_numpy(delay).to(dev)
+    d_gg = torch.from_numpy(gg.view(np.float64)).to(dev)
+    vis = torch.empty((obs.channels, obs.rows, obs.pols), dtype=torch.complex64, device=dev)
+    s = stream if stream is not None else torch.cuda.current_stream(dev).cuda_stream
+    rc = _synth_lib().leap_synth_fill_c64(vis.data_ptr(), d_delay.data_ptr(), d_gg.data_ptr(), obs.rows,
+                                          obs.nbaselines, obs.channels, obs.pols, obs.freq_start_hz,
+                                          obs.freq_inc_hz, float(obs.noise_sigma), int(seed), s)
+    if rc != 0:
+        raise RuntimeError(f"leap_synth_fill_c64 failed with CUDA error {rc}")
+    torch.cuda.synchronize(dev)
+    return vis
+
+
+def ska_low(with_vis: bool = True, timesteps: int = 16, channels: int = 384, directions: int = 128) -> tuple:
+    """512 stations, log-uniform radial layout to 40 km, 16 x 8 s, 384 x 5.4 kHz from
+    100 MHz, complex<float>, sigma 1.0, 128 directions (the source is direction 0)."""
+    obs = make_observation(ArraySpec(512, 40000.0, "loguniform"), timesteps=timesteps, channels=channels,
+                           freq_start_hz=100e6, freq_inc_hz=5.4e3, noise_sigma=1.0, source_lm=(0.01, -0.005),
+                           vis_dtype=np.complex64, with_vis=with_vis)
+    dirs, _ = random_directions(directions)
+    dirs[0] = lm_to_radec(np.array([0.01]), np.array([-0.005]))[0]
+    return obs, dirs
+
+
+def batched_uneven(chunks: int = 32, directions: int = 256, stations: int = 128):
+    """The batched workload: `chunks` consecutive integration chunks of the
+    128-antenna array (timesteps uniform in 1..64, channels from {48, 96, 384},
+    seed 4), 150 MHz / 40 kHz, sigma 0.5, and `directions` directions dealt
+    round-robin to the chunks (direction j -> chunk j mod chunks).
+
+    Returns (observations without visibilities, directions (ra, dec) in item
+    order, work items [(slot, first_direction, ndirections)], original direction
+    index of each item-ordered direction)."""
+    spec = ArraySpec(stations, 1500.0)
+    pos = antenna_positions(spec, 0)
+    gains = np.exp(1j * np.random.default_rng(1).uniform(-np.pi, np.pi, stations))
+    shapes = uneven_chunks(chunks, seed=4)
+    dirs, _ = random_directions(directions)
+    dirs[0] = lm_to_radec(np.array([0.01]), np.array([-0.005]))[0]
+    obs_list, order, items = [], [], []
+    for i, ch in enumerate(shapes):
+        obs_list.append(make_observation(spec, timesteps=ch.timesteps, channels=ch.channels, freq_start_hz=150e6,
+                                         freq_inc_hz=40e3, noise_sigma=0.5, source_lm=(0.01, -0.005),
+                                         vis_dtype=np.complex64, with_vis=False, timestep_offset=ch.timestep_offset,
+                                         positions=pos, gains=gains))
+        mine = [j for j in range(directions) if j % chunks == i]
+        if mine:
+            items.append((i, len(order), len(mine)))
+            order += mine
+    return obs_list, dirs[order], items, np.asarray(order)

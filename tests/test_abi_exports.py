@@ -42,3 +42,12 @@ def test_no_device_gives_clean_error():
         assert e.code == _abi.LEAP_ERR_CUDA
     else:
         raise AssertionError("expected LeapError without a GPU")
+
+
+def test_synth_library_exports_its_header():
+    from leap_gb300 import synth
+    text = re.sub(r"/\*.*?\*/", "", open(os.path.join(ROOT, "include", "leap_synth.h")).read(), flags=re.S)
+    names = sorted(set(re.findall(r"\b(leap_[a-z0-9_]+)\s*\(", text)))
+    assert names == ["leap_synth_fill_c64"]
+    lib = synth._synth_lib()
+    assert all(hasattr(lib, n) for n in names)
