@@ -388,68 +388,6 @@ __device__ __forceinline__ uint64_t frac_turns_u64(double x) {
   return static_cast<uint64_t>(static_cast<long long>(rint(f * 9223372036854775808.0))) << 1;
 }
 
-template <int DPW>
-__global__ void __launch_bounds__(128) refant_average_df(RotateArgs a, const int32_t* __restrict__ I1, int nI1,
-                                                        const float4* __restrict__ df_tab, double2* __restrict__ out) {
-  __shared__ float4 tab[kTwiddleSize];
-  for (int i = threadIdx.x; i < kTwiddleSize; i += blockDim.x) tab[i] = __ldg(df_tab + i);
-  __syncthreads();
-  constexpr int NW = 4;
-  const int lane = threadIdx.x & 31;
-  const int warp = threadIdx.x >> 5;
-  const int k = blockIdx.x * 32 + lane;
-  const int d0 = (blockIdx.y * NW + warp) * DPW;
-  const int slab = blockIdx.z;
-  const int ts = slab / a.n_cslab, cs = slab % a.n_cslab;
-  const int t_lo = ts * a.t_per_slab, t_hi = min(a.timesteps, t_lo + a.t_per_slab);
-  const int c_lo = cs * a.c_per_slab, c_hi = min(a.channels, c_lo + a.c_per_slab);
-  if (d0 >= a.ndir || k >= nI1) return;
-  int b = __ldg(I1 + k);
-  if (b < 0) b += a.nbl;  // VectorRangeSelect wrap-around (LA/math/cpu/vector.h:97-104)
-
-  const double kA = a.f0 / kSpeedOfLight, kB = a.df / kSpeedOfLight;
-  DfAcc re[DPW], im[DPW];
-#pragma unroll
-  for (int j = 0; j < DPW; ++j) re[j] = im[j] = DfAcc{0.f, 0.f};
-  const float2* vis = static_cast<const float2*>(a.vis);
-  for (int t = t_lo; t < t_hi; ++t) {
-    const int64_t r = static_cast<int64_t>(t) * a.nbl + b;
-    const double uu = __ldg(a.uvw + 3 * r), vv = __ldg(a.uvw + 3 * r + 1), ww = __ldg(a.uvw + 3 * r + 2);
-    uint64_t pa[DPW], pb[DPW];
-#pragma unroll
-    for (int j = 0; j < DPW; ++j) {
-      const int d = min(d0 + j, a.ndir - 1);
-      const double wrot = __ldg(a.dd + 9 * d + 6) * uu + __ldg(a.dd + 9 * d + 7) * vv + __ldg(a.dd + 9 * d + 8) * ww;
-      const double dw = wrot - ww;
-      pa[j] = frac_turns_u64(-dw * kA);
-      pb[j] = frac_turns_u64(-dw * kB);
-    }
-    const float2* src = vis + r * a.pols;
-#pragma unroll 4
-    for (int c = c_lo; c < c_hi; ++c) {
-      const float2 v = __ldg(src + static_cast<int64_t>(c) * a.rows * a.pols);
-#pragma unroll
-      for (int j = 0; j < DPW; ++j) {
-        float zrh, zrl, zih, zil;
-        df_twiddle(pa[j] + static_cast<uint64_t>(c) * pb[j], tab, zrh, zrl, zih, zil);
-        df_add_product(re[j], v.x, zrh, zrl);
-        df_add_product(re[j], -v.y, zih, zil);
-        df_add_product(im[j], v.x, zih, zil);
-        df_add_product(im[j], v.y, zrh, zrl);
-      }
-    }
-  }
-  const int64_t slab_off = static_cast<int64_t>(slab) * a.ndir * nI1;
-#pragma unroll
-  for (int j = 0; j < DPW; ++j) {
-    const int d = d0 + j;
-    if (d < a.ndir)
-      out[slab_off + static_cast<int64_t>(d) * nI1 + k] =
-          make_double2(static_cast<double>(re[j].s) + static_cast<double>(re[j].c),
-                       static_cast<double>(im[j].s) + static_cast<double>(im[j].c));
-  }
-}
-
 // UVWs as (hi, lo) float pairs for the double-float phase set-up.
 static __global__ void split_uvw(const double* __restrict__ uvw, int64_t rows, float* __restrict__ out) {
   for (int64_t i = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x; i < 3 * rows;
