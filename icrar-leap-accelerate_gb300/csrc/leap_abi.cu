@@ -17,6 +17,7 @@
 #include "kernels_rotate.cuh"
 #include "kernels_solve.cuh"
 #include "kernels_tc.cuh"
+#include "kernels_adjoint.cuh"
 
 using namespace leapgb;
 
@@ -81,6 +82,7 @@ struct Metadata {
   int32_t S = 0, Arows = 0, A1rows = 0, Kpad = 0;
   int32_t tc_mtiles = 0, tc_kblocks = 0;
   DeviceBuffer I1, Ad1, Ad, Ad_f32, arow, arow_val, Ad_tc;
+  DeviceBuffer at_ptr, at_idx, at_val;  // A^T (rows n < |I|) in compressed-row form, for the adjoint
 };
 
 }  // namespace
@@ -101,6 +103,7 @@ struct leap_ctx {
   bool tc_gemm = true;                // mixed form: Ad contraction on the tensor cores (3xTF32)
   int tc_attr_set = 0;                // bit per N tile whose shared-memory size was raised
   DeviceBuffer dphi_tc;               // packed dphi operand of the tensor-core contraction
+  DeviceBuffer adj_dphi, adj_cal1, adj_phi1, adj_gavg, adj_partial;  // adjoint scratch
   std::map<std::string, TuneChoice> tuned;
   std::string graph_key;
   cudaGraphExec_t graph_exec = nullptr;
@@ -885,6 +888,7 @@ void leap_destroy(leap_ctx* ctx) {
     Metadata& md = ctx->md;
     md.I1.release(); md.Ad1.release(); md.Ad.release(); md.Ad_f32.release(); md.arow.release(); md.arow_val.release();
     md.Ad_tc.release();
+    md.at_ptr.release(); md.at_idx.release(); md.at_val.release();
     ctx->dphi_tc.release();
     ctx->partial.release(); ctx->avg.release(); ctx->cal1.release(); ctx->dphi.release();
     ctx->gemm_partial.release(); ctx->dd.release(); ctx->cal.release(); ctx->dev_err.release(); ctx->lambda.release();
@@ -967,6 +971,33 @@ int32_t leap_set_metadata(leap_ctx* ctx, const leap_constants* k, const double* 
   LEAP_CUDA(cudaMemcpy(md.Ad_f32.ptr, adf.data(), sizeof(float) * adf.size(), cudaMemcpyHostToDevice), "upload Ad f32");
   LEAP_CUDA(cudaMemcpy(md.arow.ptr, arow.data(), sizeof(int4) * A_rows, cudaMemcpyHostToDevice), "upload A rows");
   LEAP_CUDA(cudaMemcpy(md.arow_val.ptr, aval.data(), sizeof(double2) * A_rows, cudaMemcpyHostToDevice), "upload A vals");
+  // A^T over the rows n < |I| (the rows dInt reads), compressed by column, for the adjoint.
+  {
+    const int32_t nI = A_rows - 1;
+    std::vector<int32_t> ptr(A_cols + 1, 0);
+    for (int32_t n = 0; n < nI; ++n) {
+      ++ptr[arow[n].x + 1];
+      if (arow[n].y != arow[n].x) ++ptr[arow[n].y + 1];
+    }
+    for (int32_t c = 0; c < A_cols; ++c) ptr[c + 1] += ptr[c];
+    std::vector<int32_t> idx(std::max(ptr[A_cols], 1));
+    std::vector<double> val(std::max(ptr[A_cols], 1));
+    std::vector<int32_t> fill(ptr.begin(), ptr.end() - 1);
+    for (int32_t n = 0; n < nI; ++n) {
+      idx[fill[arow[n].x]] = n;
+      val[fill[arow[n].x]++] = aval[n].x;
+      if (arow[n].y != arow[n].x) {
+        idx[fill[arow[n].y]] = n;
+        val[fill[arow[n].y]++] = aval[n].y;
+      }
+    }
+    LEAP_CUDA(md.at_ptr.ensure(sizeof(int32_t) * ptr.size()), "alloc A^T");
+    LEAP_CUDA(md.at_idx.ensure(sizeof(int32_t) * idx.size()), "alloc A^T");
+    LEAP_CUDA(md.at_val.ensure(sizeof(double) * val.size()), "alloc A^T");
+    LEAP_CUDA(cudaMemcpy(md.at_ptr.ptr, ptr.data(), sizeof(int32_t) * ptr.size(), cudaMemcpyHostToDevice), "upload A^T");
+    LEAP_CUDA(cudaMemcpy(md.at_idx.ptr, idx.data(), sizeof(int32_t) * idx.size(), cudaMemcpyHostToDevice), "upload A^T");
+    LEAP_CUDA(cudaMemcpy(md.at_val.ptr, val.data(), sizeof(double) * val.size(), cudaMemcpyHostToDevice), "upload A^T");
+  }
   // Ad split into TF32 hi/lo and packed once for the tensor-core contraction.
   md.tc_mtiles = (A_cols + kTcM - 1) / kTcM;
   md.tc_kblocks = md.Kpad / kTcKB;
@@ -1089,6 +1120,92 @@ int32_t leap_calibrate_batched(leap_ctx* ctx, const leap_work_item* items, int32
             "download cal");
   LEAP_CUDA(cudaStreamSynchronize(ctx->stream), "calibrate batched");
   return check_device_error(ctx);
+}
+
+int32_t leap_get_avgdata_device(leap_ctx* ctx, int32_t pol, double* d_out, void* stream) {
+  if (!ctx || !d_out) return fail(ctx, LEAP_ERR_INVALID_ARGUMENT, "NULL argument");
+  if (ctx->last_ndir <= 0) return fail(ctx, LEAP_ERR_NOT_READY, "no calibrate call yet");
+  if (pol < 0 || pol >= ctx->last_pols) return fail(ctx, LEAP_ERR_INVALID_ARGUMENT, "pol out of range");
+  DeviceGuard g(ctx->device);
+  cudaStream_t s = stream ? static_cast<cudaStream_t>(stream) : ctx->stream;
+  const size_t nbl = static_cast<size_t>(ctx->last_nbl);
+  // avg is [ndir][pols][nbl]: one strided 2-D copy gathers pol `pol` of every direction.
+  LEAP_CUDA(cudaMemcpy2DAsync(d_out, sizeof(double2) * nbl, ctx->avg.as<double2>() + pol * nbl,
+                              sizeof(double2) * nbl * ctx->last_pols, sizeof(double2) * nbl, ctx->last_ndir,
+                              cudaMemcpyDeviceToDevice, s),
+            "copy avgData");
+  return LEAP_OK;
+}
+
+int32_t leap_backward(leap_ctx* ctx, int32_t slot, const double* d_dd, int32_t ndir, const double* d_avg0,
+                      const double* d_grad_cal, const void* d_vis, double* d_grad_lmn, void* d_grad_vis,
+                      void* stream) {
+  if (!ctx || !d_dd || !d_avg0 || !d_grad_cal || !d_grad_lmn) return fail(ctx, LEAP_ERR_INVALID_ARGUMENT, "NULL argument");
+  if (ndir <= 0) return fail(ctx, LEAP_ERR_INVALID_ARGUMENT, "ndirections must be positive");
+  if (!ctx->md.set) return fail(ctx, LEAP_ERR_NOT_READY, "metadata not set");
+  auto it = ctx->integ.find(slot);
+  if (it == ctx->integ.end()) return fail(ctx, LEAP_ERR_NOT_READY, "integration slot not set");
+  DeviceGuard g(ctx->device);
+  Metadata& md = ctx->md;
+  const Integration& in = it->second;
+  const int nbl = static_cast<int>(md.k.nbaselines);
+  const int S = md.S, D = ndir, nI = md.Arows - 1, nI1 = md.A1rows - 1;
+  cudaStream_t s = stream ? static_cast<cudaStream_t>(stream) : ctx->stream;
+  LEAP_CUDA(ctx->adj_dphi.ensure(sizeof(double) * std::max(nI, 1) * D), "alloc adjoint scratch");
+  LEAP_CUDA(ctx->adj_cal1.ensure(sizeof(double) * S * D), "alloc adjoint scratch");
+  LEAP_CUDA(ctx->adj_phi1.ensure(sizeof(double) * std::max(nI1, 1) * D), "alloc adjoint scratch");
+  LEAP_CUDA(ctx->adj_gavg.ensure(sizeof(double2) * static_cast<size_t>(nbl) * D), "alloc adjoint scratch");
+  // Solve adjoint: g_dphi, g_cal1, g_phi1, g_avg.
+  if (nI > 0)
+    adjoint_contract_t<<<(nI * 32 + 255) / 256, 256, 0, s>>>(md.Ad.as<double>(), S, nI, d_grad_cal, D,
+                                                             ctx->adj_dphi.as<double>(), nI);
+  else
+    LEAP_CUDA(cudaMemsetAsync(ctx->adj_dphi.ptr, 0, sizeof(double) * D, s), "clear");
+  adjoint_cal1<<<(S * D + 255) / 256, 256, 0, s>>>(d_grad_cal, ctx->adj_dphi.as<double>(), std::max(nI, 1),
+                                                   md.at_ptr.as<int32_t>(), md.at_idx.as<int32_t>(),
+                                                   md.at_val.as<double>(), S, D, ctx->adj_cal1.as<double>());
+  if (nI1 > 0)
+    adjoint_contract_t<<<(nI1 * 32 + 255) / 256, 256, 0, s>>>(md.Ad1.as<double>(), S, nI1, ctx->adj_cal1.as<double>(),
+                                                              D, ctx->adj_phi1.as<double>(), nI1);
+  const double2* avg0 = reinterpret_cast<const double2*>(d_avg0);
+  adjoint_avg_dint<<<grid_1d(static_cast<int64_t>(nbl) * D, 256), 256, 0, s>>>(
+      avg0, ctx->adj_dphi.as<double>(), std::max(nI, 1), nI, nbl, D, ctx->adj_gavg.as<double2>());
+  if (nI1 > 0)
+    adjoint_avg_phi1<<<(D + 127) / 128, 128, 0, s>>>(avg0, ctx->adj_phi1.as<double>(), md.I1.as<int32_t>(), nI1, nbl,
+                                                     D, ctx->adj_gavg.as<double2>());
+  // Rotate + average adjoint over the integration, recomputing the rotated samples.
+  AdjointArgs aa{};
+  aa.vis = d_vis ? d_vis : in.vis.ptr;
+  aa.vis_c64 = in.vis_type == LEAP_VIS_C64;
+  aa.check_nan = d_vis != nullptr;
+  aa.uvw = in.uvw.as<double>();
+  aa.dd = d_dd;
+  aa.gavg = ctx->adj_gavg.as<double2>();
+  aa.rows = in.rows;
+  aa.C = in.channels;
+  aa.P = in.pols;
+  aa.nbl = nbl;
+  aa.D = D;
+  aa.f0 = md.k.freq_start_hz;
+  aa.df = md.k.freq_inc_hz;
+  constexpr int kDPB = 4;
+  const int64_t items = in.rows * ((in.channels + kAdjChannels - 1) / kAdjChannels);
+  const int dgroups = (D + kDPB - 1) / kDPB;
+  const int64_t want = (items + 255) / 256;
+  const int bx = static_cast<int>(std::max<int64_t>(1, std::min<int64_t>(want, std::max(1, ctx->sms * 8 / dgroups))));
+  LEAP_CUDA(ctx->adj_partial.ensure(sizeof(double) * 3 * static_cast<size_t>(bx) * D), "alloc adjoint partials");
+  aa.partial = ctx->adj_partial.as<double>();
+  adjoint_lmn<kDPB><<<dim3(bx, dgroups), 256, 0, s>>>(aa);
+  adjoint_lmn_reduce<<<(3 * D + 127) / 128, 128, 0, s>>>(aa.partial, bx, D, d_grad_lmn);
+  if (d_grad_vis) {
+    const size_t esz = aa.vis_c64 ? sizeof(float2) : sizeof(double2);
+    LEAP_CUDA(cudaMemsetAsync(d_grad_vis, 0, esz * static_cast<size_t>(in.rows) * in.channels * in.pols, s),
+              "clear vis gradient");
+    aa.gvis = d_grad_vis;
+    adjoint_vis<<<grid_1d(items, 256), 256, 0, s>>>(aa);
+  }
+  LEAP_CUDA(cudaGetLastError(), "adjoint launch");
+  return LEAP_OK;
 }
 
 int32_t leap_set_option(leap_ctx* ctx, int32_t option, int32_t value) {

@@ -149,6 +149,17 @@ def _vis_type(dtype) -> int:
     raise InvalidArgument(_abi.LEAP_ERR_INVALID_ARGUMENT, f"unsupported visibility dtype {dtype}")
 
 
+CUDA_STREAM_LEGACY = 1  # cudaStreamLegacy: the legacy default stream as an explicit handle
+
+
+def stream_handle(stream: Optional[int]):
+    """C-ABI stream argument for a cudaStream_t handle: None selects the context's stream
+    (NULL); 0, the legacy default stream (torch's default stream), becomes cudaStreamLegacy."""
+    if stream is None:
+        return None
+    return int(stream) if stream else CUDA_STREAM_LEGACY
+
+
 class Context:
     """One device, one stream, the resident buffers (leap_create ... leap_destroy)."""
 
@@ -159,6 +170,7 @@ class Context:
         self.device = device
         self.md: Optional[MetaData] = None
         self.slots = {}
+        self.autograd_slots = {}  # slot -> (key, vis, uvw) of the differentiable form's last upload
         self._last_slot = None
 
     @property
@@ -204,6 +216,7 @@ class Context:
     def set_integration(self, slot: int, vis, uvw):
         """vis: (channels, rows, pols) complex64/complex128 numpy array or CUDA torch tensor
         (a torch complex tensor or its real view); uvw: (rows, 3) float64."""
+        self.autograd_slots.pop(slot, None)
         if isinstance(vis, np.ndarray):
             vis = np.ascontiguousarray(vis)
             uvw = np.ascontiguousarray(uvw, dtype=np.float64)
@@ -213,6 +226,8 @@ class Context:
         else:  # torch tensor on the device
             import torch
             assert vis.is_cuda and vis.is_contiguous() and uvw.is_cuda and uvw.is_contiguous()
+            # The copy runs on the context's stream: finish torch's pending work on the inputs first.
+            torch.cuda.synchronize(vis.device)
             vt = {torch.complex64: _abi.LEAP_VIS_C64, torch.complex128: _abi.LEAP_VIS_C128}[vis.dtype]
             C, rows, P = vis.shape
             self._check(lib.leap_set_integration(self._h, slot, vt, vis.data_ptr(), uvw.data_ptr(), rows, C, P,
@@ -220,6 +235,7 @@ class Context:
         self.slots[slot] = (C, rows, P)
 
     def release_integration(self, slot: int):
+        self.autograd_slots.pop(slot, None)
         self._check(lib.leap_release_integration(self._h, slot))
         self.slots.pop(slot, None)
 
@@ -248,8 +264,11 @@ class Context:
     def set_option(self, option: int, value: int):
         self._check(lib.leap_set_option(self._h, int(option), int(value)))
 
-    def calibrate_async(self, slot: int, dd_ptr: int, ndir: int, precision: int, cal_ptr: int, stream: int = 0):
-        self._check(lib.leap_calibrate_async(self._h, slot, dd_ptr, ndir, precision, cal_ptr, stream or None))
+    def calibrate_async(self, slot: int, dd_ptr: int, ndir: int, precision: int, cal_ptr: int,
+                        stream: Optional[int] = None):
+        """Device pointers; `stream` is a cudaStream_t handle (torch's Stream.cuda_stream; 0 is the
+        legacy default stream), None the context's own stream."""
+        self._check(lib.leap_calibrate_async(self._h, slot, dd_ptr, ndir, precision, cal_ptr, stream_handle(stream)))
 
     def avgdata(self, direction: int) -> np.ndarray:
         """avgData of one direction from the last call, as (nbl, pols) complex128."""

@@ -128,7 +128,8 @@ int32_t leap_calibrate(leap_ctx* ctx, int32_t slot, const double* dd, int32_t nd
                        double* cal_out);
 
 /* Same with DEVICE pointers, stream-ordered on `stream` (a cudaStream_t; NULL
- * selects the context's stream).  Does not synchronise; the context's scratch
+ * selects the context's own non-blocking stream; pass cudaStreamLegacy to order
+ * the call with work on the legacy default stream).  Does not synchronise; the context's scratch
  * buffers are shared by all calls, so calls on different streams must not overlap. */
 int32_t leap_calibrate_async(leap_ctx* ctx, int32_t slot, const double* d_dd, int32_t ndirections,
                              int32_t precision, double* d_cal_out, void* stream);
@@ -159,6 +160,35 @@ int32_t leap_set_option(leap_ctx* ctx, int32_t option, int32_t value);
  * (pols x nbl complex doubles): MetaData::GetAvgData after RotateVisibilities
  * (LA/model/cpu/MetaData.h:127; DeviceMetaData::ToHost). */
 int32_t leap_get_avgdata(leap_ctx* ctx, int32_t direction, double* out);
+
+/* Device-side copy of pol `pol` of the avgData of every direction of the last
+ * calibrate call: d_out is [ndirections][nbl] complex doubles (DEVICE), written
+ * on `stream` (NULL: the context's stream).  In the mixed form the
+ * reference-antenna rows hold the compensated sums the solve used. */
+int32_t leap_get_avgdata_device(leap_ctx* ctx, int32_t pol, double* d_out, void* stream);
+
+/* Adjoint of one calibrate call (rotate -> average -> arg -> solve), in FP64.
+ * Replaces nothing in the reference (its path has no gradient); it is the
+ * backward of the differentiable form for the Python leap_drops layer.
+ * Inputs (DEVICE, on `stream`; NULL: the context's stream):
+ *   d_dd        [ndirections][9] the direction matrices of the forward call
+ *   d_avg0      [ndirections][nbl] complex: pol 0 of the forward's avgData
+ *               (leap_get_avgdata_device right after the forward call)
+ *   d_grad_cal  [ndirections][S] dL/dcal
+ *   d_vis       the caller's own visibilities of slot `slot` (same type and
+ *               layout as given to leap_set_integration), used to recompute the
+ *               rotated samples and to find NaN groups; NULL: the slot's copy
+ *               (same dL/d(l,m,n); NaN groups then receive a vis gradient)
+ * Outputs:
+ *   d_grad_lmn  [ndirections][3] dL/d(third row of dd) = dL/d(l, m, n)
+ *   d_grad_vis  [channels][rows][pols] dL/dV as complex gradients
+ *               (dL/dRe + i dL/dIm), element type of the slot; only pol 0 is
+ *               non-zero; NULL: not computed.
+ * The chain rule ignores arg()'s 2*pi jumps: gradients hold on the smooth
+ * branch, away from angles at +-pi. */
+int32_t leap_backward(leap_ctx* ctx, int32_t slot, const double* d_dd, int32_t ndirections, const double* d_avg0,
+                      const double* d_grad_cal, const void* d_vis, double* d_grad_lmn, void* d_grad_vis,
+                      void* stream);
 
 /* Rotate the UVWs of a resident integration by ndirections direction matrices
  * (host dd, host out [ndirections][rows][3]).  Replaces MetaData::CalcUVW /
