@@ -99,7 +99,7 @@ class ClockSampler:
 
 def make_workload(args, rank: int):
     from leap_gb300 import synth
-    obs, dirs = synth.mwa_precision(timesteps=args.timesteps, channels=args.channels, directions=args.directions)
+    obs, dirs = synth.mwa_precision(timesteps=args.timesteps or 14, channels=args.channels, directions=args.directions)
     if rank:
         # Each rank calibrates its own directions (same array and integration).
         _, lm = synth.random_directions(args.directions, seed=3 + 1000 * rank)
@@ -215,7 +215,7 @@ def setup_single(args, ctx, lg, torch, local, rank, kind: str):
         w.name = (f"mwa_precision {obs.num_stations}ant/{obs.nbaselines}bl/{obs.timesteps}t/{obs.channels}ch/"
                   f"{obs.pols}pol/{len(dirs)}dir c64")
     else:
-        obs, dirs = synth.ska_low(with_vis=False, directions=args.directions or 128)
+        obs, dirs = synth.ska_low(with_vis=False, timesteps=args.timesteps or 16, directions=args.directions or 128)
         if rank:
             _, lm = synth.random_directions(len(dirs), seed=3 + 1000 * rank)
             dirs = synth.lm_to_radec(lm[:, 0], lm[:, 1])
@@ -349,6 +349,51 @@ def setup_batched(args, ctx, lg, torch, local, rank):
     return w
 
 
+def setup_differentiable(args, ctx, lg, torch, local, rank):
+    """Forward + backward of the differentiable form: 128 antennas, 8 timesteps, 96 channels,
+    16 directions, complex<float>; loss = sum of squared wrapped residuals to the gain phases,
+    gradients with respect to every direction's (l, m) and the visibilities."""
+    from leap_gb300 import synth
+    from leap_gb300.autograd import calibrate_lm
+    dev = f"cuda:{local}"
+    w = Workload()
+    nd = args.directions or 16
+    obs, _ = synth.mwa_precision(timesteps=8, channels=96, directions=nd)
+    _, lm = synth.random_directions(nd, seed=31 + 1000 * rank)
+    md = lg.build_metadata(obs)
+    ctx.set_metadata(md)
+    vis = torch.from_numpy(obs.vis).to(dev).requires_grad_()
+    uvw = torch.from_numpy(obs.uvw).to(dev)
+    gain = torch.from_numpy(np.angle(obs.gains)).to(dev)
+    lm_t = torch.from_numpy(lm).to(dev).requires_grad_()
+    holder = {}
+
+    def step(p):
+        lm_t.grad = None
+        vis.grad = None
+        cal = calibrate_lm(ctx, 0, lm_t, vis, uvw, p)
+        res = torch.atan2(torch.sin(cal - gain[None, :]), torch.cos(cal - gain[None, :]))
+        (res * res).sum().backward()
+        holder["cal"] = cal
+
+    w.step = step
+    w.result = lambda: holder["cal"].detach().cpu().numpy()
+    w.kernel_timing = "events"
+    w.extra_launches = 8  # leap_backward: 2 transposed contractions, cal1, 2 avgData, (l, m, n) + reduce, vis
+    w.obs, w.dirs, w.md, w.D, w.S = obs, None, md, nd, md.A.shape[1]
+    w.units = vis_dirs(obs, nd)
+    w.b_alg = alg_bytes(4.0 * obs.rows * obs.channels, obs.rows, nd, obs.nbaselines, 4, 8)
+    w.f_alg = fma_slots(obs.rows, obs.rows * obs.channels, nd, 4)
+    w.name = (f"differentiable {obs.num_stations}ant/{obs.nbaselines}bl/{obs.timesteps}t/{obs.channels}ch/4pol/"
+              f"{nd}dir c64: forward + FP64 adjoint (d/d(l,m) and d/dV)")
+    w.config = {"workload": w.name, "precision": args.precision, "l2": "inputs (203 MB) larger than L2; no flush"}
+    w.e2e_step = None
+    dirs = synth.lm_to_radec(lm[:, 0], lm[:, 1])
+    w.dirs = dirs
+    w.cpu_case = (obs, dirs, obs.vis[:, :obs.nbaselines, :])
+    return w
+
+
 def run_gpu(args, rank: int, world: int):
     import torch
     import leap_gb300 as lg
@@ -367,6 +412,8 @@ def run_gpu(args, rank: int, world: int):
     torch.cuda.set_stream(bstream)
     if args.workload == "batched":
         w = setup_batched(args, ctx, lg, torch, local, rank)
+    elif args.workload == "differentiable":
+        w = setup_differentiable(args, ctx, lg, torch, local, rank)
     else:
         w = setup_single(args, ctx, lg, torch, local, rank, args.workload)
     prec = lg.LEAP_PRECISION_MIXED if args.precision == "mixed" else lg.LEAP_PRECISION_FP64
@@ -404,7 +451,7 @@ def run_gpu(args, rank: int, world: int):
     clocks = clk.summary()
     value = w.units * world / (ms / 1e3)
     cal_main = w.result()
-    gpu_launches = int(tim.kernels) * args.steps
+    gpu_launches = (int(tim.kernels) + getattr(w, "extra_launches", 0)) * args.steps
 
     checks = {}
     plain = None
@@ -449,6 +496,9 @@ def run_gpu(args, rank: int, world: int):
     if w.kernel_timing == "rotate":
         k_ms = tim.rotate_ms / max(1, tim.calls)
         k_name = "rotate_average (mixed: persistent TMA-pipelined kernel + compensated reference-antenna pass)"
+    elif w.kernel_timing == "events":
+        k_ms = ms
+        k_name = "whole forward + backward step"
     else:
         k_ms = ms
         k_name = "whole batched call (graph replay)"
@@ -502,10 +552,10 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--precision", default="mixed", choices=["mixed", "fp64"])
-    ap.add_argument("--workload", default="mwa", choices=["mwa", "batched", "ska_low"],
+    ap.add_argument("--workload", default="mwa", choices=["mwa", "batched", "ska_low", "differentiable"],
                     help="mwa: 128 antennas, 14 t, 384 ch, 64 directions (default); batched: 32 uneven chunks, "
                          "256 directions; ska_low: 512 stations, 16 t, 384 ch, 128 directions")
-    ap.add_argument("--timesteps", type=int, default=14)
+    ap.add_argument("--timesteps", type=int, default=0, help="0: the workload's own count (MWA 14, SKA-Low 16)")
     ap.add_argument("--channels", type=int, default=384)
     ap.add_argument("--directions", type=int, default=0, help="0: the workload's own count")
     ap.add_argument("--chunks", type=int, default=32)

@@ -4,8 +4,11 @@
 // contiguous range of directions (the single-integration call is one item; a
 // batched call has one item per integration chunk).  An item is cut into units
 // = (group of TPB 32-baseline tiles, group of (NC/TPB)*DPW directions,
-// timestep slab); units of all items are numbered consecutively and visited
-// round-robin by persistent blocks, so uneven chunks share one launch.
+// timestep slab); units of all items are numbered consecutively, so uneven
+// chunks share one launch.  The host assigns units to the persistent blocks
+// longest first, each to the least-loaded block, and passes the result as an
+// order table (block b visits order[b], order[b + grid], ... up to a -1), so
+// blocks finish together even when unit sizes differ by 100x.
 //
 // A unit is a sequence of chunks = (timestep, CH channels).  The visibility
 // tensor of an item is viewed as a 2-D array [channel][row*8 floats]; a chunk
@@ -51,6 +54,8 @@ struct alignas(128) PipeItem {
 
 struct PipeParams {
   const PipeItem* items;
+  const int32_t* order;    // [nslots]: block b visits units order[b], order[b + grid], ... until -1
+  int32_t nslots;
   int32_t nitems, units;
   int32_t nbl;
   const float* dirk;       // [ndir_total][12]
@@ -75,20 +80,28 @@ __host__ __device__ constexpr int pipe_smem_bytes() {
   return kPipeStages * pipe_stage_bytes<TPB>() + kTwiddleSize * 8 + 2 * kPipeStages * 8 + kPipeMaxItems * 4;
 }
 
-// Position in a block's chunk sequence.
+// Position in a block's chunk sequence: slot s of the order table, unit u = order[s].
 struct ChunkCursor {
-  int u, item, t, cb;
+  int s, u, item, t, cb;
   int t_hi;
 };
 
-__device__ __forceinline__ int find_item(const int* unit_begin, int nitems, int u, int hint) {
-  int i = hint;
-  while (i + 1 < nitems && unit_begin[i + 1] <= u) ++i;
-  return i;
+// Item holding unit u: the last item whose first unit is <= u (binary search; units of
+// an item are consecutive and items are in unit order).
+__device__ __forceinline__ int find_item(const int* unit_begin, int nitems, int u) {
+  int lo = 0, hi = nitems - 1;
+  while (lo < hi) {
+    const int mid = (lo + hi + 1) >> 1;
+    if (unit_begin[mid] <= u) lo = mid;
+    else hi = mid - 1;
+  }
+  return lo;
 }
 
+__device__ __forceinline__ int slot_unit(const PipeParams& p, int s) { return s < p.nslots ? __ldg(p.order + s) : -1; }
+
 __device__ __forceinline__ void cursor_unit(ChunkCursor& k, const PipeParams& p, const int* unit_begin) {
-  k.item = find_item(unit_begin, p.nitems, k.u, k.item);
+  k.item = find_item(unit_begin, p.nitems, k.u);
   const PipeItem& it = p.items[k.item];
   const int slab = (k.u - it.unit_begin) % it.nslab;
   k.t = slab * it.t_per_slab;
@@ -102,8 +115,9 @@ __device__ __forceinline__ void cursor_next(ChunkCursor& k, const PipeParams& p,
   if (k.cb < p.items[k.item].C) return;
   k.cb = 0;
   if (++k.t < k.t_hi) return;
-  k.u += gridDim.x;
-  if (k.u < p.units) cursor_unit(k, p, unit_begin);
+  k.s += gridDim.x;
+  k.u = slot_unit(p, k.s);
+  if (k.u >= 0) cursor_unit(k, p, unit_begin);
 }
 
 template <int TPB>
@@ -166,10 +180,11 @@ __global__ void __launch_bounds__(NC * 32, 1) rotate_average_mixed_pipe(const Pi
       mbar_init(&empty[i], NC);
     }
     fence_mbar_init();
-    pc.u = blockIdx.x;
+    pc.s = blockIdx.x;
+    pc.u = slot_unit(p, pc.s);
     pc.item = 0;
-    if (pc.u < p.units) cursor_unit(pc, p, unit_begin);
-    for (; issued < kPipeStages && pc.u < p.units; ++issued) {
+    if (pc.u >= 0) cursor_unit(pc, p, unit_begin);
+    for (; issued < kPipeStages && pc.u >= 0; ++issued) {
       issue_chunk<TPB>(pc, p, stage_mem, full, issued);
       cursor_next<TPB>(pc, p, unit_begin);
     }
@@ -181,8 +196,10 @@ __global__ void __launch_bounds__(NC * 32, 1) rotate_average_mixed_pipe(const Pi
   uint32_t it = 0;
   bool ok = true;
   int item = 0;
-  for (int u = blockIdx.x; u < p.units && ok; u += gridDim.x) {
-    item = find_item(unit_begin, p.nitems, u, item);
+  for (int sl = blockIdx.x; ok; sl += gridDim.x) {
+    const int u = slot_unit(p, sl);
+    if (u < 0) break;
+    item = find_item(unit_begin, p.nitems, u);
     const PipeItem& I = p.items[item];
     const int l = u - I.unit_begin;
     const int tg = l / (I.dgroups * I.nslab);
@@ -276,7 +293,7 @@ __global__ void __launch_bounds__(NC * 32, 1) rotate_average_mixed_pipe(const Pi
         }
         __syncwarp();
         if (lane == 0) mbar_arrive(&empty[st]);
-        if (producer && pc.u < p.units) {
+        if (producer && pc.u >= 0) {
           // Refill this stage with the chunk kPipeStages ahead once every warp released it.
           if (!mbar_wait_bounded(&empty[st], (it / kPipeStages) & 1)) {
             atomicOr(p.err, kDevErrTimeout);

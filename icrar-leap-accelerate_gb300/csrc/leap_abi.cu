@@ -6,6 +6,7 @@
 #include <cstdio>
 #include <cstring>
 #include <map>
+#include <queue>
 #include <memory>
 #include <string>
 #include <vector>
@@ -109,9 +110,10 @@ struct leap_ctx {
   cudaGraphExec_t graph_exec = nullptr;
   uint64_t graph_epoch = 0;
   std::vector<PipeItem> pipe_items_host;
+  std::vector<int32_t> pipe_order_host;
   std::vector<ReduceItem> reduce_items_host, refant_reduce_host;
   std::vector<RefantItem> refant_items_host;
-  DeviceBuffer pipe_items, reduce_items, refant_items, refant_reduce;
+  DeviceBuffer pipe_items, pipe_order, reduce_items, refant_items, refant_reduce;
   cudaStream_t stream = nullptr;
   std::string err;
   Metadata md;
@@ -328,6 +330,44 @@ int rotate_stage(leap_ctx* ctx, const std::vector<WorkItem>& items, const double
         it.out = ctx->avg.as<double2>() + static_cast<int64_t>(it.dir0) * 4 * nbl;
       }
     }
+    // Unit schedule: longest unit first, each to the least-loaded block (cost in channel
+    // steps: timesteps x (padded channels + a per-timestep set-up allowance)).
+    const int grid = std::min(units, ctx->sms);
+    {
+      const int CH = tpb == 4 ? PipeShape<4>::CH : PipeShape<1>::CH;
+      std::vector<std::pair<int64_t, int>> cost;
+      cost.reserve(units);
+      for (const PipeItem& it : pit) {
+        const int64_t per_t = static_cast<int64_t>((it.C + CH - 1) / CH) * CH + 8;
+        const int per_item = it.tgroups * it.dgroups * it.nslab;
+        for (int l = 0; l < per_item; ++l) {
+          const int slab = l % it.nslab;
+          const int t_lo = slab * it.t_per_slab, t_hi = std::min(it.T, t_lo + it.t_per_slab);
+          cost.emplace_back(-(t_hi - t_lo) * per_t, it.unit_begin + l);
+        }
+      }
+      std::stable_sort(cost.begin(), cost.end());
+      std::vector<std::vector<int32_t>> lists(grid);
+      std::priority_queue<std::pair<int64_t, int>, std::vector<std::pair<int64_t, int>>, std::greater<>> load;
+      for (int b = 0; b < grid; ++b) load.emplace(0, b);
+      for (const auto& c : cost) {
+        auto [l, b] = load.top();
+        load.pop();
+        lists[b].push_back(c.second);
+        load.emplace(l - c.first, b);
+      }
+      size_t rounds = 0;
+      for (const auto& l : lists) rounds = std::max(rounds, l.size());
+      std::vector<int32_t>& order = ctx->pipe_order_host;
+      order.assign(rounds * grid + grid, -1);  // one extra round of -1 ends every block
+      for (int b = 0; b < grid; ++b)
+        for (size_t k = 0; k < lists[b].size(); ++k) order[k * grid + b] = lists[b][k];
+      LEAP_CUDA(ctx->pipe_order.ensure(sizeof(int32_t) * order.size()), "alloc unit order");
+      if (!ctx->capturing)
+        LEAP_CUDA(cudaMemcpyAsync(ctx->pipe_order.ptr, order.data(), sizeof(int32_t) * order.size(),
+                                  cudaMemcpyHostToDevice, s),
+                  "upload unit order");
+    }
     LEAP_CUDA(ctx->pipe_items.ensure(sizeof(PipeItem) * pit.size()), "alloc item table");
     if (!ctx->capturing)
       LEAP_CUDA(cudaMemcpyAsync(ctx->pipe_items.ptr, pit.data(), sizeof(PipeItem) * pit.size(), cudaMemcpyHostToDevice, s),
@@ -343,13 +383,14 @@ int rotate_stage(leap_ctx* ctx, const std::vector<WorkItem>& items, const double
     ++kernels;
     PipeParams pp{};
     pp.items = ctx->pipe_items.as<PipeItem>();
+    pp.order = ctx->pipe_order.as<int32_t>();
+    pp.nslots = static_cast<int32_t>(ctx->pipe_order_host.size());
     pp.nitems = static_cast<int32_t>(pit.size());
     pp.units = units;
     pp.nbl = nbl;
     pp.dirk = ctx->dirk.as<float>();
     pp.twiddle = ctx->twiddle.as<float2>();
     pp.err = ctx->dev_err.as<int>();
-    const int grid = std::min(units, ctx->sms);
     if (tpb == 4) {
       if (!ctx->pipe_attr_set4) {
         LEAP_CUDA(cudaFuncSetAttribute(rotate_average_mixed_pipe<kPipeNC, kPipeDPW, 4>,
@@ -906,6 +947,7 @@ void leap_destroy(leap_ctx* ctx) {
     ctx->partial_i1.release();
     ctx->avg_i1.release();
     ctx->pipe_items.release();
+    ctx->pipe_order.release();
     ctx->reduce_items.release();
     ctx->refant_items.release();
     ctx->refant_reduce.release();
