@@ -12,9 +12,12 @@ is needed between steps.
 
   value      inputs resident in HBM, the mixed-precision form, CUDA events on
              the launching stream around exactly --steps calls
-  e2e        the public C ABI with host buffers: per step the pinned host->device
-             upload of the step's visibilities + UVWs (leap_set_integration), the
-             calibration (leap_calibrate) and the device->host read of the cal phases
+  e2e        the public C ABI with host buffers: per step the visibilities in
+             MeasurementSet order ([row][channel][pol], page-locked host memory) +
+             UVWs go up through leap_set_integration_ms (transposed on the device),
+             then leap_calibrate with host dd / cal buffers; the upload of the
+             pre-transposed Integration layout (leap_set_integration) is reported
+             beside it
   plain_fp64 the all-FP64 form on the same workload
   roofline   the rotate+average kernel against the measured HBM copy bandwidth
   cpu_baseline  the oracle port (C, OpenMP over directions) on a bounded sample
@@ -260,6 +263,12 @@ def setup_single(args, ctx, lg, torch, local, rank, kind: str):
                 "l2": f"inputs ({obs.vis.nbytes / 1e9 if obs.vis is not None else obs.rows * obs.channels * 32 / 1e9:.2f} GB)"
                       " larger than L2; no flush"}
     if vis_host is not None:
+        # The host holds the visibilities in MeasurementSet order, [row][channel][pol]
+        # (page-locked); each step ingests them through leap_set_integration_ms, which
+        # transposes on the device, then calibrates with host dd / cal buffers.
+        ms_host = torch.empty((vis_host.shape[1], vis_host.shape[0], vis_host.shape[2]), dtype=vis_host.dtype,
+                              pin_memory=True)
+        ms_host.copy_(vis_host.permute(1, 0, 2))
         vis_np = vis_host.numpy()
         uvw_np = uvw_host.numpy()
         cal_host = np.zeros((D, S), dtype=np.float64)
@@ -268,11 +277,17 @@ def setup_single(args, ctx, lg, torch, local, rank, kind: str):
         from leap_gb300 import _abi
 
         def e2e_step():
+            ctx._check(_abi.lib.leap_set_integration_ms(ctx.handle, 0, _abi.LEAP_VIS_C64, ms_host.data_ptr(), C, 0,
+                                                        uvw_np.ctypes.data, rows, C, P, _abi.LEAP_MEMORY_HOST))
+            ctx._check(_abi.lib.leap_calibrate(ctx.handle, 0, dds.ctypes.data, D, prec, cal_host.ctypes.data))
+
+        def e2e_layout_step():
             ctx._check(_abi.lib.leap_set_integration(ctx.handle, 0, _abi.LEAP_VIS_C64, vis_np.ctypes.data,
                                                      uvw_np.ctypes.data, rows, C, P, _abi.LEAP_MEMORY_HOST))
             ctx._check(_abi.lib.leap_calibrate(ctx.handle, 0, dds.ctypes.data, D, prec, cal_host.ctypes.data))
 
         w.e2e_step = e2e_step
+        w.e2e_alt = ("integration_layout_upload", e2e_layout_step)
         w.h2d = vis_np.nbytes + uvw_np.nbytes + dds.nbytes
         w.d2h = cal_host.nbytes
     else:
@@ -490,6 +505,15 @@ def run_gpu(args, rank: int, world: int):
             e2e_s = float(tt.item())
         e2e = {"value": w.units * world / e2e_s, "unit": "vis-directions/s", "h2d_bytes_per_step": int(w.h2d),
                "d2h_bytes_per_step": int(w.d2h), "ms_per_step": e2e_s * 1e3, "steps": e2e_steps}
+        alt = getattr(w, "e2e_alt", None)
+        if alt is not None:
+            name, fn = alt
+            fn()
+            t0 = time.perf_counter()
+            for _ in range(e2e_steps):
+                fn()
+            e2e[name] = {"value": w.units * world / ((time.perf_counter() - t0) / e2e_steps),
+                         "ms_per_step": (time.perf_counter() - t0) / e2e_steps * 1e3}
 
     peaks = _peaks()
     peak = peaks["hbm_gbs"] if peaks else 6800.0

@@ -56,15 +56,11 @@ cpu::CalibrationCollection GpuLeapCalibrator::Calibrate(const MeasurementSet& ms
     const uint32_t startRow = static_cast<uint32_t>(s) * interval.interval * nbl;
     const uint32_t rows = static_cast<uint32_t>(interval.interval) * nbl;
     const std::vector<double> uvw = ms.GetCoords(startRow, rows);
-    if (ms.HasFloatData()) {
-      const auto vis = ms.GetVisF32(startRow, 0, C, rows, P);
-      check(leap_set_integration(m_ctx, 0, LEAP_VIS_C64, vis.data(), uvw.data(), rows, C, P, LEAP_MEMORY_HOST), m_ctx,
-            "leap_set_integration");
-    } else {
-      const auto vis = ms.GetVis(startRow, 0, C, rows, P);
-      check(leap_set_integration(m_ctx, 0, LEAP_VIS_C128, vis.data(), uvw.data(), rows, C, P, LEAP_MEMORY_HOST), m_ctx,
-            "leap_set_integration");
-    }
+    // The interval's rows go up in MeasurementSet order; the device transposes them
+    // (the reference's host-side GetVis transpose, LA/ms/MeasurementSet.h:95-204).
+    check(leap_set_integration_ms(m_ctx, 0, ms.HasFloatData() ? LEAP_VIS_C64 : LEAP_VIS_C128, ms.GetRawVis(startRow), C,
+                                  0, uvw.data(), rows, C, P, LEAP_MEMORY_HOST),
+          m_ctx, "leap_set_integration_ms");
     std::vector<double> cal(static_cast<size_t>(S) * directions.size());
     check(leap_calibrate(m_ctx, 0, dd.data(), static_cast<int32_t>(directions.size()), m_options.precision, cal.data()),
           m_ctx, "leap_calibrate");

@@ -77,6 +77,13 @@ class MeasurementSet {
   std::vector<std::complex<float>> GetVisF32(uint32_t startRow, uint32_t startChannel, uint32_t nChannels,
                                              uint32_t nRows, uint32_t nPols) const;
   bool HasFloatData() const { return !m_data.data32.empty(); }
+  // DATA in the MeasurementSet's own order, [row][channel][pol], from row startRow
+  // (what casacore hands out for the DATA column); the device transposes it.
+  const void* GetRawVis(uint32_t startRow) const {
+    const size_t off = static_cast<size_t>(startRow) * m_data.channels * m_data.pols;
+    return HasFloatData() ? static_cast<const void*>(m_data.data32.data() + off)
+                          : static_cast<const void*>(m_data.data64.data() + off);
+  }
 
   const MeasurementSetData& GetData() const { return m_data; }
 

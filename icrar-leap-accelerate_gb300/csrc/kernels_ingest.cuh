@@ -1,0 +1,81 @@
+// MeasurementSet ingestion on the device: the MS DATA column is row-major
+// [row][channel][pol] (LA/ms/utils.h:81-146, where the reference transposes and
+// widens it on the host); the Integration layout is [channel][row][pol]
+// (column-major (pol, row, channel), LA/model/cpu/Integration.h:73).  One
+// kernel does the transpose through a shared-memory tile and applies the NaN
+// rule on the way (a (row, channel) group with a NaN in any pol is zeroed, so
+// it adds nothing to the averages, as CpuLeapCalibrator.cc:201-214 skips it).
+//
+// The source may be device memory or page-locked host memory (read directly
+// over the host link, no staging copy).  Tile: 32 rows x TC channels of
+// (pol group) elements; reads are contiguous along channels, writes along rows.
+#pragma once
+
+#include "leap_common.cuh"
+
+namespace leapgb {
+
+template <typename VisT, int P>
+struct IngestGroup {
+  VisT v[P];
+};
+
+template <typename VisT> struct IngestTile;
+template <> struct IngestTile<float2> { static constexpr int TC = 32; };
+template <> struct IngestTile<double2> { static constexpr int TC = 16; };
+
+// src: element (r, c, p) of the selected block at src[(r * row_channels + start_channel + c) * P + p],
+// r in [0, nrows); dst: the integration [channels][rows_total][P], rows [row0, row0 + nrows).
+template <typename VisT, int P>
+__global__ void __launch_bounds__(256) ingest_ms_transpose(const VisT* __restrict__ src, int64_t row_channels,
+                                                           int start_channel, int64_t nrows, int channels,
+                                                           VisT* __restrict__ dst, int64_t rows_total, int64_t row0) {
+  constexpr int TR = 32, TC = IngestTile<VisT>::TC;
+  using G = IngestGroup<VisT, P>;
+  __shared__ G tile[TC][TR + 1];
+  const int64_t r_tiles = (nrows + TR - 1) / TR;
+  const int c_tiles = (channels + TC - 1) / TC;
+  for (int64_t t = blockIdx.x; t < r_tiles * c_tiles; t += gridDim.x) {
+    const int64_t rt = t % r_tiles;
+    const int ct = static_cast<int>(t / r_tiles);
+    const int64_t rbase = rt * TR;
+    const int cbase = ct * TC;
+    // load: threads run along channels (contiguous in the MS row)
+    for (int i = threadIdx.x; i < TR * TC; i += blockDim.x) {
+      const int lc = i % TC, lr = i / TC;
+      const int64_t r = rbase + lr;
+      const int c = cbase + lc;
+      G g;
+      if (r < nrows && c < channels) {
+        const VisT* s = src + (r * row_channels + start_channel + c) * P;
+        bool nan = false;
+#pragma unroll
+        for (int p = 0; p < P; ++p) {
+          g.v[p] = s[p];
+          nan |= isnan(g.v[p].x) || isnan(g.v[p].y);
+        }
+        if (nan) {
+#pragma unroll
+          for (int p = 0; p < P; ++p) g.v[p].x = g.v[p].y = 0;
+        }
+        tile[lc][lr] = g;
+      }
+    }
+    __syncthreads();
+    // store: threads run along rows (contiguous in the integration)
+    for (int i = threadIdx.x; i < TR * TC; i += blockDim.x) {
+      const int lr = i % TR, lc = i / TR;
+      const int64_t r = rbase + lr;
+      const int c = cbase + lc;
+      if (r < nrows && c < channels) {
+        VisT* d = dst + (static_cast<int64_t>(c) * rows_total + row0 + r) * P;
+        const G g = tile[lc][lr];
+#pragma unroll
+        for (int p = 0; p < P; ++p) d[p] = g.v[p];
+      }
+    }
+    __syncthreads();
+  }
+}
+
+}  // namespace leapgb

@@ -29,7 +29,8 @@
 // every kPipeReseed channels and advanced by one FP32 complex multiply per
 // channel in between (drift over 8 steps ~5e-7; it reaches the cal phases only
 // through baselines that the reference-antenna pass does not cover, with
-// weight ~1/S).  Sums: FP32 over each chunk, folded into Kahan pairs.
+// weight ~1/S).  Sums: FP32 over 16 channels (one or two chunks), folded into
+// Kahan pairs.
 //
 // Shared-memory reads: lane i reads its 32 bytes as two 16-byte halves; lanes
 // with bit 2 set read the upper half first so that each quarter-warp covers
@@ -65,6 +66,7 @@ struct PipeParams {
 
 constexpr int kPipeMaxItems = 128;
 constexpr int kPipeReseed = 8;          // channels between table-accurate twiddles
+constexpr int kPipeFold = 16;           // channels summed in FP32 before a Kahan fold
 constexpr int kPipeStages = 4;
 constexpr int kPipeItemBytes = 32 * 4 * 8;  // one channel of one tile: 32 baselines x 4 pols x complex<float>
 
@@ -241,6 +243,12 @@ __global__ void __launch_bounds__(NC * 32, 1) rotate_average_mixed_pipe(const Pi
           twiddle_turns(pb[j], tab, wr[j], wi[j]);
         }
       }
+      // FP32 partial sums of up to kPipeFold channels (one or two chunks), then a Kahan fold.
+      float pr[DPW][4], pi[DPW][4];
+#pragma unroll
+      for (int j = 0; j < DPW; ++j)
+#pragma unroll
+        for (int q = 0; q < 4; ++q) pr[j][q] = pi[j][q] = 0.f;
       for (int cb = 0; cb < C; cb += CH, ++it) {
         const int n = min(CH, C - cb);
         const int st = it % kPipeStages;
@@ -250,12 +258,7 @@ __global__ void __launch_bounds__(NC * 32, 1) rotate_average_mixed_pipe(const Pi
           break;
         }
         if (active) {
-          float pr[DPW][4], pi[DPW][4];
           float zr[DPW], zi[DPW];
-#pragma unroll
-          for (int j = 0; j < DPW; ++j)
-#pragma unroll
-            for (int q = 0; q < 4; ++q) pr[j][q] = pi[j][q] = 0.f;
           const unsigned char* src = stage_mem + st * pipe_stage_bytes<TPB>() + ts * CH * kPipeItemBytes + lane * 32;
           if (n == CH) {
 #pragma unroll
@@ -277,19 +280,22 @@ __global__ void __launch_bounds__(NC * 32, 1) rotate_average_mixed_pipe(const Pi
               mac_channel<DPW>(src + k * kPipeItemBytes, h, pr, pi, zr, zi, wr, wi);
             }
           }
+          if ((cb + CH) % kPipeFold == 0 || cb + CH >= C) {
 #pragma unroll
-          for (int j = 0; j < DPW; ++j)
+            for (int j = 0; j < DPW; ++j)
 #pragma unroll
-            for (int q = 0; q < 4; ++q) {
-              float y = pr[j][q] - cr[j][q];
-              float tt = sr[j][q] + y;
-              cr[j][q] = (tt - sr[j][q]) - y;
-              sr[j][q] = tt;
-              y = pi[j][q] - ci[j][q];
-              tt = si[j][q] + y;
-              ci[j][q] = (tt - si[j][q]) - y;
-              si[j][q] = tt;
-            }
+              for (int q = 0; q < 4; ++q) {
+                float y = pr[j][q] - cr[j][q];
+                float tt = sr[j][q] + y;
+                cr[j][q] = (tt - sr[j][q]) - y;
+                sr[j][q] = tt;
+                y = pi[j][q] - ci[j][q];
+                tt = si[j][q] + y;
+                ci[j][q] = (tt - si[j][q]) - y;
+                si[j][q] = tt;
+                pr[j][q] = pi[j][q] = 0.f;
+              }
+          }
         }
         __syncwarp();
         if (lane == 0) mbar_arrive(&empty[st]);

@@ -19,6 +19,7 @@
 #include "kernels_solve.cuh"
 #include "kernels_tc.cuh"
 #include "kernels_adjoint.cuh"
+#include "kernels_ingest.cuh"
 
 using namespace leapgb;
 
@@ -105,6 +106,12 @@ struct leap_ctx {
   int tc_attr_set = 0;                // bit per N tile whose shared-memory size was raised
   DeviceBuffer dphi_tc;               // packed dphi operand of the tensor-core contraction
   DeviceBuffer adj_dphi, adj_cal1, adj_phi1, adj_gavg, adj_partial;  // adjoint scratch
+  // MeasurementSet-order ingestion from pageable host memory: two pinned staging
+  // buffers and their device twins, each reused once its piece has been transposed.
+  static constexpr size_t kStageBytes = size_t(64) << 20;
+  void* stage_host[2] = {nullptr, nullptr};
+  DeviceBuffer stage_dev[2];
+  cudaEvent_t stage_done[2] = {nullptr, nullptr};
   std::map<std::string, TuneChoice> tuned;
   std::string graph_key;
   cudaGraphExec_t graph_exec = nullptr;
@@ -861,6 +868,60 @@ int fill_timings(leap_ctx* ctx, leap_timings* out) {
   return LEAP_OK;
 }
 
+// Split UVWs, record the shape and build the TMA views of a freshly written integration.
+int finish_integration(leap_ctx* ctx, Integration& in, int32_t vis_type, int64_t rows, int32_t channels, int32_t pols) {
+  LEAP_CUDA(in.uvw_f.ensure(sizeof(float) * 6 * rows), "alloc split uvw");
+  split_uvw<<<grid_1d(3 * rows, 256), 256, 0, ctx->stream>>>(in.uvw.as<double>(), rows, in.uvw_f.as<float>());
+  LEAP_CUDA(cudaGetLastError(), "ingestion launch");
+  LEAP_CUDA(cudaStreamSynchronize(ctx->stream), "set integration");
+  in.vis_type = vis_type;
+  in.rows = rows;
+  in.channels = channels;
+  in.pols = pols;
+  in.has_map = false;
+  if (vis_type == LEAP_VIS_C64 && pols == 4 && rows * 8 < (int64_t(1) << 31)) {
+    // The pipelined kernel's view: 2-D floats [channels][rows*8], box 256 x (16 or 8) channels.
+    auto enc = tensor_map_encoder();
+    if (!enc) return fail(ctx, LEAP_ERR_CUDA, "cuTensorMapEncodeTiled unavailable");
+    cuuint64_t dims[2] = {static_cast<cuuint64_t>(rows) * 8, static_cast<cuuint64_t>(channels)};
+    cuuint64_t strides[1] = {static_cast<cuuint64_t>(rows) * 32};
+    cuuint32_t estr[2] = {1, 1};
+    for (int which = 0; which < 2; ++which) {
+      cuuint32_t box[2] = {256, static_cast<cuuint32_t>(which == 0 ? PipeShape<1>::CH : PipeShape<4>::CH)};
+      CUresult r = enc(which == 0 ? &in.map16 : &in.map8, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 2, in.vis.ptr, dims, strides,
+                       box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
+                       CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+      if (r != CUDA_SUCCESS) return fail(ctx, LEAP_ERR_CUDA, "cuTensorMapEncodeTiled failed: " + std::to_string(r));
+    }
+    in.has_map = true;
+  }
+  return LEAP_OK;
+}
+
+template <typename VisT>
+int launch_ingest(leap_ctx* ctx, const void* src, int64_t row_channels, int32_t start_channel, int64_t nrows,
+                  int32_t channels, int32_t pols, void* dst, int64_t rows_total, int64_t row0, cudaStream_t s) {
+  const int TC = IngestTile<VisT>::TC;
+  const int64_t tiles = ((nrows + 31) / 32) * ((channels + TC - 1) / TC);
+  const int grid = static_cast<int>(std::max<int64_t>(1, std::min<int64_t>(tiles, static_cast<int64_t>(ctx->sms) * 8)));
+  const VisT* sp = static_cast<const VisT*>(src);
+  VisT* dp = static_cast<VisT*>(dst);
+  switch (pols) {
+    case 1: ingest_ms_transpose<VisT, 1><<<grid, 256, 0, s>>>(sp, row_channels, start_channel, nrows, channels, dp, rows_total, row0); break;
+    case 2: ingest_ms_transpose<VisT, 2><<<grid, 256, 0, s>>>(sp, row_channels, start_channel, nrows, channels, dp, rows_total, row0); break;
+    default: ingest_ms_transpose<VisT, 4><<<grid, 256, 0, s>>>(sp, row_channels, start_channel, nrows, channels, dp, rows_total, row0); break;
+  }
+  LEAP_CUDA(cudaGetLastError(), "ingestion kernel");
+  return LEAP_OK;
+}
+
+int ingest(leap_ctx* ctx, int32_t vis_type, const void* src, int64_t row_channels, int32_t start_channel, int64_t nrows,
+           int32_t channels, int32_t pols, void* dst, int64_t rows_total, int64_t row0, cudaStream_t s) {
+  return vis_type == LEAP_VIS_C64
+             ? launch_ingest<float2>(ctx, src, row_channels, start_channel, nrows, channels, pols, dst, rows_total, row0, s)
+             : launch_ingest<double2>(ctx, src, row_channels, start_channel, nrows, channels, pols, dst, rows_total, row0, s);
+}
+
 }  // namespace
 
 extern "C" {
@@ -951,6 +1012,13 @@ void leap_destroy(leap_ctx* ctx) {
     ctx->reduce_items.release();
     ctx->refant_items.release();
     ctx->refant_reduce.release();
+    ctx->adj_dphi.release(); ctx->adj_cal1.release(); ctx->adj_phi1.release(); ctx->adj_gavg.release();
+    ctx->adj_partial.release();
+    for (int b = 0; b < 2; ++b) {
+      ctx->stage_dev[b].release();
+      if (ctx->stage_host[b]) cudaFreeHost(ctx->stage_host[b]);
+      if (ctx->stage_done[b]) cudaEventDestroy(ctx->stage_done[b]);
+    }
   }
   delete ctx;
 }
@@ -1080,32 +1148,75 @@ int32_t leap_set_integration(leap_ctx* ctx, int32_t slot, int32_t vis_type, cons
     if (pols == 4) sanitize_nan_groups<double2, 4><<<grid, 256, 0, ctx->stream>>>(p, p, groups);
     else sanitize_nan_groups_generic<double2><<<grid, 256, 0, ctx->stream>>>(p, p, groups, pols);
   }
-  LEAP_CUDA(in.uvw_f.ensure(sizeof(float) * 6 * rows), "alloc split uvw");
-  split_uvw<<<grid_1d(3 * rows, 256), 256, 0, ctx->stream>>>(in.uvw.as<double>(), rows, in.uvw_f.as<float>());
-  LEAP_CUDA(cudaGetLastError(), "sanitize launch");
-  LEAP_CUDA(cudaStreamSynchronize(ctx->stream), "set integration");
-  in.vis_type = vis_type;
-  in.rows = rows;
-  in.channels = channels;
-  in.pols = pols;
-  in.has_map = false;
-  if (vis_type == LEAP_VIS_C64 && pols == 4 && rows * 8 < (int64_t(1) << 31)) {
-    // The pipelined kernel's view: 2-D floats [channels][rows*8], box 256 x (16 or 8) channels.
-    auto enc = tensor_map_encoder();
-    if (!enc) return fail(ctx, LEAP_ERR_CUDA, "cuTensorMapEncodeTiled unavailable");
-    cuuint64_t dims[2] = {static_cast<cuuint64_t>(rows) * 8, static_cast<cuuint64_t>(channels)};
-    cuuint64_t strides[1] = {static_cast<cuuint64_t>(rows) * 32};
-    cuuint32_t estr[2] = {1, 1};
-    for (int which = 0; which < 2; ++which) {
-      cuuint32_t box[2] = {256, static_cast<cuuint32_t>(which == 0 ? PipeShape<1>::CH : PipeShape<4>::CH)};
-      CUresult r = enc(which == 0 ? &in.map16 : &in.map8, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 2, in.vis.ptr, dims, strides,
-                       box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
-                       CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
-      if (r != CUDA_SUCCESS) return fail(ctx, LEAP_ERR_CUDA, "cuTensorMapEncodeTiled failed: " + std::to_string(r));
-    }
-    in.has_map = true;
+  return finish_integration(ctx, in, vis_type, rows, channels, pols);
+}
+
+
+int32_t leap_set_integration_ms(leap_ctx* ctx, int32_t slot, int32_t vis_type, const void* ms_data, int64_t row_channels,
+                                int32_t start_channel, const double* uvw, int64_t rows, int32_t channels, int32_t pols,
+                                int32_t memory) {
+  if (!ctx || !ms_data || !uvw) return fail(ctx, LEAP_ERR_INVALID_ARGUMENT, "NULL argument");
+  if (slot < 0) return fail(ctx, LEAP_ERR_INVALID_ARGUMENT, "slot must be >= 0");
+  if (vis_type != LEAP_VIS_C64 && vis_type != LEAP_VIS_C128) return fail(ctx, LEAP_ERR_INVALID_ARGUMENT, "unknown vis type");
+  if (rows <= 0 || channels <= 0 || pols <= 0) return fail(ctx, LEAP_ERR_INVALID_ARGUMENT, "empty integration");
+  if (pols != 1 && pols != 2 && pols != 4) return fail(ctx, LEAP_ERR_INVALID_ARGUMENT, "pols must be 1, 2 or 4");
+  if (start_channel < 0 || static_cast<int64_t>(start_channel) + channels > row_channels)
+    return fail(ctx, LEAP_ERR_INVALID_ARGUMENT, "channel range outside the MeasurementSet row");
+  if (memory != LEAP_MEMORY_HOST && memory != LEAP_MEMORY_DEVICE) return fail(ctx, LEAP_ERR_INVALID_ARGUMENT, "unknown memory kind");
+  DeviceGuard g(ctx->device);
+  Integration& in = ctx->integ[slot];
+  const size_t esz = vis_type == LEAP_VIS_C64 ? sizeof(float2) : sizeof(double2);
+  LEAP_CUDA(in.vis.ensure(esz * static_cast<size_t>(rows) * channels * pols), "alloc vis");
+  LEAP_CUDA(in.uvw.ensure(sizeof(double) * 3 * rows), "alloc uvw");
+  cudaStream_t s = ctx->stream;
+  LEAP_CUDA(cudaMemcpyAsync(in.uvw.ptr, uvw, sizeof(double) * 3 * rows,
+                            memory == LEAP_MEMORY_HOST ? cudaMemcpyHostToDevice : cudaMemcpyDeviceToDevice, s),
+            "copy uvw");
+  // A source the kernel can read directly: device memory, or page-locked host memory
+  // through its device mapping (read over the host link, no staging copy).
+  const void* direct = memory == LEAP_MEMORY_DEVICE ? ms_data : nullptr;
+  if (!direct) {
+    cudaPointerAttributes at{};
+    if (cudaPointerGetAttributes(&at, ms_data) == cudaSuccess && at.type == cudaMemoryTypeHost && at.devicePointer)
+      direct = at.devicePointer;
+    else
+      cudaGetLastError();  // pageable memory: not an error
   }
-  return LEAP_OK;
+  if (direct) {
+    int rc = ingest(ctx, vis_type, direct, row_channels, start_channel, rows, channels, pols, in.vis.ptr, rows, 0, s);
+    if (rc != LEAP_OK) return rc;
+  } else {
+    // Pageable host memory: pieces of whole rows go through the pinned staging buffers.
+    // The host copy of piece k overlaps the upload and transpose of piece k-1.
+    const size_t row_bytes = esz * static_cast<size_t>(channels) * pols;
+    const int64_t piece_rows = std::max<int64_t>(1, static_cast<int64_t>(leap_ctx::kStageBytes / row_bytes));
+    const size_t stage_bytes = row_bytes * static_cast<size_t>(std::min<int64_t>(piece_rows, rows));
+    for (int b = 0; b < 2; ++b) {
+      if (!ctx->stage_host[b]) {
+        LEAP_CUDA(cudaHostAlloc(&ctx->stage_host[b], std::max(stage_bytes, leap_ctx::kStageBytes), cudaHostAllocDefault),
+                  "alloc pinned staging");
+        LEAP_CUDA(cudaEventCreateWithFlags(&ctx->stage_done[b], cudaEventDisableTiming), "staging event");
+      }
+      LEAP_CUDA(ctx->stage_dev[b].ensure(std::max(stage_bytes, leap_ctx::kStageBytes)), "alloc device staging");
+    }
+    const unsigned char* base = static_cast<const unsigned char*>(ms_data);
+    const size_t src_row_bytes = esz * static_cast<size_t>(row_channels) * pols;
+    int k = 0;
+    for (int64_t r0 = 0; r0 < rows; r0 += piece_rows, ++k) {
+      const int b = k & 1;
+      const int64_t nr = std::min(piece_rows, rows - r0);
+      if (k >= 2) LEAP_CUDA(cudaEventSynchronize(ctx->stage_done[b]), "staging wait");
+      unsigned char* h = static_cast<unsigned char*>(ctx->stage_host[b]);
+      for (int64_t r = 0; r < nr; ++r)
+        std::memcpy(h + r * row_bytes, base + (r0 + r) * src_row_bytes + esz * static_cast<size_t>(start_channel) * pols,
+                    row_bytes);
+      LEAP_CUDA(cudaMemcpyAsync(ctx->stage_dev[b].ptr, h, row_bytes * nr, cudaMemcpyHostToDevice, s), "upload piece");
+      int rc = ingest(ctx, vis_type, ctx->stage_dev[b].ptr, channels, 0, nr, channels, pols, in.vis.ptr, rows, r0, s);
+      if (rc != LEAP_OK) return rc;
+      LEAP_CUDA(cudaEventRecord(ctx->stage_done[b], s), "staging event");
+    }
+  }
+  return finish_integration(ctx, in, vis_type, rows, channels, pols);
 }
 
 int32_t leap_release_integration(leap_ctx* ctx, int32_t slot) {

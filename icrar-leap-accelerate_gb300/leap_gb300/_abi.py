@@ -58,6 +58,7 @@ SIGNATURES = {
     "leap_last_error": ([vp], ctypes.c_char_p),
     "leap_set_metadata": ([vp, ctypes.POINTER(LeapConstants), vp, i32, i32, vp, vp, vp, i32, vp, vp], i32),
     "leap_set_integration": ([vp, i32, i32, vp, vp, i64, i32, i32, i32], i32),
+    "leap_set_integration_ms": ([vp, i32, i32, vp, i64, i32, vp, i64, i32, i32, i32], i32),
     "leap_release_integration": ([vp, i32], i32),
     "leap_calibrate": ([vp, i32, vp, i32, i32, vp], i32),
     "leap_calibrate_async": ([vp, i32, vp, i32, i32, vp, vp], i32),

@@ -234,6 +234,34 @@ class Context:
                                                  _abi.LEAP_MEMORY_DEVICE))
         self.slots[slot] = (C, rows, P)
 
+    def set_integration_ms(self, slot: int, ms_vis, uvw, start_channel: int = 0, channels: Optional[int] = None):
+        """Upload from the MeasurementSet's DATA order: ms_vis is (rows, row_channels, pols)
+        complex, a numpy array (pageable or not) or a torch tensor (CUDA, or pinned CPU memory);
+        channels [start_channel, start_channel + channels) are taken.  Transpose and NaN rule
+        run on the device (leap_set_integration_ms)."""
+        self.autograd_slots.pop(slot, None)
+        if isinstance(ms_vis, np.ndarray):
+            ms_vis = np.ascontiguousarray(ms_vis)
+            uvw = np.ascontiguousarray(uvw, dtype=np.float64)
+            rows, row_channels, P = ms_vis.shape
+            vt, vp, up, mem = _vis_type(ms_vis.dtype), _ptr(ms_vis), _ptr(uvw), _abi.LEAP_MEMORY_HOST
+        else:
+            import torch
+            assert ms_vis.is_contiguous() and uvw.is_contiguous() and uvw.dtype == torch.float64
+            vt = {torch.complex64: _abi.LEAP_VIS_C64, torch.complex128: _abi.LEAP_VIS_C128}[ms_vis.dtype]
+            rows, row_channels, P = ms_vis.shape
+            if ms_vis.is_cuda:
+                torch.cuda.synchronize(ms_vis.device)
+                mem = _abi.LEAP_MEMORY_DEVICE
+                assert uvw.is_cuda
+            else:
+                mem = _abi.LEAP_MEMORY_HOST
+                assert not uvw.is_cuda
+            vp, up = ms_vis.data_ptr(), uvw.data_ptr()
+        C = row_channels - start_channel if channels is None else channels
+        self._check(lib.leap_set_integration_ms(self._h, slot, vt, vp, row_channels, start_channel, up, rows, C, P, mem))
+        self.slots[slot] = (C, rows, P)
+
     def release_integration(self, slot: int):
         self.autograd_slots.pop(slot, None)
         self._check(lib.leap_release_integration(self._h, slot))

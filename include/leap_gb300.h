@@ -117,6 +117,19 @@ int32_t leap_set_metadata(leap_ctx* ctx, const leap_constants* constants, const 
 int32_t leap_set_integration(leap_ctx* ctx, int32_t slot, int32_t vis_type, const void* vis, const double* uvw,
                              int64_t rows, int32_t channels, int32_t pols, int32_t memory);
 
+/* Same, from the MeasurementSet's own DATA order: ms_data is row-major
+ * [rows][row_channels][pols] (the MS column layout that the reference transposes
+ * and widens on the host, LA/ms/utils.h:81-146 via MeasurementSet::GetVis,
+ * LA/ms/MeasurementSet.h:95-204); channels [start_channel, start_channel +
+ * channels) of each row are taken.  The transpose to the Integration layout and
+ * the NaN rule run on the device.  Device memory and page-locked host memory
+ * are read directly by the transpose kernel; pageable host memory goes through
+ * two pinned 64 MiB staging buffers, the host copy of one piece overlapping the
+ * upload and transpose of the previous one. */
+int32_t leap_set_integration_ms(leap_ctx* ctx, int32_t slot, int32_t vis_type, const void* ms_data,
+                                int64_t row_channels, int32_t start_channel, const double* uvw, int64_t rows,
+                                int32_t channels, int32_t pols, int32_t memory);
+
 /* Release the HBM held by one integration slot. */
 int32_t leap_release_integration(leap_ctx* ctx, int32_t slot);
 
