@@ -517,7 +517,7 @@ static __global__ void reduce_slabs(const double2* __restrict__ partial, int nsl
 // copying src -> dst (dst may equal src).  This applies the reference's
 // per-sample NaN skip (CpuLeapCalibrator.cc:201-214) once, at ingestion.
 template <typename VisT, int P>
-__global__ void sanitize_nan_groups(const VisT* __restrict__ src, VisT* __restrict__ dst, int64_t groups) {
+__global__ void sanitize_nan_groups(const VisT* src, VisT* dst, int64_t groups) {  // src may equal dst
   using S = typename VisScalar<VisT>::type;
   for (int64_t g = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x; g < groups;
        g += static_cast<int64_t>(gridDim.x) * blockDim.x) {
@@ -528,6 +528,7 @@ __global__ void sanitize_nan_groups(const VisT* __restrict__ src, VisT* __restri
       v[p] = src[g * P + p];
       nan |= isnan(v[p].x) || isnan(v[p].y);
     }
+    if (!nan && src == dst) continue;  // in place: a clean group stays as it is
 #pragma unroll
     for (int p = 0; p < P; ++p) {
       VisT o = v[p];
@@ -539,7 +540,7 @@ __global__ void sanitize_nan_groups(const VisT* __restrict__ src, VisT* __restri
 
 // Runtime-P variant of the NaN sanitiser for pol counts without a template instance.
 template <typename VisT>
-__global__ void sanitize_nan_groups_generic(const VisT* __restrict__ src, VisT* __restrict__ dst, int64_t groups, int P) {
+__global__ void sanitize_nan_groups_generic(const VisT* src, VisT* dst, int64_t groups, int P) {
   using S = typename VisScalar<VisT>::type;
   for (int64_t g = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x; g < groups;
        g += static_cast<int64_t>(gridDim.x) * blockDim.x) {
@@ -548,6 +549,7 @@ __global__ void sanitize_nan_groups_generic(const VisT* __restrict__ src, VisT* 
       const VisT v = src[g * P + p];
       nan |= isnan(v.x) || isnan(v.y);
     }
+    if (!nan && src == dst) continue;
     for (int p = 0; p < P; ++p) {
       VisT o = src[g * P + p];
       if (nan) { o.x = S(0); o.y = S(0); }
