@@ -78,4 +78,30 @@ __global__ void __launch_bounds__(256) ingest_ms_transpose(const VisT* __restric
   }
 }
 
+// Opt-in flagging: zero every (row, channel) group whose MeasurementSet FLAG is set
+// for any pol.  flags is MS order, [rows][row_channels][flag_pols] bytes (non-zero =
+// flagged); threads run along channels so the flag reads are contiguous, and only
+// flagged groups are written.  The reference averages flagged samples (it skips only
+// NaN, CpuLeapCalibrator.cc:201-214), so this is off unless a caller asks for it.
+template <typename VisT>
+__global__ void apply_flag_groups(VisT* __restrict__ vis, const uint8_t* __restrict__ flags, int64_t rows, int channels,
+                                  int pols, int64_t row_channels, int start_channel, int flag_pols,
+                                  unsigned long long* __restrict__ count) {
+  unsigned long long mine = 0;
+  for (int64_t i = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x; i < rows * channels;
+       i += static_cast<int64_t>(gridDim.x) * blockDim.x) {
+    const int c = static_cast<int>(i % channels);
+    const int64_t r = i / channels;
+    const uint8_t* f = flags + (r * row_channels + start_channel + c) * flag_pols;
+    bool flagged = false;
+    for (int p = 0; p < flag_pols; ++p) flagged |= f[p] != 0;
+    if (flagged) {
+      VisT* v = vis + (static_cast<int64_t>(c) * rows + r) * pols;
+      for (int p = 0; p < pols; ++p) v[p].x = v[p].y = 0;
+      ++mine;
+    }
+  }
+  if (mine) atomicAdd(count, mine);
+}
+
 }  // namespace leapgb

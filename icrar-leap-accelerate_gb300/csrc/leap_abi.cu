@@ -106,6 +106,7 @@ struct leap_ctx {
   int tc_attr_set = 0;                // bit per N tile whose shared-memory size was raised
   DeviceBuffer dphi_tc;               // packed dphi operand of the tensor-core contraction
   DeviceBuffer adj_dphi, adj_cal1, adj_phi1, adj_gavg, adj_partial;  // adjoint scratch
+  DeviceBuffer flag_count;
   // MeasurementSet-order ingestion from pageable host memory: two pinned staging
   // buffers and their device twins, each reused once its piece has been transposed.
   static constexpr size_t kStageBytes = size_t(64) << 20;
@@ -1014,6 +1015,7 @@ void leap_destroy(leap_ctx* ctx) {
     ctx->refant_reduce.release();
     ctx->adj_dphi.release(); ctx->adj_cal1.release(); ctx->adj_phi1.release(); ctx->adj_gavg.release();
     ctx->adj_partial.release();
+    ctx->flag_count.release();
     for (int b = 0; b < 2; ++b) {
       ctx->stage_dev[b].release();
       if (ctx->stage_host[b]) cudaFreeHost(ctx->stage_host[b]);
@@ -1217,6 +1219,44 @@ int32_t leap_set_integration_ms(leap_ctx* ctx, int32_t slot, int32_t vis_type, c
     }
   }
   return finish_integration(ctx, in, vis_type, rows, channels, pols);
+}
+
+int32_t leap_apply_flags(leap_ctx* ctx, int32_t slot, const uint8_t* flags, int64_t row_channels, int32_t start_channel,
+                         int32_t flag_pols, int32_t memory, int64_t* flagged_groups) {
+  if (!ctx || !flags) return fail(ctx, LEAP_ERR_INVALID_ARGUMENT, "NULL argument");
+  auto it = ctx->integ.find(slot);
+  if (it == ctx->integ.end()) return fail(ctx, LEAP_ERR_NOT_READY, "integration slot not set");
+  Integration& in = it->second;
+  if (flag_pols < 1 || start_channel < 0 || static_cast<int64_t>(start_channel) + in.channels > row_channels)
+    return fail(ctx, LEAP_ERR_INVALID_ARGUMENT, "flag array shape does not cover the integration");
+  if (memory != LEAP_MEMORY_HOST && memory != LEAP_MEMORY_DEVICE) return fail(ctx, LEAP_ERR_INVALID_ARGUMENT, "unknown memory kind");
+  DeviceGuard g(ctx->device);
+  cudaStream_t s = ctx->stream;
+  const size_t fbytes = static_cast<size_t>(in.rows) * row_channels * flag_pols;
+  const uint8_t* dflags = flags;
+  DeviceBuffer tmp;
+  if (memory == LEAP_MEMORY_HOST) {
+    LEAP_CUDA(tmp.ensure(fbytes), "alloc flags");
+    LEAP_CUDA(cudaMemcpyAsync(tmp.ptr, flags, fbytes, cudaMemcpyHostToDevice, s), "upload flags");
+    dflags = tmp.as<uint8_t>();
+  }
+  LEAP_CUDA(ctx->flag_count.ensure(sizeof(unsigned long long)), "alloc flag count");
+  LEAP_CUDA(cudaMemsetAsync(ctx->flag_count.ptr, 0, sizeof(unsigned long long), s), "clear flag count");
+  const int grid = grid_1d(in.rows * in.channels, 256);
+  if (in.vis_type == LEAP_VIS_C64)
+    apply_flag_groups<float2><<<grid, 256, 0, s>>>(in.vis.as<float2>(), dflags, in.rows, in.channels, in.pols, row_channels,
+                                                   start_channel, flag_pols, ctx->flag_count.as<unsigned long long>());
+  else
+    apply_flag_groups<double2><<<grid, 256, 0, s>>>(in.vis.as<double2>(), dflags, in.rows, in.channels, in.pols,
+                                                    row_channels, start_channel, flag_pols,
+                                                    ctx->flag_count.as<unsigned long long>());
+  LEAP_CUDA(cudaGetLastError(), "flag kernel");
+  unsigned long long n = 0;
+  LEAP_CUDA(cudaMemcpyAsync(&n, ctx->flag_count.ptr, sizeof(n), cudaMemcpyDeviceToHost, s), "read flag count");
+  LEAP_CUDA(cudaStreamSynchronize(s), "apply flags");
+  tmp.release();
+  if (flagged_groups) *flagged_groups = static_cast<int64_t>(n);
+  return LEAP_OK;
 }
 
 int32_t leap_release_integration(leap_ctx* ctx, int32_t slot) {

@@ -59,6 +59,7 @@ SIGNATURES = {
     "leap_set_metadata": ([vp, ctypes.POINTER(LeapConstants), vp, i32, i32, vp, vp, vp, i32, vp, vp], i32),
     "leap_set_integration": ([vp, i32, i32, vp, vp, i64, i32, i32, i32], i32),
     "leap_set_integration_ms": ([vp, i32, i32, vp, i64, i32, vp, i64, i32, i32, i32], i32),
+    "leap_apply_flags": ([vp, i32, vp, i64, i32, i32, i32, ctypes.POINTER(i64)], i32),
     "leap_release_integration": ([vp, i32], i32),
     "leap_calibrate": ([vp, i32, vp, i32, i32, vp], i32),
     "leap_calibrate_async": ([vp, i32, vp, i32, i32, vp, vp], i32),

@@ -262,6 +262,18 @@ class Context:
         self._check(lib.leap_set_integration_ms(self._h, slot, vt, vp, row_channels, start_channel, up, rows, C, P, mem))
         self.slots[slot] = (C, rows, P)
 
+    def apply_flags(self, slot: int, flags: np.ndarray, start_channel: int = 0) -> int:
+        """Opt-in: zero the (row, channel) groups whose FLAG (rows, row_channels[, pols], MS order)
+        is set for any pol; returns the number of groups zeroed (leap_apply_flags)."""
+        f = np.ascontiguousarray(flags, dtype=np.uint8)
+        if f.ndim == 2:
+            f = f[:, :, None]
+        rows, row_channels, fp = f.shape
+        n = ctypes.c_int64(0)
+        self._check(lib.leap_apply_flags(self._h, slot, _ptr(f), row_channels, start_channel, fp,
+                                         _abi.LEAP_MEMORY_HOST, ctypes.byref(n)))
+        return int(n.value)
+
     def release_integration(self, slot: int):
         self.autograd_slots.pop(slot, None)
         self._check(lib.leap_release_integration(self._h, slot))
@@ -361,7 +373,11 @@ class GpuLeapCalibrator:
         for s in range(solutions):
             r0 = s * interval * nbl  # start row ignores Slice.start, as CpuLeapCalibrator.cc:116 does
             nrows = interval * nbl
-            self.ctx.set_integration(0, np.ascontiguousarray(obs.vis[:, r0:r0 + nrows, :]), obs.uvw[r0:r0 + nrows])
+            ms_vis = getattr(obs, "ms_vis", None)
+            if ms_vis is not None:  # MeasurementSet order [row][channel][pol]: transposed on the device
+                self.ctx.set_integration_ms(0, ms_vis[r0:r0 + nrows], obs.uvw[r0:r0 + nrows])
+            else:
+                self.ctx.set_integration(0, np.ascontiguousarray(obs.vis[:, r0:r0 + nrows, :]), obs.uvw[r0:r0 + nrows])
             cal = self.ctx.calibrate(0, dds, self.precision)
             out.append({
                 "epoch": {"start": float(obs.epochs[s * interval]), "end": float(obs.epochs[(s + 1) * interval - 1])},

@@ -229,6 +229,36 @@ def uneven_chunks(count: int = 32, seed: int = 4, t_range=(1, 64), channel_choic
     return chunks
 
 
+def read_leapms(path: str, read_autocorrelations: bool = True) -> Observation:
+    """Read a ".leapms" file (the format write_leapms writes) as an Observation whose
+    visibilities stay in MeasurementSet order: ``obs.ms_vis`` is (rows, channels, pols)
+    and ``obs.vis`` is its (channels, rows, pols) view.  The baseline count follows the
+    reference, n(n+1)/2 with autocorrelations (LA/ms/MeasurementSet.cc:149-167)."""
+    with open(path, "rb") as f:
+        if f.read(8) != b"LEAPMS01":
+            raise ValueError(f"{path}: not a .leapms file")
+        stations, total, rows, channels, pols, is_double = (int(x) for x in np.fromfile(f, "<u4", 6))
+        f0, df, ra0, dec0 = (float(x) for x in np.fromfile(f, "<f8", 4))
+        a1 = np.fromfile(f, "<i4", rows)
+        a2 = np.fromfile(f, "<i4", rows)
+        flags = np.fromfile(f, np.uint8, rows)
+        times = np.fromfile(f, "<f8", rows)
+        uvw = np.fromfile(f, "<f8", rows * 3).reshape(rows, 3)
+        dt = np.complex128 if is_double else np.complex64
+        ms_vis = np.fromfile(f, dt, rows * channels * pols).reshape(rows, channels, pols)
+    nbl = stations * (stations + 1) // 2 if read_autocorrelations else stations * (stations - 1) // 2
+    if rows % nbl:
+        raise ValueError(f"{path}: {rows} rows is not a whole number of {nbl}-baseline timesteps")
+    T = rows // nbl
+    obs = Observation(num_stations=stations, total_antennas=total, nbaselines=nbl, timesteps=T, channels=channels,
+                      pols=pols, freq_start_hz=f0, freq_inc_hz=df, phase_centre=(ra0, dec0),
+                      antenna1=a1[:nbl].copy(), antenna2=a2[:nbl].copy(), flags=flags[:nbl].copy(), uvw=uvw,
+                      epochs=times[::nbl][:T].copy(), vis=ms_vis.transpose(1, 0, 2), gains=np.ones(stations),
+                      positions_enu=np.zeros((stations, 3)), source_lmn=np.zeros(3))
+    obs.ms_vis = ms_vis
+    return obs
+
+
 def write_leapms(obs: Observation, path: str) -> None:
     """Write an observation as a ".leapms" file for the C++ MeasurementSet stand-in:
     header, per-row ANTENNA1/ANTENNA2/FLAG/TIME/UVW, then DATA in the

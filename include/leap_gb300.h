@@ -130,6 +130,17 @@ int32_t leap_set_integration_ms(leap_ctx* ctx, int32_t slot, int32_t vis_type, c
                                 int64_t row_channels, int32_t start_channel, const double* uvw, int64_t rows,
                                 int32_t channels, int32_t pols, int32_t memory);
 
+/* Opt-in flagging (off unless called): zero every (row, channel) group of a resident
+ * integration whose MeasurementSet FLAG is set for any pol, so flagged samples add
+ * nothing to the averages.  The reference averages flagged samples and skips only
+ * NaN (LA/algorithm/cpu/CpuLeapCalibrator.cc:201-214; flags enter only the phase
+ * matrix, LA/ms/MeasurementSet.cc:181-240), so results match it only without this
+ * call.  flags is MS order, [rows][row_channels][flag_pols] bytes (non-zero =
+ * flagged), channel start_channel onwards; HOST or DEVICE memory.  The number of
+ * groups zeroed is written to *flagged_groups when it is not NULL. */
+int32_t leap_apply_flags(leap_ctx* ctx, int32_t slot, const uint8_t* flags, int64_t row_channels,
+                         int32_t start_channel, int32_t flag_pols, int32_t memory, int64_t* flagged_groups);
+
 /* Release the HBM held by one integration slot. */
 int32_t leap_release_integration(leap_ctx* ctx, int32_t slot);
 

@@ -76,3 +76,33 @@ def test_ms_order_rejects_bad_channel_range(ctx):
     ms = np.ascontiguousarray(obs.vis.transpose(1, 0, 2))
     with pytest.raises(lg.InvalidArgument):
         ctx.set_integration_ms(0, ms, obs.uvw, start_channel=2, channels=3)
+
+
+@pytest.mark.parametrize("flag_pols", [1, 4])
+def test_opt_in_flags_equal_nan_groups(ctx, flag_pols):
+    """Flagged groups are zeroed, exactly like NaN groups; no flag changes nothing (the default)."""
+    obs, dirs = synth.small_case(stations=22, timesteps=3, channels=19, directions=4, vis_dtype=np.complex64,
+                                 seed_shift=5)
+    md = lg.build_metadata(obs)
+    ctx.set_metadata(md)
+    dds = _dds(md, dirs)
+    rows, C = obs.rows, obs.channels
+    flags = np.zeros((rows, C + 2, flag_pols), dtype=np.uint8)  # MS rows hold 2 more channels than taken
+    rng = np.random.default_rng(11)
+    pick_r = rng.integers(0, rows, 40)
+    pick_c = rng.integers(0, C, 40)
+    pick_p = rng.integers(0, flag_pols, 40)
+    flags[pick_r, pick_c + 1, pick_p] = 1
+    expect_groups = len(set(zip(pick_r.tolist(), pick_c.tolist())))
+    ctx.set_integration(0, obs.vis, obs.uvw)
+    plain = ctx.calibrate(0, dds, lg.LEAP_PRECISION_FP64)
+    assert ctx.apply_flags(0, np.zeros_like(flags), start_channel=1) == 0
+    np.testing.assert_array_equal(ctx.calibrate(0, dds, lg.LEAP_PRECISION_FP64), plain)
+    assert ctx.apply_flags(0, flags, start_channel=1) == expect_groups
+    got = ctx.calibrate(0, dds, lg.LEAP_PRECISION_FP64)
+    nan_vis = obs.vis.copy()
+    nan_vis[pick_c, pick_r, 0] = np.nan
+    ctx.set_integration(1, nan_vis, obs.uvw)
+    np.testing.assert_array_equal(got, ctx.calibrate(1, dds, lg.LEAP_PRECISION_FP64))
+    assert np.abs(got - plain).max() > 0
+    ctx.release_integration(1)
