@@ -32,12 +32,25 @@ cpu::CalibrationCollection GpuLeapCalibrator::Calibrate(const MeasurementSet& ms
   const int timesteps = static_cast<int>(ms.GetNumTimesteps());
   const Range interval = solutionInterval.Evaluate(timesteps);
   const std::vector<double> epochs = ms.GetEpochs();
-  const cpu::MetaData metadata(ms, referenceAntenna, minimumBaselineThreshold, isFileSystemCacheEnabled);
+  const bool onDevice = m_options.deviceMetadata && !isFileSystemCacheEnabled;
+  const cpu::MetaData metadata =
+      onDevice ? cpu::MetaData(ms, referenceAntenna, minimumBaselineThreshold, cpu::MetaData::ConstantsOnly{})
+               : cpu::MetaData(ms, referenceAntenna, minimumBaselineThreshold, isFileSystemCacheEnabled);
   const leap_constants k = metadata.GetConstants().ToAbi();
-  check(leap_set_metadata(m_ctx, &k, metadata.GetA().data(), metadata.GetARows(), metadata.GetStations(),
-                          metadata.GetI().data(), metadata.GetAd().data(), metadata.GetA1().data(),
-                          metadata.GetA1Rows(), metadata.GetI1().data(), metadata.GetAd1().data()),
-        m_ctx, "leap_set_metadata");
+  int32_t S = 0;
+  if (onDevice) {
+    int32_t hostPath = 0;
+    check(leap_build_metadata(m_ctx, &k, metadata.GetAntenna1().data(), metadata.GetAntenna2().data(),
+                              metadata.GetBaselineFlags().data(), static_cast<int32_t>(k.nbaselines), &hostPath),
+          m_ctx, "leap_build_metadata");
+    check(leap_get_metadata_matrix(m_ctx, 0, nullptr, 0, &S, nullptr), m_ctx, "leap_get_metadata_matrix");
+  } else {
+    check(leap_set_metadata(m_ctx, &k, metadata.GetA().data(), metadata.GetARows(), metadata.GetStations(),
+                            metadata.GetI().data(), metadata.GetAd().data(), metadata.GetA1().data(),
+                            metadata.GetA1Rows(), metadata.GetI1().data(), metadata.GetAd1().data()),
+          m_ctx, "leap_set_metadata");
+    S = metadata.GetStations();
+  }
 
   std::vector<double> dd(9 * directions.size());
   for (size_t i = 0; i < directions.size(); ++i) {
@@ -46,7 +59,6 @@ cpu::CalibrationCollection GpuLeapCalibrator::Calibrate(const MeasurementSet& ms
   }
   const uint32_t nbl = ms.GetNumBaselines();
   const uint32_t C = ms.GetNumChannels(), P = ms.GetNumPols();
-  const int32_t S = metadata.GetStations();
   std::vector<cpu::Calibration> output;
   const int solutions = interval.GetSize();
   for (int s = 0; s < solutions; ++s) {

@@ -14,6 +14,9 @@ namespace gb300 {
 struct GpuOptions {
   int device = 0;
   int precision = LEAP_PRECISION_FP64;  // LEAP_PRECISION_FP64 (reference-faithful) or LEAP_PRECISION_MIXED
+  // Build A, A1 and their pseudo-inverses on the device (leap_build_metadata) unless the
+  // file cache is requested, which keeps the host path and its A.hash / Ad.cache files.
+  bool deviceMetadata = true;
 };
 
 class GpuLeapCalibrator : public ILeapCalibrator {

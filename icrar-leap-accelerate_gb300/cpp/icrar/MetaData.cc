@@ -76,8 +76,8 @@ uint64_t matrix_hash(const std::vector<double>& A, int32_t rows, int32_t cols) {
 
 }  // namespace
 
-MetaData::MetaData(const MeasurementSet& ms, std::optional<unsigned int> refAnt, double minimumBaselineThreshold,
-                   bool useCache) {
+void MetaData::SetConstants(const MeasurementSet& ms, std::optional<unsigned int> refAnt,
+                            double minimumBaselineThreshold) {
   m_constants.nbaselines = ms.GetNumBaselines();
   m_constants.referenceAntenna = refAnt ? *refAnt : ms.GetTotalAntennas() - 1;
   m_constants.channels = ms.GetNumChannels();
@@ -90,9 +90,22 @@ MetaData::MetaData(const MeasurementSet& ms, std::optional<unsigned int> refAnt,
   m_constants.phase_centre_dec_rad = ms.GetPhaseCentreDec();
 
   const auto filtered = ms.GetFilteredBaselines(minimumBaselineThreshold);
-  std::vector<uint8_t> fg(filtered.begin(), filtered.end());
-  const auto a1 = ms.GetAntenna1();
-  const auto a2 = ms.GetAntenna2();
+  m_fg.assign(filtered.begin(), filtered.end());
+  m_a1 = ms.GetAntenna1();
+  m_a2 = ms.GetAntenna2();
+}
+
+MetaData::MetaData(const MeasurementSet& ms, std::optional<unsigned int> refAnt, double minimumBaselineThreshold,
+                   ConstantsOnly) {
+  SetConstants(ms, refAnt, minimumBaselineThreshold);
+}
+
+MetaData::MetaData(const MeasurementSet& ms, std::optional<unsigned int> refAnt, double minimumBaselineThreshold,
+                   bool useCache) {
+  SetConstants(ms, refAnt, minimumBaselineThreshold);
+  const auto& fg = m_fg;
+  const auto& a1 = m_a1;
+  const auto& a2 = m_a2;
   int32_t cols1 = 0, cols = 0;
   phase_matrix(a1, a2, fg, m_constants.referenceAntenna, m_A1, m_I1, m_A1rows, cols1);
   phase_matrix(a1, a2, fg, std::nullopt, m_A, m_I, m_Arows, cols);

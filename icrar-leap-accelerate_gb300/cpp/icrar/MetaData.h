@@ -39,6 +39,16 @@ class MetaData {
   // (ProcessCache, LA/common/eigen_extensions.h:164-199).
   MetaData(const MeasurementSet& ms, std::optional<unsigned int> refAnt, double minimumBaselineThreshold, bool useCache);
 
+  // Constants and the first-epoch baseline columns only (antenna1, antenna2 and the
+  // filtered-baseline flags); the matrices are then built on the device
+  // (leap_build_metadata).
+  struct ConstantsOnly {};
+  MetaData(const MeasurementSet& ms, std::optional<unsigned int> refAnt, double minimumBaselineThreshold,
+           ConstantsOnly);
+  const std::vector<int32_t>& GetAntenna1() const { return m_a1; }
+  const std::vector<int32_t>& GetAntenna2() const { return m_a2; }
+  const std::vector<uint8_t>& GetBaselineFlags() const { return m_fg; }
+
   const Constants& GetConstants() const { return m_constants; }
   int32_t GetARows() const { return m_Arows; }
   int32_t GetA1Rows() const { return m_A1rows; }
@@ -60,6 +70,9 @@ class MetaData {
   int32_t m_S = 0, m_Arows = 0, m_A1rows = 0;
   std::vector<double> m_A, m_Ad, m_A1, m_Ad1;
   std::vector<int32_t> m_I, m_I1;
+  std::vector<int32_t> m_a1, m_a2;
+  std::vector<uint8_t> m_fg;
+  void SetConstants(const MeasurementSet& ms, std::optional<unsigned int> refAnt, double minimumBaselineThreshold);
 };
 
 }  // namespace cpu

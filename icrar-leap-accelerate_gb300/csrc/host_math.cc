@@ -30,9 +30,11 @@ void dd_matrix(double phase_ra, double phase_dec, double ra, double dec, double*
     for (int j = 0; j < 3; ++j) dd[3 * i + j] = t[3 * i] * r1[j] + t[3 * i + 1] * r1[3 + j] + t[3 * i + 2] * r1[6 + j];
 }
 
-// PhaseMatrixFunction (LA/algorithm/cpu/PhaseMatrixFunction.cc:35-93).
-int phase_matrix(const int32_t* a1, const int32_t* a2, const uint8_t* fg, int32_t n, int32_t ref_ant,
-                 std::vector<double>& A, std::vector<int32_t>& I, int32_t& rows, int32_t& cols, std::string& err) {
+// PhaseMatrixFunction (LA/algorithm/cpu/PhaseMatrixFunction.cc:35-93): the checks, the
+// number of antenna columns and the baselines kept (first-epoch cross baselines, not
+// flagged, containing ref_ant when one is given), in baseline order.
+static int phase_matrix_rows(const int32_t* a1, const int32_t* a2, const uint8_t* fg, int32_t n, int32_t ref_ant,
+                             std::vector<int32_t>& keep, int32_t& cols, std::string& err) {
   if (ref_ant >= 0 && ref_ant >= n) {
     err = "refAnt " + std::to_string(ref_ant) + " is out of bounds";
     return LEAP_ERR_INVALID_ARGUMENT;
@@ -54,13 +56,21 @@ int phase_matrix(const int32_t* a1, const int32_t* a2, const uint8_t* fg, int32_
     maxc = std::max(maxc, std::max(a1[i], a2[i]));
   }
   cols = maxc + 1;
-  std::vector<int32_t> keep;
+  keep.clear();
   keep.reserve(n);
   for (int32_t i = 0; i < n; ++i) {
     if (a1[i] == a2[i] || fg[i]) continue;
     if (ref_ant >= 0 && a1[i] != ref_ant && a2[i] != ref_ant) continue;
     keep.push_back(i);
   }
+  return LEAP_OK;
+}
+
+int phase_matrix(const int32_t* a1, const int32_t* a2, const uint8_t* fg, int32_t n, int32_t ref_ant,
+                 std::vector<double>& A, std::vector<int32_t>& I, int32_t& rows, int32_t& cols, std::string& err) {
+  std::vector<int32_t> keep;
+  const int rc = phase_matrix_rows(a1, a2, fg, n, ref_ant, keep, cols, err);
+  if (rc != LEAP_OK) return rc;
   rows = static_cast<int32_t>(keep.size()) + 1;
   A.assign(static_cast<size_t>(rows) * cols, 0.0);
   I.assign(keep.begin(), keep.end());
@@ -69,6 +79,23 @@ int phase_matrix(const int32_t* a1, const int32_t* a2, const uint8_t* fg, int32_
     A[k + static_cast<size_t>(rows) * a2[keep[k]]] = -1.0;
   }
   A[(rows - 1) + static_cast<size_t>(rows) * (ref_ant < 0 ? 0 : ref_ant)] = 1.0;
+  return LEAP_OK;
+}
+
+int phase_matrix_sparse(const int32_t* a1, const int32_t* a2, const uint8_t* fg, int32_t n, int32_t ref_ant,
+                        std::vector<SparseRow>& A, std::vector<int32_t>& I, int32_t& cols, std::string& err) {
+  std::vector<int32_t> keep;
+  const int rc = phase_matrix_rows(a1, a2, fg, n, ref_ant, keep, cols, err);
+  if (rc != LEAP_OK) return rc;
+  A.resize(keep.size() + 1);
+  I.assign(keep.begin(), keep.end());
+  for (size_t k = 0; k < keep.size(); ++k) {
+    // column order, as the dense row of A lists its non-zeros
+    const int32_t p = a1[keep[k]], q = a2[keep[k]];
+    A[k] = p < q ? SparseRow{p, q, 1.0, -1.0} : SparseRow{q, p, -1.0, 1.0};
+  }
+  const int32_t r = ref_ant < 0 ? 0 : ref_ant;
+  A[keep.size()] = SparseRow{r, r, 1.0, 0.0};
   return LEAP_OK;
 }
 

@@ -15,6 +15,17 @@ void dd_matrix(double phase_ra, double phase_dec, double ra, double dec, double*
 int phase_matrix(const int32_t* a1, const int32_t* a2, const uint8_t* fg, int32_t n, int32_t ref_ant,
                  std::vector<double>& A, std::vector<int32_t>& I, int32_t& rows, int32_t& cols, std::string& err);
 
+// One row of a phase matrix: the non-zeros (c0, v0), (c1, v1) in column order; a row with a
+// single non-zero has c1 == c0 and v1 == 0.
+struct SparseRow {
+  int32_t c0, c1;
+  double v0, v1;
+};
+
+// PhaseMatrixFunction in sparse row form (no dense rows x cols array).
+int phase_matrix_sparse(const int32_t* a1, const int32_t* a2, const uint8_t* fg, int32_t n, int32_t ref_ant,
+                        std::vector<SparseRow>& A, std::vector<int32_t>& I, int32_t& cols, std::string& err);
+
 // SVDPseudoInverse (LA/math/cpu/matrix_invert.h:49-56): A (m x n, column-major) -> Ad (n x m, column-major).
 int pseudo_inverse(const double* A, int32_t m, int32_t n, double* Ad, std::string& err);
 

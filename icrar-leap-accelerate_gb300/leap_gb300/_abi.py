@@ -58,6 +58,8 @@ SIGNATURES = {
     "leap_last_error": ([vp], ctypes.c_char_p),
     "leap_set_metadata": ([vp, ctypes.POINTER(LeapConstants), vp, i32, i32, vp, vp, vp, i32, vp, vp], i32),
     "leap_set_integration": ([vp, i32, i32, vp, vp, i64, i32, i32, i32], i32),
+    "leap_build_metadata": ([vp, ctypes.POINTER(LeapConstants), vp, vp, vp, i32, ctypes.POINTER(i32)], i32),
+    "leap_get_metadata_matrix": ([vp, i32, vp, i64, ctypes.POINTER(i32), ctypes.POINTER(i32)], i32),
     "leap_set_integration_ms": ([vp, i32, i32, vp, i64, i32, vp, i64, i32, i32, i32], i32),
     "leap_apply_flags": ([vp, i32, vp, i64, i32, i32, i32, ctypes.POINTER(i64)], i32),
     "leap_release_integration": ([vp, i32], i32),

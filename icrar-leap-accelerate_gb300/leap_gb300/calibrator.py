@@ -213,6 +213,41 @@ class Context:
                                           _ptr(Ad), _ptr(A1), A1.shape[0], _ptr(I1), _ptr(Ad1)))
         self.md = md
 
+    def build_metadata(self, obs, reference_antenna: Optional[int] = None, minimum_baseline_threshold: float = 0.0,
+                       fetch: bool = True) -> MetaData:
+        """MetaData built on the device (leap_build_metadata) from the observation's first-epoch
+        baselines; installs it on this context.  With fetch, Ad / Ad1 are copied back and A / I /
+        A1 / I1 rebuilt on the host, so the returned MetaData is complete.  The host-path bits
+        (1: A, 2: A1) are in ``md.host_path``."""
+        ref = reference_antenna if reference_antenna is not None else obs.total_antennas - 1
+        fg = np.ascontiguousarray(filtered_baselines(obs, minimum_baseline_threshold), dtype=np.uint8)
+        nbl = obs.nbaselines
+        a1 = np.ascontiguousarray(obs.antenna1[:nbl], dtype=np.int32)
+        a2 = np.ascontiguousarray(obs.antenna2[:nbl], dtype=np.int32)
+        k = _abi.LeapConstants(nbl, ref, obs.channels, obs.pols, obs.num_stations, obs.rows, obs.freq_start_hz,
+                               obs.freq_inc_hz, obs.phase_centre[0], obs.phase_centre[1], 0.0, 0.0)
+        host = ctypes.c_int32(0)
+        self._check(lib.leap_build_metadata(self._h, ctypes.byref(k), _ptr(a1), _ptr(a2), _ptr(fg), nbl,
+                                            ctypes.byref(host)))
+        if fetch:
+            A1, I1 = phase_matrix(a1, a2, fg, ref)
+            A, I = phase_matrix(a1, a2, fg, None)
+            mats = []
+            for which in (0, 1):
+                r, c = ctypes.c_int32(0), ctypes.c_int32(0)
+                self._check(lib.leap_get_metadata_matrix(self._h, which, None, 0, ctypes.byref(r), ctypes.byref(c)))
+                out = np.zeros((c.value, r.value), dtype=np.float64)  # column-major S x cols
+                self._check(lib.leap_get_metadata_matrix(self._h, which, _ptr(out), out.size, None, None))
+                mats.append(out.T.copy())
+            md = MetaData(nbl, ref, obs.channels, obs.pols, obs.num_stations, obs.rows, obs.freq_start_hz,
+                          obs.freq_inc_hz, obs.phase_centre[0], obs.phase_centre[1], A, I, mats[0], A1, I1, mats[1])
+        else:
+            md = None
+        self.md = md
+        if md is not None:
+            md.host_path = int(host.value)
+        return md
+
     def set_integration(self, slot: int, vis, uvw):
         """vis: (channels, rows, pols) complex64/complex128 numpy array or CUDA torch tensor
         (a torch complex tensor or its real view); uvw: (rows, 3) float64."""

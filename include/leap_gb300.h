@@ -108,6 +108,25 @@ int32_t leap_set_metadata(leap_ctx* ctx, const leap_constants* constants, const 
                           int32_t A_cols, const int32_t* I, const double* Ad, const double* A1,
                           int32_t A1_rows, const int32_t* I1, const double* Ad1);
 
+/* MetaData build on the device: from the first-epoch antenna columns a1/a2 and
+ * the baseline flags fg (flagged or shorter than the minimum baseline, as
+ * MeasurementSet::GetFilteredBaselines gives them, LA/ms/MeasurementSet.cc:181-240),
+ * build A / I (no reference antenna) and A1 / I1 (constants->referenceAntenna) as
+ * PhaseMatrixFunction does (LA/algorithm/cpu/PhaseMatrixFunction.cc:35-93), their
+ * pseudo-inverses on the GPU, and install everything as leap_set_metadata would
+ * (replaces the host MetaData construction, LA/model/cpu/MetaData.cc:84-136).
+ * The pseudo-inverse is G^-1 A^T with G = A^T A inverted in FP64 and refined with
+ * double-double residuals; when G is singular or too ill-conditioned for the
+ * reference's truncation rule to leave it whole, the host SVD-style path runs
+ * instead and bit 0 (A) / bit 1 (A1) of *used_host_path is set. */
+int32_t leap_build_metadata(leap_ctx* ctx, const leap_constants* constants, const int32_t* a1, const int32_t* a2,
+                            const uint8_t* fg, int32_t nbl, int32_t* used_host_path);
+
+/* Copy Ad (which 0, S x Arows) or Ad1 (which 1, S x A1rows), column-major, to host
+ * memory (e.g. for the reference's Ad file cache); out NULL only reports the shape. */
+int32_t leap_get_metadata_matrix(leap_ctx* ctx, int32_t which, double* out, int64_t capacity, int32_t* rows_out,
+                                 int32_t* cols_out);
+
 /* Make an integration resident in HBM under `slot` (any int >= 0; a later
  * call with the same slot replaces it).  Replaces HostIntegration +
  * DeviceIntegration::Set and SolutionIntervalBuffer::SetUVW
