@@ -1580,6 +1580,16 @@ int32_t leap_backward(leap_ctx* ctx, int32_t slot, const double* d_dd, int32_t n
   return LEAP_OK;
 }
 
+int32_t leap_selftest_bounded_wait(leap_ctx* ctx, int32_t polls) {
+  if (!ctx) return fail(ctx, LEAP_ERR_INVALID_ARGUMENT, "NULL context");
+  if (polls < 1 || polls > (1 << 20)) return fail(ctx, LEAP_ERR_INVALID_ARGUMENT, "polls must be in [1, 2^20]");
+  DeviceGuard g(ctx->device);
+  selftest_bounded_wait<<<1, 32, 0, ctx->stream>>>(static_cast<uint32_t>(polls), ctx->dev_err.as<int>());
+  LEAP_CUDA(cudaGetLastError(), "self-test launch");
+  LEAP_CUDA(cudaStreamSynchronize(ctx->stream), "self-test");
+  return check_device_error(ctx);
+}
+
 int32_t leap_set_option(leap_ctx* ctx, int32_t option, int32_t value) {
   if (!ctx) return fail(ctx, LEAP_ERR_INVALID_ARGUMENT, "NULL context");
   switch (option) {

@@ -55,11 +55,24 @@ __device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, uint32_t parity) {
 }
 
 // Bounded wait on one phase of an mbarrier.  Returns false if it gave up.
-__device__ __forceinline__ bool mbar_wait_bounded(uint64_t* bar, uint32_t parity) {
-  for (uint32_t i = 0; i < kMaxWaitPolls; ++i) {
+__device__ __forceinline__ bool mbar_wait_bounded(uint64_t* bar, uint32_t parity, uint32_t max_polls = kMaxWaitPolls) {
+  for (uint32_t i = 0; i < max_polls; ++i) {
     if (mbar_try_wait(bar, parity)) return true;
   }
   return false;
+}
+
+// Self-test of the timeout path: an mbarrier phase that nothing completes,
+// waited for with a bound of `polls`; the kernel records the timeout in the
+// error word exactly as the production kernels do, and returns.
+static __global__ void selftest_bounded_wait(uint32_t polls, int* err) {
+  __shared__ uint64_t bar;
+  if (threadIdx.x == 0) {
+    mbar_init(&bar, 1);
+    fence_mbar_init();
+  }
+  __syncthreads();
+  if (threadIdx.x == 0 && !mbar_wait_bounded(&bar, 0, polls)) atomicOr(err, kDevErrTimeout);
 }
 
 // Two-dimensional tiled TMA load global -> shared through a tensor map,

@@ -68,6 +68,7 @@ SIGNATURES = {
     "leap_calibrate_batched": ([vp, vp, i32, vp, i32, i32, vp], i32),
     "leap_set_autotune": ([vp, i32], i32),
     "leap_set_option": ([vp, i32, i32], i32),
+    "leap_selftest_bounded_wait": ([vp, i32], i32),
     "leap_get_avgdata_device": ([vp, i32, vp, vp], i32),
     "leap_backward": ([vp, i32, vp, i32, vp, vp, vp, vp, vp, vp], i32),
     "leap_get_avgdata": ([vp, i32, vp], i32),

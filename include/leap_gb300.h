@@ -190,6 +190,12 @@ int32_t leap_calibrate_async(leap_ctx* ctx, int32_t slot, const double* d_dd, in
 int32_t leap_calibrate_batched(leap_ctx* ctx, const leap_work_item* items, int32_t nitems, const double* dd,
                                int32_t ndirections, int32_t precision, double* cal_out);
 
+/* Failure-detection self-test (no counterpart in the reference): runs one kernel
+ * whose mbarrier wait nothing completes, bounded to `polls` polls (1 .. 2^20),
+ * through the same timeout path as the production kernels.  Returns
+ * LEAP_ERR_DEVICE_TIMEOUT when that path works; the context stays usable. */
+int32_t leap_selftest_bounded_wait(leap_ctx* ctx, int32_t polls);
+
 /* Enable (default) or disable tuning of new batched shapes on first use. */
 int32_t leap_set_autotune(leap_ctx* ctx, int32_t enable);
 

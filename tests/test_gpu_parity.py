@@ -201,3 +201,13 @@ def test_mixed_reference_antenna_rows_are_near_fp64(ctx, dtype):
         got = ctx.avgdata(d)[mdo.I1, 0]
         err = np.abs(got - avg_o[d][mdo.I1, 0]) / scale[mdo.I1]
         assert err.max() < 1e-9, (d, err.max())
+
+
+def test_bounded_wait_timeout_is_reported_and_context_survives(ctx):
+    """Failure detection without a fault: a wait that nothing completes gives up after a
+    bounded number of polls, the host reads LEAP_ERR_DEVICE_TIMEOUT, and the next call works."""
+    from leap_gb300 import _abi
+    assert _abi.lib.leap_selftest_bounded_wait(ctx.handle, 1000) == _abi.LEAP_ERR_DEVICE_TIMEOUT
+    obs, dirs = synth.small_case(stations=8, timesteps=1, channels=4, directions=2)
+    md, mdo, dds, cal, cal_o, avg_o = run_case(ctx, obs, dirs, lg.LEAP_PRECISION_FP64)
+    assert np.abs(cal - cal_o).max() <= FP64_CAL_TOL
