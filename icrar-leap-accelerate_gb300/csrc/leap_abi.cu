@@ -65,6 +65,10 @@ struct Integration {
   int32_t channels = 0, pols = 0;
   bool has_map = false;
   CUtensorMap map16, map8;  // [channel][row*8 floats] views of a 4-pol complex<float> integration, box heights 16 / 8
+  // Asynchronous ingestion: the upload runs on the context's copy stream and `ready`
+  // marks its end; calibrate calls make their stream wait for it.
+  cudaEvent_t ready = nullptr;
+  bool pending = false;
 };
 
 // cuTensorMapEncodeTiled through the runtime's driver entry point (no libcuda link).
@@ -132,6 +136,8 @@ struct leap_ctx {
   DeviceBuffer partial, avg, cal1, dphi, gemm_partial, dd, cal, dev_err, lambda, twiddle, twiddle_df, partial_i1, avg_i1,
       dirk;
   cudaStream_t aux = nullptr;           // second stream for the FP64 reference-antenna pass
+  cudaStream_t copy = nullptr;          // asynchronous ingestion
+  cudaEvent_t copy_fence = nullptr;     // orders an asynchronous upload after earlier calls
   cudaEvent_t fork = nullptr, join = nullptr;
   int last_ndir = 0, last_pols = 0, last_nbl = 0;
   std::vector<double> lambda_host;
@@ -680,6 +686,22 @@ int solve_stage(leap_ctx* ctx, int32_t D, int32_t precision, int P, bool refant,
 }
 
 // The whole calibration of a list of work items with D directions in total.
+// Make stream s wait for the asynchronous uploads of the items' slots.
+void wait_for_uploads(leap_ctx* ctx, const std::vector<WorkItem>& items, cudaStream_t s) {
+  for (const auto& w : items) {
+    auto it = ctx->integ.find(w.slot);
+    if (it != ctx->integ.end() && it->second.pending) cudaStreamWaitEvent(s, it->second.ready, 0);
+  }
+}
+
+// Before a slot is rewritten or freed: its asynchronous upload must be over.
+void finish_upload(Integration& in) {
+  if (in.pending) {
+    cudaEventSynchronize(in.ready);
+    in.pending = false;
+  }
+}
+
 int calibrate_items(leap_ctx* ctx, const std::vector<WorkItem>& items, const double* d_dd, int32_t D, int32_t precision,
                     double* d_cal, cudaStream_t s) {
   if (!ctx->md.set) return fail(ctx, LEAP_ERR_NOT_READY, "metadata not set");
@@ -709,6 +731,7 @@ int calibrate_items(leap_ctx* ctx, const std::vector<WorkItem>& items, const dou
   LEAP_CUDA(ctx->gemm_partial.ensure(sizeof(double) * static_cast<size_t>(nk) * D * md.S), "alloc gemm partial");
 
   int kernels = 0;
+  if (!ctx->capturing) wait_for_uploads(ctx, items, s);
   cudaEvent_t* ev = ctx->ring[ctx->ring_count % leap_ctx::kRing];
   if (!ctx->capturing) cudaEventRecord(ev[0], s);
   const bool refant = precision == LEAP_PRECISION_MIXED && md.A1rows > 1;
@@ -799,6 +822,7 @@ int calibrate_batched_impl(leap_ctx* ctx, const leap_work_item* witems, int32_t 
   const std::string key = batch_key(ctx, items, D, precision);
   cudaStream_t s = ctx->stream;
   if (ctx->graph_exec && ctx->graph_key == key && ctx->graph_epoch == g_alloc_epoch) {
+    wait_for_uploads(ctx, items, s);
     cudaEvent_t* ev = ctx->ring[ctx->ring_count % leap_ctx::kRing];
     cudaEventRecord(ev[0], s);
     cudaEventRecord(ev[1], s);
@@ -903,10 +927,11 @@ int finish_integration(leap_ctx* ctx, Integration& in, int32_t vis_type, int64_t
 
 template <typename VisT>
 int launch_ingest(leap_ctx* ctx, const void* src, int64_t row_channels, int32_t start_channel, int64_t nrows,
-                  int32_t channels, int32_t pols, void* dst, int64_t rows_total, int64_t row0, cudaStream_t s) {
+                  int32_t channels, int32_t pols, void* dst, int64_t rows_total, int64_t row0, cudaStream_t s,
+                  int max_blocks) {
   const int TC = IngestTile<VisT>::TC;
   const int64_t tiles = ((nrows + 31) / 32) * ((channels + TC - 1) / TC);
-  const int grid = static_cast<int>(std::max<int64_t>(1, std::min<int64_t>(tiles, static_cast<int64_t>(ctx->sms) * 8)));
+  const int grid = static_cast<int>(std::max<int64_t>(1, std::min<int64_t>(tiles, max_blocks)));
   const VisT* sp = static_cast<const VisT*>(src);
   VisT* dp = static_cast<VisT*>(dst);
   switch (pols) {
@@ -918,11 +943,17 @@ int launch_ingest(leap_ctx* ctx, const void* src, int64_t row_channels, int32_t 
   return LEAP_OK;
 }
 
+// max_blocks: the synchronous path fills the GPU (8 blocks per SM); the asynchronous one
+// keeps to one block per SM so that a calibration kernel running beside it stays resident.
 int ingest(leap_ctx* ctx, int32_t vis_type, const void* src, int64_t row_channels, int32_t start_channel, int64_t nrows,
-           int32_t channels, int32_t pols, void* dst, int64_t rows_total, int64_t row0, cudaStream_t s) {
+           int32_t channels, int32_t pols, void* dst, int64_t rows_total, int64_t row0, cudaStream_t s,
+           int max_blocks = 0) {
+  if (max_blocks <= 0) max_blocks = ctx->sms * 8;
   return vis_type == LEAP_VIS_C64
-             ? launch_ingest<float2>(ctx, src, row_channels, start_channel, nrows, channels, pols, dst, rows_total, row0, s)
-             : launch_ingest<double2>(ctx, src, row_channels, start_channel, nrows, channels, pols, dst, rows_total, row0, s);
+             ? launch_ingest<float2>(ctx, src, row_channels, start_channel, nrows, channels, pols, dst, rows_total, row0,
+                                     s, max_blocks)
+             : launch_ingest<double2>(ctx, src, row_channels, start_channel, nrows, channels, pols, dst, rows_total,
+                                      row0, s, max_blocks);
 }
 
 // Install a metadata set: constants, sparse rows of A, I1, and Ad / Ad1 from host
@@ -1123,6 +1154,13 @@ int32_t leap_create(int32_t device, leap_ctx** out) {
     LEAP_CUDA(cudaDeviceGetAttribute(&ctx->sms, cudaDevAttrMultiProcessorCount, device), "query SM count");
     LEAP_CUDA(cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking), "create stream");
     LEAP_CUDA(cudaStreamCreateWithFlags(&ctx->aux, cudaStreamNonBlocking), "create aux stream");
+    {
+      // Uploads queue behind calibration work: the copy stream has the lowest priority.
+      int least = 0, greatest = 0;
+      LEAP_CUDA(cudaDeviceGetStreamPriorityRange(&least, &greatest), "stream priorities");
+      LEAP_CUDA(cudaStreamCreateWithPriority(&ctx->copy, cudaStreamNonBlocking, least), "create copy stream");
+    }
+    LEAP_CUDA(cudaEventCreateWithFlags(&ctx->copy_fence, cudaEventDisableTiming), "create event");
     LEAP_CUDA(cudaEventCreateWithFlags(&ctx->fork, cudaEventDisableTiming), "create event");
     LEAP_CUDA(cudaEventCreateWithFlags(&ctx->join, cudaEventDisableTiming), "create event");
     for (auto& tri : ctx->ring)
@@ -1185,6 +1223,13 @@ void leap_destroy(leap_ctx* ctx) {
         if (ev) cudaEventDestroy(ev);
     if (ctx->stream) cudaStreamDestroy(ctx->stream);
     if (ctx->aux) cudaStreamDestroy(ctx->aux);
+    if (ctx->copy) {
+      cudaStreamSynchronize(ctx->copy);
+      cudaStreamDestroy(ctx->copy);
+    }
+    if (ctx->copy_fence) cudaEventDestroy(ctx->copy_fence);
+    for (auto& kv : ctx->integ)
+      if (kv.second.ready) cudaEventDestroy(kv.second.ready);
     if (ctx->graph_exec) cudaGraphExecDestroy(ctx->graph_exec);
     if (ctx->fork) cudaEventDestroy(ctx->fork);
     if (ctx->join) cudaEventDestroy(ctx->join);
@@ -1311,6 +1356,7 @@ int32_t leap_set_integration(leap_ctx* ctx, int32_t slot, int32_t vis_type, cons
   if (memory != LEAP_MEMORY_HOST && memory != LEAP_MEMORY_DEVICE) return fail(ctx, LEAP_ERR_INVALID_ARGUMENT, "unknown memory kind");
   DeviceGuard g(ctx->device);
   Integration& in = ctx->integ[slot];
+  finish_upload(in);
   const size_t esz = vis_type == LEAP_VIS_C64 ? sizeof(float2) : sizeof(double2);
   const int64_t groups = rows * channels;
   const size_t vbytes = esz * static_cast<size_t>(groups) * pols;
@@ -1346,6 +1392,7 @@ int32_t leap_set_integration_ms(leap_ctx* ctx, int32_t slot, int32_t vis_type, c
   if (memory != LEAP_MEMORY_HOST && memory != LEAP_MEMORY_DEVICE) return fail(ctx, LEAP_ERR_INVALID_ARGUMENT, "unknown memory kind");
   DeviceGuard g(ctx->device);
   Integration& in = ctx->integ[slot];
+  finish_upload(in);
   const size_t esz = vis_type == LEAP_VIS_C64 ? sizeof(float2) : sizeof(double2);
   LEAP_CUDA(in.vis.ensure(esz * static_cast<size_t>(rows) * channels * pols), "alloc vis");
   LEAP_CUDA(in.uvw.ensure(sizeof(double) * 3 * rows), "alloc uvw");
@@ -1400,12 +1447,83 @@ int32_t leap_set_integration_ms(leap_ctx* ctx, int32_t slot, int32_t vis_type, c
   return finish_integration(ctx, in, vis_type, rows, channels, pols);
 }
 
+int32_t leap_set_integration_ms_async(leap_ctx* ctx, int32_t slot, int32_t vis_type, const void* ms_data,
+                                      int64_t row_channels, int32_t start_channel, const double* uvw, int64_t rows,
+                                      int32_t channels, int32_t pols, int32_t memory) {
+  if (!ctx || !ms_data || !uvw) return fail(ctx, LEAP_ERR_INVALID_ARGUMENT, "NULL argument");
+  if (slot < 0) return fail(ctx, LEAP_ERR_INVALID_ARGUMENT, "slot must be >= 0");
+  if (vis_type != LEAP_VIS_C64 && vis_type != LEAP_VIS_C128) return fail(ctx, LEAP_ERR_INVALID_ARGUMENT, "unknown vis type");
+  if (rows <= 0 || channels <= 0 || pols <= 0) return fail(ctx, LEAP_ERR_INVALID_ARGUMENT, "empty integration");
+  if (pols != 1 && pols != 2 && pols != 4) return fail(ctx, LEAP_ERR_INVALID_ARGUMENT, "pols must be 1, 2 or 4");
+  if (start_channel < 0 || static_cast<int64_t>(start_channel) + channels > row_channels)
+    return fail(ctx, LEAP_ERR_INVALID_ARGUMENT, "channel range outside the MeasurementSet row");
+  if (memory != LEAP_MEMORY_HOST && memory != LEAP_MEMORY_DEVICE) return fail(ctx, LEAP_ERR_INVALID_ARGUMENT, "unknown memory kind");
+  DeviceGuard g(ctx->device);
+  // The kernel reads the source directly: device memory or page-locked host memory only.
+  const void* direct = memory == LEAP_MEMORY_DEVICE ? ms_data : nullptr;
+  bool uvw_pinned = memory == LEAP_MEMORY_DEVICE;
+  if (memory == LEAP_MEMORY_HOST) {
+    cudaPointerAttributes at{};
+    if (cudaPointerGetAttributes(&at, ms_data) == cudaSuccess && at.type == cudaMemoryTypeHost && at.devicePointer)
+      direct = at.devicePointer;
+    cudaGetLastError();
+    cudaPointerAttributes au{};
+    uvw_pinned = cudaPointerGetAttributes(&au, uvw) == cudaSuccess && au.type == cudaMemoryTypeHost;
+    cudaGetLastError();
+  }
+  if (!direct || !uvw_pinned)
+    return fail(ctx, LEAP_ERR_INVALID_ARGUMENT, "asynchronous ingestion needs device or page-locked host memory");
+  Integration& in = ctx->integ[slot];
+  finish_upload(in);
+  const size_t esz = vis_type == LEAP_VIS_C64 ? sizeof(float2) : sizeof(double2);
+  LEAP_CUDA(in.vis.ensure(esz * static_cast<size_t>(rows) * channels * pols), "alloc vis");
+  LEAP_CUDA(in.uvw.ensure(sizeof(double) * 3 * rows), "alloc uvw");
+  LEAP_CUDA(in.uvw_f.ensure(sizeof(float) * 6 * rows), "alloc split uvw");
+  if (!in.ready) LEAP_CUDA(cudaEventCreateWithFlags(&in.ready, cudaEventDisableTiming), "create event");
+  cudaStream_t c = ctx->copy;
+  // After every earlier call on the context's stream (which may still read this slot).
+  LEAP_CUDA(cudaEventRecord(ctx->copy_fence, ctx->stream), "fence");
+  LEAP_CUDA(cudaStreamWaitEvent(c, ctx->copy_fence, 0), "fence");
+  LEAP_CUDA(cudaMemcpyAsync(in.uvw.ptr, uvw, sizeof(double) * 3 * rows,
+                            memory == LEAP_MEMORY_HOST ? cudaMemcpyHostToDevice : cudaMemcpyDeviceToDevice, c),
+            "copy uvw");
+  int rc = ingest(ctx, vis_type, direct, row_channels, start_channel, rows, channels, pols, in.vis.ptr, rows, 0, c,
+                  ctx->sms);
+  if (rc != LEAP_OK) return rc;
+  split_uvw<<<grid_1d(3 * rows, 256), 256, 0, c>>>(in.uvw.as<double>(), rows, in.uvw_f.as<float>());
+  LEAP_CUDA(cudaGetLastError(), "ingestion launch");
+  LEAP_CUDA(cudaEventRecord(in.ready, c), "upload event");
+  in.pending = true;
+  in.vis_type = vis_type;
+  in.rows = rows;
+  in.channels = channels;
+  in.pols = pols;
+  in.has_map = false;
+  if (vis_type == LEAP_VIS_C64 && pols == 4 && rows * 8 < (int64_t(1) << 31)) {
+    auto enc = tensor_map_encoder();
+    if (!enc) return fail(ctx, LEAP_ERR_CUDA, "cuTensorMapEncodeTiled unavailable");
+    cuuint64_t dims[2] = {static_cast<cuuint64_t>(rows) * 8, static_cast<cuuint64_t>(channels)};
+    cuuint64_t strides[1] = {static_cast<cuuint64_t>(rows) * 32};
+    cuuint32_t estr[2] = {1, 1};
+    for (int which = 0; which < 2; ++which) {
+      cuuint32_t box[2] = {256, static_cast<cuuint32_t>(which == 0 ? PipeShape<1>::CH : PipeShape<4>::CH)};
+      CUresult r = enc(which == 0 ? &in.map16 : &in.map8, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 2, in.vis.ptr, dims, strides,
+                       box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
+                       CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+      if (r != CUDA_SUCCESS) return fail(ctx, LEAP_ERR_CUDA, "cuTensorMapEncodeTiled failed: " + std::to_string(r));
+    }
+    in.has_map = true;
+  }
+  return LEAP_OK;
+}
+
 int32_t leap_apply_flags(leap_ctx* ctx, int32_t slot, const uint8_t* flags, int64_t row_channels, int32_t start_channel,
                          int32_t flag_pols, int32_t memory, int64_t* flagged_groups) {
   if (!ctx || !flags) return fail(ctx, LEAP_ERR_INVALID_ARGUMENT, "NULL argument");
   auto it = ctx->integ.find(slot);
   if (it == ctx->integ.end()) return fail(ctx, LEAP_ERR_NOT_READY, "integration slot not set");
   Integration& in = it->second;
+  finish_upload(in);
   if (flag_pols < 1 || start_channel < 0 || static_cast<int64_t>(start_channel) + in.channels > row_channels)
     return fail(ctx, LEAP_ERR_INVALID_ARGUMENT, "flag array shape does not cover the integration");
   if (memory != LEAP_MEMORY_HOST && memory != LEAP_MEMORY_DEVICE) return fail(ctx, LEAP_ERR_INVALID_ARGUMENT, "unknown memory kind");
@@ -1444,6 +1562,8 @@ int32_t leap_release_integration(leap_ctx* ctx, int32_t slot) {
   if (it == ctx->integ.end()) return fail(ctx, LEAP_ERR_NOT_READY, "integration slot not set");
   DeviceGuard g(ctx->device);
   cudaStreamSynchronize(ctx->stream);
+  finish_upload(it->second);
+  if (it->second.ready) cudaEventDestroy(it->second.ready);
   it->second.vis.release();
   it->second.uvw.release();
   it->second.uvw_f.release();
@@ -1523,6 +1643,7 @@ int32_t leap_backward(leap_ctx* ctx, int32_t slot, const double* d_dd, int32_t n
   const int nbl = static_cast<int>(md.k.nbaselines);
   const int S = md.S, D = ndir, nI = md.Arows - 1, nI1 = md.A1rows - 1;
   cudaStream_t s = stream ? static_cast<cudaStream_t>(stream) : ctx->stream;
+  if (in.pending) cudaStreamWaitEvent(s, in.ready, 0);
   LEAP_CUDA(ctx->adj_dphi.ensure(sizeof(double) * std::max(nI, 1) * D), "alloc adjoint scratch");
   LEAP_CUDA(ctx->adj_cal1.ensure(sizeof(double) * S * D), "alloc adjoint scratch");
   LEAP_CUDA(ctx->adj_phi1.ensure(sizeof(double) * std::max(nI1, 1) * D), "alloc adjoint scratch");
@@ -1621,6 +1742,7 @@ int32_t leap_rotate_uvw(leap_ctx* ctx, int32_t slot, const double* dd, int32_t n
   if (it == ctx->integ.end()) return fail(ctx, LEAP_ERR_NOT_READY, "integration slot not set");
   if (ndir <= 0) return fail(ctx, LEAP_ERR_INVALID_ARGUMENT, "ndirections must be positive");
   DeviceGuard g(ctx->device);
+  finish_upload(it->second);
   const int64_t rows = it->second.rows;
   DeviceBuffer d_dd, d_out;
   LEAP_CUDA(d_dd.ensure(sizeof(double) * 9 * ndir), "alloc dd");

@@ -61,6 +61,7 @@ SIGNATURES = {
     "leap_build_metadata": ([vp, ctypes.POINTER(LeapConstants), vp, vp, vp, i32, ctypes.POINTER(i32)], i32),
     "leap_get_metadata_matrix": ([vp, i32, vp, i64, ctypes.POINTER(i32), ctypes.POINTER(i32)], i32),
     "leap_set_integration_ms": ([vp, i32, i32, vp, i64, i32, vp, i64, i32, i32, i32], i32),
+    "leap_set_integration_ms_async": ([vp, i32, i32, vp, i64, i32, vp, i64, i32, i32, i32], i32),
     "leap_apply_flags": ([vp, i32, vp, i64, i32, i32, i32, ctypes.POINTER(i64)], i32),
     "leap_release_integration": ([vp, i32], i32),
     "leap_calibrate": ([vp, i32, vp, i32, i32, vp], i32),

@@ -269,7 +269,8 @@ class Context:
                                                  _abi.LEAP_MEMORY_DEVICE))
         self.slots[slot] = (C, rows, P)
 
-    def set_integration_ms(self, slot: int, ms_vis, uvw, start_channel: int = 0, channels: Optional[int] = None):
+    def set_integration_ms(self, slot: int, ms_vis, uvw, start_channel: int = 0, channels: Optional[int] = None,
+                           asynchronous: bool = False):
         """Upload from the MeasurementSet's DATA order: ms_vis is (rows, row_channels, pols)
         complex, a numpy array (pageable or not) or a torch tensor (CUDA, or pinned CPU memory);
         channels [start_channel, start_channel + channels) are taken.  Transpose and NaN rule
@@ -294,7 +295,8 @@ class Context:
                 assert not uvw.is_cuda
             vp, up = ms_vis.data_ptr(), uvw.data_ptr()
         C = row_channels - start_channel if channels is None else channels
-        self._check(lib.leap_set_integration_ms(self._h, slot, vt, vp, row_channels, start_channel, up, rows, C, P, mem))
+        fn = lib.leap_set_integration_ms_async if asynchronous else lib.leap_set_integration_ms
+        self._check(fn(self._h, slot, vt, vp, row_channels, start_channel, up, rows, C, P, mem))
         self.slots[slot] = (C, rows, P)
 
     def apply_flags(self, slot: int, flags: np.ndarray, start_channel: int = 0) -> int:

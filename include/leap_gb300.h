@@ -149,6 +149,18 @@ int32_t leap_set_integration_ms(leap_ctx* ctx, int32_t slot, int32_t vis_type, c
                                 int64_t row_channels, int32_t start_channel, const double* uvw, int64_t rows,
                                 int32_t channels, int32_t pols, int32_t memory);
 
+/* Asynchronous form of leap_set_integration_ms for device or page-locked host
+ * memory (ms_data and uvw; anything else is rejected): the upload is queued on the
+ * context's copy stream, after every call already queued on the context's stream,
+ * and the function returns at once.  Calibrate calls on the slot wait for it on the
+ * device; rewriting or releasing the slot waits for it on the host.  The caller
+ * keeps the source buffers unchanged until a call that reads the slot has
+ * finished.  This overlaps the upload of the next integration chunk with the
+ * calibration of the current one. */
+int32_t leap_set_integration_ms_async(leap_ctx* ctx, int32_t slot, int32_t vis_type, const void* ms_data,
+                                      int64_t row_channels, int32_t start_channel, const double* uvw, int64_t rows,
+                                      int32_t channels, int32_t pols, int32_t memory);
+
 /* Opt-in flagging (off unless called): zero every (row, channel) group of a resident
  * integration whose MeasurementSet FLAG is set for any pol, so flagged samples add
  * nothing to the averages.  The reference averages flagged samples and skips only

@@ -106,3 +106,33 @@ def test_opt_in_flags_equal_nan_groups(ctx, flag_pols):
     np.testing.assert_array_equal(got, ctx.calibrate(1, dds, lg.LEAP_PRECISION_FP64))
     assert np.abs(got - plain).max() > 0
     ctx.release_integration(1)
+
+
+def test_async_ingestion_double_buffered(ctx):
+    """Chunks uploaded asynchronously into two slots while the other slot is calibrated:
+    every chunk's cal phases equal those of a synchronous upload."""
+    chunks = []
+    for i in range(4):
+        obs, dirs = synth.small_case(stations=24, timesteps=2, channels=33, directions=5, vis_dtype=np.complex64,
+                                     seed_shift=20 + i)
+        chunks.append((obs, dirs))
+    md = lg.build_metadata(chunks[0][0])
+    ctx.set_metadata(md)
+    dds = _dds(md, chunks[0][1])
+    exp = []
+    for obs, _ in chunks:
+        ctx.set_integration(0, obs.vis, obs.uvw)
+        exp.append(ctx.calibrate(0, dds, lg.LEAP_PRECISION_MIXED))
+    hosts = [(torch.from_numpy(np.ascontiguousarray(o.vis.transpose(1, 0, 2))).pin_memory(),
+              torch.from_numpy(o.uvw).pin_memory()) for o, _ in chunks]
+    ctx.set_integration_ms(10, *hosts[0], asynchronous=True)
+    for k in range(len(chunks)):
+        if k + 1 < len(chunks):
+            ctx.set_integration_ms(10 + (k + 1) % 2, *hosts[k + 1], asynchronous=True)
+        got = ctx.calibrate(10 + k % 2, dds, lg.LEAP_PRECISION_MIXED)
+        np.testing.assert_array_equal(got, exp[k])
+    with pytest.raises(lg.InvalidArgument):  # pageable memory cannot be read asynchronously
+        ctx.set_integration_ms(12, np.ascontiguousarray(chunks[0][0].vis.transpose(1, 0, 2)), chunks[0][0].uvw,
+                               asynchronous=True)
+    ctx.release_integration(10)
+    ctx.release_integration(11)
