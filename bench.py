@@ -436,6 +436,8 @@ def run_gpu(args, rank: int, world: int):
         dist.init_process_group("nccl")
 
     ctx = lg.Context(local)
+    if args.tc_rotation >= 0:
+        ctx.set_option(_abi.LEAP_OPTION_TENSOR_CORE_ROTATION, args.tc_rotation)
     # A dedicated stream: the calls and the timing events go on the same (non-null) stream.
     bstream = torch.cuda.Stream(device=f"cuda:{local}")
     torch.cuda.set_stream(bstream)
@@ -615,6 +617,8 @@ def main():
     ap.add_argument("--directions", type=int, default=0, help="0: the workload's own count")
     ap.add_argument("--chunks", type=int, default=32)
     ap.add_argument("--e2e", type=int, default=-1, help="1/0: force the host-buffer end-to-end timing on/off")
+    ap.add_argument("--tc-rotation", type=int, default=-1,
+                    help="tensor-core rotate + average: 0 never, 1 autotuned (library default), 2 always")
     ap.add_argument("--cpu-budget", type=float, default=15.0)
     ap.add_argument("--skip-cpu", action="store_true")
     ap.add_argument("--skip-plain", action="store_true")

@@ -22,6 +22,7 @@
 #include "kernels_adjoint.cuh"
 #include "kernels_ingest.cuh"
 #include "kernels_metadata.cuh"
+#include "kernels_mma.cuh"
 
 using namespace leapgb;
 
@@ -99,6 +100,7 @@ struct Metadata {
 struct TuneChoice {
   int tpb = 0;    // tiles per block of the pipelined kernel (1 or 4)
   int waves = 0;  // target rounds of the persistent grid when planning slabs
+  int mma = -1;   // 1: tensor-core (mma.sync) bulk kernel, 0: CUDA-core kernel, -1: by direction count
 };
 
 struct leap_ctx {
@@ -109,6 +111,8 @@ struct leap_ctx {
   bool capturing = false;             // recording a CUDA graph: skip host-side uploads and timing events
   bool autotune = true;               // tune new batched shapes on first use
   bool tc_gemm = true;                // mixed form: Ad contraction on the tensor cores (3xTF32)
+  int mma_rotate = 1;                 // tensor-core rotate + average: 0 never, 1 autotuner candidate, 2 always
+  bool pipe_attr_mma = false;
   int tc_attr_set = 0;                // bit per N tile whose shared-memory size was raised
   DeviceBuffer dphi_tc;               // packed dphi operand of the tensor-core contraction
   DeviceBuffer adj_dphi, adj_cal1, adj_phi1, adj_gavg, adj_partial;  // adjoint scratch
@@ -283,15 +287,20 @@ int rotate_stage(leap_ctx* ctx, const std::vector<WorkItem>& items, const double
   }
 
   if (all_pipe) {
-    // Tiles per block: 4 when items hold at most 8 directions (one block covers
-    // 128 baselines x 8 directions), else 1 (32 baselines x 32 directions).
-    const int tpb = (ctx->tune.tpb > 0) ? ctx->tune.tpb : (min_ndir <= 8 ? 4 : 1);
+    // Kernel: the tensor-core one (16 directions per unit) when the autotuner chose it or the
+    // option forces it (items of at least 12 directions); else the CUDA-core one with 4 tiles
+    // per block when items hold at most 8 directions (one block covers 128 baselines x 8
+    // directions), else 1 tile (32 baselines x 32 directions).
+    const bool mma = ctx->mma_rotate > 0 && (ctx->tune.mma >= 0 ? ctx->tune.mma == 1
+                                                                : ctx->mma_rotate == 2 && min_ndir >= 12);
+    const int tpb = mma ? 1 : (ctx->tune.tpb > 0) ? ctx->tune.tpb : (min_ndir <= 8 ? 4 : 1);
     const int wpt = kPipeNC / tpb;
+    const int dirs_per_unit = mma ? kMmaDirs : wpt * kPipeDPW;
     const int tgroups = (tiles + tpb - 1) / tpb;
     int64_t work = 0;  // timestep-channels x unit multiplicity, for the slab plan
     for (const auto& w : items) {
       const Integration& in = ctx->integ.at(w.slot);
-      work += (in.rows / nbl) * in.channels * static_cast<int64_t>(tgroups) * ((w.ndir + wpt * kPipeDPW - 1) / (wpt * kPipeDPW));
+      work += (in.rows / nbl) * in.channels * static_cast<int64_t>(tgroups) * ((w.ndir + dirs_per_unit - 1) / dirs_per_unit);
     }
     // Target work per unit: enough units for ~target_waves rounds of the persistent grid.
     const int waves = ctx->tune.waves > 0 ? ctx->tune.waves : 4;
@@ -317,15 +326,15 @@ int rotate_stage(leap_ctx* ctx, const std::vector<WorkItem>& items, const double
       int tps;
       if (items.size() == 1 && ctx->tune.waves <= 0) {
         int nts;
-        choose_pipe_slabs(T, static_cast<int64_t>(tgroups) * ((w.ndir + wpt * kPipeDPW - 1) / (wpt * kPipeDPW)),
-                          ctx->sms, tps, nts);
+        choose_pipe_slabs(T, static_cast<int64_t>(tgroups) * ((w.ndir + dirs_per_unit - 1) / dirs_per_unit), ctx->sms,
+                          tps, nts);
       } else {
         tps = static_cast<int>(std::max<int64_t>(1, std::min<int64_t>(T, (per_unit + C - 1) / C)));
       }
       it.t_per_slab = tps;
       it.nslab = (T + tps - 1) / tps;
       it.tgroups = tgroups;
-      it.dgroups = (w.ndir + wpt * kPipeDPW - 1) / (wpt * kPipeDPW);
+      it.dgroups = (w.ndir + dirs_per_unit - 1) / dirs_per_unit;
       it.dir0 = w.dir0;
       it.ndir = w.ndir;
       it.unit_begin = units;
@@ -407,7 +416,15 @@ int rotate_stage(leap_ctx* ctx, const std::vector<WorkItem>& items, const double
     pp.dirk = ctx->dirk.as<float>();
     pp.twiddle = ctx->twiddle.as<float2>();
     pp.err = ctx->dev_err.as<int>();
-    if (tpb == 4) {
+    if (mma) {
+      if (!ctx->pipe_attr_mma) {
+        LEAP_CUDA(cudaFuncSetAttribute(rotate_average_mma_pipe, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                       pipe_smem_bytes<1>()),
+                  "set shared memory size");
+        ctx->pipe_attr_mma = true;
+      }
+      rotate_average_mma_pipe<<<grid, kPipeNC * 32, pipe_smem_bytes<1>(), s>>>(pp);
+    } else if (tpb == 4) {
       if (!ctx->pipe_attr_set4) {
         LEAP_CUDA(cudaFuncSetAttribute(rotate_average_mixed_pipe<kPipeNC, kPipeDPW, 4>,
                                        cudaFuncAttributeMaxDynamicSharedMemorySize, pipe_smem_bytes<4>()),
@@ -770,7 +787,8 @@ int calibrate_impl(leap_ctx* ctx, int32_t slot, const double* d_dd, int32_t ndir
 }
 
 std::string batch_key(const leap_ctx* ctx, const std::vector<WorkItem>& items, int32_t D, int32_t precision) {
-  std::string k = std::to_string(D) + ":" + std::to_string(precision) + (ctx->tc_gemm ? ":tc" : ":cc");
+  std::string k = std::to_string(D) + ":" + std::to_string(precision) + (ctx->tc_gemm ? ":tc" : ":cc") +
+                  ":mma" + std::to_string(ctx->mma_rotate);
   for (const auto& w : items) k += "|" + std::to_string(w.slot) + "," + std::to_string(w.dir0) + "," + std::to_string(w.ndir);
   return k;
 }
@@ -785,8 +803,10 @@ int autotune_batch(leap_ctx* ctx, const std::vector<WorkItem>& items, int32_t D,
   const int tpbs[2] = {1, 4};
   for (int tpb : tpbs) {
     if (tpb == 4 && min_ndir > 8) continue;
-    for (int waves : {2, 4, 8}) cands.push_back(TuneChoice{tpb, waves});
+    for (int waves : {2, 4, 8}) cands.push_back(TuneChoice{tpb, waves, 0});
   }
+  if (ctx->mma_rotate > 0 && precision == LEAP_PRECISION_MIXED && min_ndir >= 12)
+    for (int waves : {2, 4, 8}) cands.push_back(TuneChoice{1, waves, 1});
   cudaEvent_t e0, e1;
   LEAP_CUDA(cudaEventCreate(&e0), "tuning event");
   LEAP_CUDA(cudaEventCreate(&e1), "tuning event");
@@ -1716,6 +1736,10 @@ int32_t leap_set_option(leap_ctx* ctx, int32_t option, int32_t value) {
   switch (option) {
     case LEAP_OPTION_AUTOTUNE: ctx->autotune = value != 0; return LEAP_OK;
     case LEAP_OPTION_TENSOR_CORE_CONTRACTION: ctx->tc_gemm = value != 0; return LEAP_OK;
+    case LEAP_OPTION_TENSOR_CORE_ROTATION:
+      if (value < 0 || value > 2) return fail(ctx, LEAP_ERR_INVALID_ARGUMENT, "rotation option must be 0, 1 or 2");
+      ctx->mma_rotate = value;
+      return LEAP_OK;
     default: return fail(ctx, LEAP_ERR_INVALID_ARGUMENT, "unknown option");
   }
 }

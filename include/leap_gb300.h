@@ -215,6 +215,10 @@ int32_t leap_set_autotune(leap_ctx* ctx, int32_t enable);
 #define LEAP_OPTION_AUTOTUNE 1                   /* as leap_set_autotune (default on) */
 #define LEAP_OPTION_TENSOR_CORE_CONTRACTION 2    /* mixed form: Ad contraction as 3xTF32 tcgen05 MMAs (default on);
                                                     off: FP32 CUDA-core GEMM */
+#define LEAP_OPTION_TENSOR_CORE_ROTATION 3       /* mixed form, 4-pol complex<float>: the rotate + average
+                                                    multiply-accumulate as 3xTF32 mma.sync for items of >= 12
+                                                    directions.  0: never; 1 (default): only where the batched
+                                                    autotuner measures it faster; 2: always */
 int32_t leap_set_option(leap_ctx* ctx, int32_t option, int32_t value);
 
 /* Copy the avgData of `direction` from the last calibrate call to host memory

@@ -72,3 +72,36 @@ def test_tensor_core_contraction_batched(ctx):
 def test_unknown_option_is_rejected(ctx):
     with pytest.raises(lg.InvalidArgument):
         ctx.set_option(99, 1)
+
+
+@pytest.mark.parametrize("stations,timesteps,channels,ndir", [(64, 9, 23, 40), (33, 5, 5, 16), (40, 3, 70, 12),
+                                                              (128, 2, 96, 64)])
+def test_tensor_core_rotation_matches_cuda_core_and_oracle(ctx, stations, timesteps, channels, ndir):
+    """The rotate + average multiply-accumulate as 3xTF32 mma.sync (16 directions per unit) against
+    the FP32 CUDA-core kernel and the oracle: partial 32-baseline tiles, partial 16-channel chunks,
+    direction counts that are not multiples of 16, several timestep slabs."""
+    from leap_gb300._abi import LEAP_OPTION_TENSOR_CORE_ROTATION
+    obs, dirs = synth.small_case(stations=stations, timesteps=timesteps, channels=channels, directions=ndir,
+                                 vis_dtype=np.complex64, seed_shift=stations + 3)
+    md = lg.build_metadata(obs)
+    mdo = oracle.metadata(obs)
+    ctx.set_metadata(md)
+    ctx.set_integration(0, obs.vis, obs.uvw)
+    dds = _dds(md, dirs)
+    out = {}
+    try:
+        for flag in (1, 0):
+            ctx.set_option(LEAP_OPTION_TENSOR_CORE_ROTATION, 2 if flag else 0)
+            cal = ctx.calibrate(0, dds, lg.LEAP_PRECISION_MIXED)
+            out[flag] = (cal, np.stack([ctx.avgdata(d) for d in range(ndir)]))
+    finally:
+        ctx.set_option(LEAP_OPTION_TENSOR_CORE_ROTATION, 1)
+    cal_o, avg_o = oracle.calibrate_interval(obs.vis, obs.uvw, dds, mdo, return_avg=True)
+    scale = np.abs(obs.vis).sum(axis=0).reshape(timesteps, obs.nbaselines, 4).sum(axis=0)
+    for flag in (1, 0):
+        cal, avg = out[flag]
+        err = np.abs(avg - avg_o) / np.maximum(scale, 1e-30)[None]
+        assert err.max() < 2e-6, (flag, err.max())
+        assert np.abs(cal - cal_o).max() <= MIXED_CAL_TOL, flag
+    assert np.abs(out[1][0] - out[0][0]).max() <= 5 * TC_VS_CUDA_CORE_TOL
+    ctx.release_integration(0)
