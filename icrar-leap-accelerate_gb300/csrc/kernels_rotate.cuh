@@ -432,6 +432,8 @@ struct RefantItem {
   int32_t dgroups, block_begin, pad_[2];
 };
 
+constexpr int kRefantPrefetch = 16;  // channel loads in flight per lane in the compensated pass
+
 template <int DPW>
 __global__ void __launch_bounds__(128) refant_average_df_items(const RefantItem* __restrict__ items, int nitems,
                                                               int nbl, double f0, double df,
@@ -475,17 +477,28 @@ __global__ void __launch_bounds__(128) refant_average_df_items(const RefantItem*
       pb[j] = frac_turns_u64(-dw * kB);
     }
     const float2* src = it.vis + r * it.pols;
-#pragma unroll 4
-    for (int c = c_lo; c < c_hi; ++c) {
-      const float2 v = __ldg(src + static_cast<int64_t>(c) * it.rows * it.pols);
+    const int64_t cstride = static_cast<int64_t>(it.rows) * it.pols;
+    // Blocks of kRefantPrefetch channels: all loads of a block are issued before any use,
+    // so each lane keeps that many scattered 8-byte reads in flight (the rows of the
+    // reference-antenna baselines are spread over the cube).
+    for (int c0 = c_lo; c0 < c_hi; c0 += kRefantPrefetch) {
+      float2 vb[kRefantPrefetch];
 #pragma unroll
-      for (int j = 0; j < DPW; ++j) {
-        float zrh, zrl, zih, zil;
-        df_twiddle(pa[j] + static_cast<uint64_t>(c) * pb[j], tab, zrh, zrl, zih, zil);
-        df_add_product(re[j], v.x, zrh, zrl);
-        df_add_product(re[j], -v.y, zih, zil);
-        df_add_product(im[j], v.x, zih, zil);
-        df_add_product(im[j], v.y, zrh, zrl);
+      for (int i = 0; i < kRefantPrefetch; ++i)
+        vb[i] = c0 + i < c_hi ? __ldg(src + static_cast<int64_t>(c0 + i) * cstride) : make_float2(0.f, 0.f);
+#pragma unroll
+      for (int i = 0; i < kRefantPrefetch; ++i) {
+        if (c0 + i >= c_hi) break;
+        const float2 v = vb[i];
+#pragma unroll
+        for (int j = 0; j < DPW; ++j) {
+          float zrh, zrl, zih, zil;
+          df_twiddle(pa[j] + static_cast<uint64_t>(c0 + i) * pb[j], tab, zrh, zrl, zih, zil);
+          df_add_product(re[j], v.x, zrh, zrl);
+          df_add_product(re[j], -v.y, zih, zil);
+          df_add_product(im[j], v.x, zih, zil);
+          df_add_product(im[j], v.y, zrh, zrl);
+        }
       }
     }
   }
