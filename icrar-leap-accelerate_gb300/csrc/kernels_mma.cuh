@@ -62,16 +62,17 @@ __device__ __forceinline__ void mma_16x8x8_tf32(float (&d)[4], uint32_t a0, uint
 __global__ void __launch_bounds__(256, 1) rotate_average_mma_pipe(const PipeParams p) {
   constexpr int TPB = 1;
   constexpr int CH = PipeShape<TPB>::CH;
+  constexpr int NS = PipeShape<TPB>::STAGES;
   constexpr int NC = 8;
   constexpr int NB = kMmaBaselines;
   static_assert(NC * NB == 32, "8 warps x 4 baselines cover a 32-baseline tile");
   static_assert(CH == 16, "4 MMA steps of 4 channels per chunk");
   extern __shared__ __align__(128) unsigned char smem[];
   unsigned char* stage_mem = smem;
-  float2* tab = reinterpret_cast<float2*>(smem + kPipeStages * pipe_stage_bytes<TPB>());
+  float2* tab = reinterpret_cast<float2*>(smem + NS * pipe_stage_bytes<TPB>());
   uint64_t* full = reinterpret_cast<uint64_t*>(tab + kTwiddleSize);
-  uint64_t* empty = full + kPipeStages;
-  int* unit_begin = reinterpret_cast<int*>(empty + kPipeStages);
+  uint64_t* empty = full + NS;
+  int* unit_begin = reinterpret_cast<int*>(empty + NS);
 
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int g = lane >> 2, q = lane & 3;
@@ -82,7 +83,7 @@ __global__ void __launch_bounds__(256, 1) rotate_average_mma_pipe(const PipePara
   ChunkCursor pc{};
   uint32_t issued = 0;
   if (producer) {
-    for (int i = 0; i < kPipeStages; ++i) {
+    for (int i = 0; i < NS; ++i) {
       mbar_init(&full[i], 1);
       mbar_init(&empty[i], NC);
     }
@@ -91,7 +92,7 @@ __global__ void __launch_bounds__(256, 1) rotate_average_mma_pipe(const PipePara
     pc.u = slot_unit(p, pc.s);
     pc.item = 0;
     if (pc.u >= 0) cursor_unit(pc, p, unit_begin);
-    for (; issued < kPipeStages && pc.u >= 0; ++issued) {
+    for (; issued < NS && pc.u >= 0; ++issued) {
       issue_chunk<TPB>(pc, p, stage_mem, full, issued);
       cursor_next<TPB>(pc, p, unit_begin);
     }
@@ -150,8 +151,8 @@ __global__ void __launch_bounds__(256, 1) rotate_average_mma_pipe(const PipePara
         }
       }
       for (int cb = 0; cb < C; cb += CH, ++it) {
-        const int st = it % kPipeStages;
-        if (!mbar_wait_bounded(&full[st], (it / kPipeStages) & 1)) {
+        const int st = it % NS;
+        if (!mbar_wait_bounded(&full[st], (it / NS) & 1)) {
           atomicOr(p.err, kDevErrTimeout);
           ok = false;
           break;
@@ -207,7 +208,7 @@ __global__ void __launch_bounds__(256, 1) rotate_average_mma_pipe(const PipePara
         __syncwarp();
         if (lane == 0) mbar_arrive(&empty[st]);
         if (producer && pc.u >= 0) {
-          if (!mbar_wait_bounded(&empty[st], (it / kPipeStages) & 1)) {
+          if (!mbar_wait_bounded(&empty[st], (it / NS) & 1)) {
             atomicOr(p.err, kDevErrTimeout);
             ok = false;
           } else {
@@ -237,8 +238,8 @@ __global__ void __launch_bounds__(256, 1) rotate_average_mma_pipe(const PipePara
     }
   }
   if (producer) {
-    for (uint32_t j = (issued > kPipeStages ? issued - kPipeStages : 0); j < issued; ++j)
-      if (!mbar_wait_bounded(&full[j % kPipeStages], (j / kPipeStages) & 1)) atomicOr(p.err, kDevErrTimeout);
+    for (uint32_t j = (issued > NS ? issued - NS : 0); j < issued; ++j)
+      if (!mbar_wait_bounded(&full[j % NS], (j / NS) & 1)) atomicOr(p.err, kDevErrTimeout);
   }
 }
 

@@ -18,7 +18,7 @@
 // Boxes past the last row or channel are zero-filled by the TMA unit; rows of
 // a partial tile that belong to the next timestep are loaded but not used.
 // Every warp releases a stage through its "empty" mbarrier; lane 0 of warp 0
-// then refills it with the chunk kPipeStages ahead.  (A separate producer
+// then refills it with the chunk one ring length ahead.  (A separate producer
 // warp would make 9 warps, 3 on one SM sub-partition, and cap registers at
 // 168.)  All waits are bounded and report a device error instead of hanging.
 //
@@ -29,8 +29,8 @@
 // every kPipeReseed channels and advanced by one FP32 complex multiply per
 // channel in between (drift over 8 steps ~5e-7; it reaches the cal phases only
 // through baselines that the reference-antenna pass does not cover, with
-// weight ~1/S).  Sums: FP32 over 16 channels (one or two chunks), folded into
-// Kahan pairs.
+// weight ~1/S).  Sums: FP32 over each 16-channel chunk, folded into Kahan
+// pairs.
 //
 // Shared-memory reads: lane i reads its 32 bytes as two 16-byte halves; lanes
 // with bit 2 set read the upper half first so that each quarter-warp covers
@@ -67,19 +67,20 @@ struct PipeParams {
 constexpr int kPipeMaxItems = 128;
 constexpr int kPipeReseed = 8;          // channels between table-accurate twiddles
 constexpr int kPipeFold = 16;           // channels summed in FP32 before a Kahan fold
-constexpr int kPipeStages = 4;
 constexpr int kPipeItemBytes = 32 * 4 * 8;  // one channel of one tile: 32 baselines x 4 pols x complex<float>
 
+// Channels per chunk and ring depth: 1 tile x 16 channels = 16 KB stages, 4 deep; 4 tiles x
+// 16 channels = 64 KB stages, 3 deep (192 KB of the 227 KB of shared memory).
 template <int TPB> struct PipeShape;
-template <> struct PipeShape<1> { static constexpr int CH = 16; };  // 16 KB stages
-template <> struct PipeShape<4> { static constexpr int CH = 8; };   // 4 tiles x 8 KB stages
+template <> struct PipeShape<1> { static constexpr int CH = 16, STAGES = 4; };
+template <> struct PipeShape<4> { static constexpr int CH = 16, STAGES = 3; };
 
 template <int TPB>
 __host__ __device__ constexpr int pipe_stage_bytes() { return TPB * PipeShape<TPB>::CH * kPipeItemBytes; }
 
 template <int TPB>
 __host__ __device__ constexpr int pipe_smem_bytes() {
-  return kPipeStages * pipe_stage_bytes<TPB>() + kTwiddleSize * 8 + 2 * kPipeStages * 8 + kPipeMaxItems * 4;
+  return PipeShape<TPB>::STAGES * (pipe_stage_bytes<TPB>() + 16) + kTwiddleSize * 8 + kPipeMaxItems * 4;
 }
 
 // Position in a block's chunk sequence: slot s of the order table, unit u = order[s].
@@ -160,24 +161,25 @@ __device__ __forceinline__ void mac_channel(const unsigned char* src, int h, flo
 template <int NC, int DPW, int TPB>
 __global__ void __launch_bounds__(NC * 32, 1) rotate_average_mixed_pipe(const PipeParams p) {
   constexpr int CH = PipeShape<TPB>::CH;
+  constexpr int NS = PipeShape<TPB>::STAGES;
   constexpr int WPT = NC / TPB;  // warps (direction groups of DPW) per tile
   static_assert(NC % TPB == 0, "warps must divide among tiles");
   extern __shared__ __align__(128) unsigned char smem[];
   unsigned char* stage_mem = smem;
-  float2* tab = reinterpret_cast<float2*>(smem + kPipeStages * pipe_stage_bytes<TPB>());
+  float2* tab = reinterpret_cast<float2*>(smem + NS * pipe_stage_bytes<TPB>());
   uint64_t* full = reinterpret_cast<uint64_t*>(tab + kTwiddleSize);
-  uint64_t* empty = full + kPipeStages;
-  int* unit_begin = reinterpret_cast<int*>(empty + kPipeStages);
+  uint64_t* empty = full + NS;
+  int* unit_begin = reinterpret_cast<int*>(empty + NS);
 
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const bool producer = threadIdx.x == 0;
   for (int i = threadIdx.x; i < kTwiddleSize; i += blockDim.x) tab[i] = __ldg(p.twiddle + i);
   for (int i = threadIdx.x; i < p.nitems; i += blockDim.x) unit_begin[i] = p.items[i].unit_begin;
   __syncthreads();
-  ChunkCursor pc{};  // producer cursor, kPipeStages chunks ahead of the consumers
+  ChunkCursor pc{};  // producer cursor, NS chunks ahead of the consumers
   uint32_t issued = 0;
   if (producer) {
-    for (int i = 0; i < kPipeStages; ++i) {
+    for (int i = 0; i < NS; ++i) {
       mbar_init(&full[i], 1);
       mbar_init(&empty[i], NC);
     }
@@ -186,7 +188,7 @@ __global__ void __launch_bounds__(NC * 32, 1) rotate_average_mixed_pipe(const Pi
     pc.u = slot_unit(p, pc.s);
     pc.item = 0;
     if (pc.u >= 0) cursor_unit(pc, p, unit_begin);
-    for (; issued < kPipeStages && pc.u >= 0; ++issued) {
+    for (; issued < NS && pc.u >= 0; ++issued) {
       issue_chunk<TPB>(pc, p, stage_mem, full, issued);
       cursor_next<TPB>(pc, p, unit_begin);
     }
@@ -243,7 +245,7 @@ __global__ void __launch_bounds__(NC * 32, 1) rotate_average_mixed_pipe(const Pi
           twiddle_turns(pb[j], tab, wr[j], wi[j]);
         }
       }
-      // FP32 partial sums of up to kPipeFold channels (one or two chunks), then a Kahan fold.
+      // FP32 partial sums of up to kPipeFold channels, then a Kahan fold.
       float pr[DPW][4], pi[DPW][4];
 #pragma unroll
       for (int j = 0; j < DPW; ++j)
@@ -251,8 +253,8 @@ __global__ void __launch_bounds__(NC * 32, 1) rotate_average_mixed_pipe(const Pi
         for (int q = 0; q < 4; ++q) pr[j][q] = pi[j][q] = 0.f;
       for (int cb = 0; cb < C; cb += CH, ++it) {
         const int n = min(CH, C - cb);
-        const int st = it % kPipeStages;
-        if (!mbar_wait_bounded(&full[st], (it / kPipeStages) & 1)) {
+        const int st = it % NS;
+        if (!mbar_wait_bounded(&full[st], (it / NS) & 1)) {
           atomicOr(p.err, kDevErrTimeout);
           ok = false;
           break;
@@ -300,8 +302,8 @@ __global__ void __launch_bounds__(NC * 32, 1) rotate_average_mixed_pipe(const Pi
         __syncwarp();
         if (lane == 0) mbar_arrive(&empty[st]);
         if (producer && pc.u >= 0) {
-          // Refill this stage with the chunk kPipeStages ahead once every warp released it.
-          if (!mbar_wait_bounded(&empty[st], (it / kPipeStages) & 1)) {
+          // Refill this stage with the chunk NS ahead once every warp released it.
+          if (!mbar_wait_bounded(&empty[st], (it / NS) & 1)) {
             atomicOr(p.err, kDevErrTimeout);
             ok = false;
           } else {
@@ -333,8 +335,8 @@ __global__ void __launch_bounds__(NC * 32, 1) rotate_average_mixed_pipe(const Pi
   }
   if (producer) {
     // Do not leave while copies issued by this block may still land in shared memory.
-    for (uint32_t j = (issued > kPipeStages ? issued - kPipeStages : 0); j < issued; ++j)
-      if (!mbar_wait_bounded(&full[j % kPipeStages], (j / kPipeStages) & 1)) atomicOr(p.err, kDevErrTimeout);
+    for (uint32_t j = (issued > NS ? issued - NS : 0); j < issued; ++j)
+      if (!mbar_wait_bounded(&full[j % NS], (j / NS) & 1)) atomicOr(p.err, kDevErrTimeout);
   }
 }
 

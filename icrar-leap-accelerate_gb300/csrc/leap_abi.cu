@@ -927,7 +927,7 @@ int finish_integration(leap_ctx* ctx, Integration& in, int32_t vis_type, int64_t
   in.pols = pols;
   in.has_map = false;
   if (vis_type == LEAP_VIS_C64 && pols == 4 && rows * 8 < (int64_t(1) << 31)) {
-    // The pipelined kernel's view: 2-D floats [channels][rows*8], box 256 x (16 or 8) channels.
+    // The pipelined kernels' view: 2-D floats [channels][rows*8], box 256 floats x 16 channels.
     auto enc = tensor_map_encoder();
     if (!enc) return fail(ctx, LEAP_ERR_CUDA, "cuTensorMapEncodeTiled unavailable");
     cuuint64_t dims[2] = {static_cast<cuuint64_t>(rows) * 8, static_cast<cuuint64_t>(channels)};
