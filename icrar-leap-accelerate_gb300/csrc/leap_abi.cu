@@ -952,12 +952,15 @@ int launch_ingest(leap_ctx* ctx, const void* src, int64_t row_channels, int32_t 
   const int TC = IngestTile<VisT>::TC;
   const int64_t tiles = ((nrows + 31) / 32) * ((channels + TC - 1) / TC);
   const int grid = static_cast<int>(std::max<int64_t>(1, std::min<int64_t>(tiles, max_blocks)));
+  // Beside a running calibration (one block per SM) the blocks are 128 threads, small
+  // enough in registers to share an SM with the bulk kernel's 256 x 223.
+  const int threads = max_blocks <= ctx->sms ? 128 : 256;
   const VisT* sp = static_cast<const VisT*>(src);
   VisT* dp = static_cast<VisT*>(dst);
   switch (pols) {
-    case 1: ingest_ms_transpose<VisT, 1><<<grid, 256, 0, s>>>(sp, row_channels, start_channel, nrows, channels, dp, rows_total, row0); break;
-    case 2: ingest_ms_transpose<VisT, 2><<<grid, 256, 0, s>>>(sp, row_channels, start_channel, nrows, channels, dp, rows_total, row0); break;
-    default: ingest_ms_transpose<VisT, 4><<<grid, 256, 0, s>>>(sp, row_channels, start_channel, nrows, channels, dp, rows_total, row0); break;
+    case 1: ingest_ms_transpose<VisT, 1><<<grid, threads, 0, s>>>(sp, row_channels, start_channel, nrows, channels, dp, rows_total, row0); break;
+    case 2: ingest_ms_transpose<VisT, 2><<<grid, threads, 0, s>>>(sp, row_channels, start_channel, nrows, channels, dp, rows_total, row0); break;
+    default: ingest_ms_transpose<VisT, 4><<<grid, threads, 0, s>>>(sp, row_channels, start_channel, nrows, channels, dp, rows_total, row0); break;
   }
   LEAP_CUDA(cudaGetLastError(), "ingestion kernel");
   return LEAP_OK;
