@@ -610,6 +610,9 @@ def run_gpu(args, rank: int, world: int):
                         "frac": w.f_alg / (k_ms / 1e3) / 3.6e13}}
     if hasattr(w, "vis_bytes_resident"):
         roof["hbm_read_once_frac"] = w.vis_bytes_resident / (k_ms / 1e3) / 1e9 / peak
+    if w.traffic:
+        # the DRAM bytes the kernel actually moves (ncu-measured traffic) over its event time
+        roof["dram_traffic_frac"] = w.traffic / (k_ms / 1e3) / 1e9 / peak
 
     cpu = None
     if rank == 0 and world == 1 and not args.skip_cpu:
