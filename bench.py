@@ -470,6 +470,8 @@ def run_gpu(args, rank: int, world: int):
     ctx = lg.Context(local)
     if args.tc_rotation >= 0:
         ctx.set_option(_abi.LEAP_OPTION_TENSOR_CORE_ROTATION, args.tc_rotation)
+    if args.gridded >= 0:
+        ctx.set_option(_abi.LEAP_OPTION_GRIDDED_ROTATION, args.gridded)
     # A dedicated stream: the calls and the timing events go on the same (non-null) stream.
     bstream = torch.cuda.Stream(device=f"cuda:{local}")
     torch.cuda.set_stream(bstream)
@@ -667,6 +669,8 @@ def main():
     ap.add_argument("--e2e", type=int, default=-1, help="1/0: force the host-buffer end-to-end timing on/off")
     ap.add_argument("--tc-rotation", type=int, default=-1,
                     help="tensor-core rotate + average: 0 never, 1 autotuned (library default), 2 always")
+    ap.add_argument("--gridded", type=int, default=-1,
+                    help="gridded rotate + average (tcgen05 grid product): 0 off, 1 on, -1 library default")
     ap.add_argument("--cpu-budget", type=float, default=15.0)
     ap.add_argument("--skip-cpu", action="store_true")
     ap.add_argument("--skip-plain", action="store_true")

@@ -271,3 +271,69 @@ int pseudo_inverse(const double* A, int32_t m, int32_t n, double* Ad, std::strin
 }
 
 }  // namespace leapgb
+
+namespace leapgb {
+
+std::vector<double> es_kernel_transform(int32_t taps, double beta, int32_t n, int32_t kmax) {
+  // psi and all its derivatives are ~exp(-beta) at the ends of the support, so the
+  // trapezoidal rule converges spectrally; 8192 panels give full FP64 accuracy.
+  const int panels = 8192;
+  const double half = 0.5 * taps, h = 2.0 * half / panels;
+  std::vector<double> psi(panels + 1);
+  for (int i = 0; i <= panels; ++i) {
+    const double x = -half + i * h, z = x / half;
+    const double q = std::max(0.0, 1.0 - z * z);
+    psi[i] = std::exp(beta * (std::sqrt(q) - 1.0)) * ((i == 0 || i == panels) ? 0.5 : 1.0);
+  }
+  std::vector<double> out(kmax + 1);
+  const double kTwoPiD = 6.283185307179586476925286766559;
+  for (int k = 0; k <= kmax; ++k) {
+    double s = 0.0;
+    const double w = kTwoPiD * k / n;
+    for (int i = 0; i <= panels; ++i) s += psi[i] * std::cos(w * (-half + i * h));
+    out[k] = s * h;
+  }
+  return out;
+}
+
+namespace {
+// Round to the nearest TF32 value (10 mantissa bits), ties away from zero.
+float round_tf32(float x) {
+  uint32_t b;
+  std::memcpy(&b, &x, 4);
+  b = (b + 0x1000u) & 0xFFFFE000u;
+  float y;
+  std::memcpy(&y, &b, 4);
+  return y;
+}
+}  // namespace
+
+void grid_table(int32_t C, int32_t taps, double beta, int32_t lbase, int32_t rows, std::vector<float>& out) {
+  const int n = 2 * C, c0 = C / 2;
+  const int nchunk = (C + 15) / 16, nrg = rows / 8;
+  const std::vector<double> psi_hat = es_kernel_transform(taps, beta, n, std::max(c0, C - 1 - c0));
+  out.assign(static_cast<size_t>(nchunk) * 2 * 2 * 2 * rows * 8, 0.0f);
+  const double kTwoPiD = 6.283185307179586476925286766559;
+  for (int c = 0; c < C; ++c) {
+    const int k = c - c0;
+    const double inv = 1.0 / psi_hat[std::abs(k)];
+    const int q = c / 16, ks = (c % 16) / 8, kk = c % 8;
+    for (int r = 0; r < rows; ++r) {
+      const long long l = static_cast<long long>(r) - lbase;
+      long long m = (static_cast<long long>(k) * l) % n;  // exact phase index
+      if (m < 0) m += n;
+      const double ang = kTwoPiD * static_cast<double>(m) / n;
+      const double v[2] = {std::cos(ang) * inv, std::sin(ang) * inv};
+      for (int ri = 0; ri < 2; ++ri) {
+        const float hi = round_tf32(static_cast<float>(v[ri]));
+        const float lo = round_tf32(static_cast<float>(v[ri] - static_cast<double>(hi)));
+        for (int hl = 0; hl < 2; ++hl) {
+          const size_t base = ((static_cast<size_t>((q * 2 + ks) * 2 + hl) * 2 + ri) * nrg + (r >> 3)) * 64;
+          out[base + ((kk >> 2) & 1) * 32 + (r & 7) * 4 + (kk & 3)] = hl == 0 ? hi : lo;
+        }
+      }
+    }
+  }
+}
+
+}  // namespace leapgb

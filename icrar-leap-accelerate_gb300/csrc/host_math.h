@@ -29,4 +29,15 @@ int phase_matrix_sparse(const int32_t* a1, const int32_t* a2, const uint8_t* fg,
 // SVDPseudoInverse (LA/math/cpu/matrix_invert.h:49-56): A (m x n, column-major) -> Ad (n x m, column-major).
 int pseudo_inverse(const double* A, int32_t m, int32_t n, double* Ad, std::string& err);
 
+// Grid matrix of the gridded rotate + average (kernels_grid.cuh) for C channels:
+// E[l][c] = exp(2 pi i (c - C/2) l / (2C)) / Psi(c - C/2) for table rows r = l + lbase,
+// r in [0, rows), with Psi the Fourier transform of the exponential-of-semicircle
+// kernel of width `taps` and shape `beta` at frequency k / (2C).  Written as 3xTF32
+// (hi, lo) splits in the packed K-major layout the kernel copies from:
+// [chunk of 16 channels][k-step][hi, lo][re, im][row group of 8][8 rows x 8 k].
+void grid_table(int32_t C, int32_t taps, double beta, int32_t lbase, int32_t rows, std::vector<float>& out);
+
+// Psi(k) = integral over |x| < taps/2 of psi(x) cos(2 pi x k / n), for k = 0..kmax.
+std::vector<double> es_kernel_transform(int32_t taps, double beta, int32_t n, int32_t kmax);
+
 }  // namespace leapgb

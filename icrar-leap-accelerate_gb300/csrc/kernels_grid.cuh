@@ -1,0 +1,741 @@
+// Gridded rotate + average (mixed form, 4 pols, complex<float>) on the tensor cores.
+//
+// For one row r and one direction the averaging sums (LA/algorithm/cpu/
+// CpuLeapCalibrator.cc:181-217) are
+//   sum_c V[p, r, c] exp(2 pi i (A + c B)),   A, B in turns (A: f0 term, B: df term).
+// With c = c0 + k (c0 = C/2) that is exp(2 pi i (A + c0 B)) G(B) where
+//   G(B) = sum_k f_k exp(2 pi i k B),  f_k = V[p, r, c0 + k],
+// a trigonometric polynomial in B that does not depend on the direction.  G is
+// evaluated as a type-2 non-uniform DFT: on the grid B_l = l / n (n = 2C, twice
+// oversampled) the values
+//   b_l = sum_k f_k exp(2 pi i k l / n) / Psi(k)
+// are one dense product of the visibility tile with a fixed matrix E[l, k], and
+//   G(B) ~= sum_l b_l psi(n B - l)
+// over the W grid points nearest n B, with psi the "exponential of semicircle"
+// kernel psi(x) = exp(beta (sqrt(1 - (2x/W)^2) - 1)) and Psi its Fourier
+// transform at frequency k / n (Barnett, Magland & af Klinteberg, SIAM J. Sci.
+// Comput. 41 (2019) C479).  With W = 10, beta = 2.3 W the interpolation error is
+// about 1e-8 of the l2 norm of f.  Per (row, direction) the work is W complex
+// multiply-adds instead of C, so the direction count no longer multiplies the
+// channel work; the channel work moves to the tensor cores.
+//
+// Tile: M = 128 rows of the product = 4 baselines x 4 timesteps x 4 pols x
+// (re, im).  TMEM lane m = 32 q + 8 t + 2 p + s holds baseline q of the quad, so
+// each 32-lane quarter is one baseline at 4 neighbouring timesteps, whose grid
+// positions differ by far less than a grid step: one warp-uniform tcgen05.ld of
+// W + 1 columns serves all 32 lanes of a direction.
+//
+// The product runs in 3xTF32.  The tensor cores accumulate FP32 with truncation,
+// whose error grows with the number of accumulation steps and the size of the
+// accumulator; so the large hi*hi products restart in a fresh accumulator every
+// 64 channels (a "segment") and the small lo*hi + hi*lo corrections go to an
+// accumulator of their own.  Converter warps add the segments together with
+// rounded FP32 adds.  Measured on 128 antennas x 384 channels this keeps the
+// averages within ~5e-7 of the FP64 sums (relative to the sum of |terms|).
+//
+// TMEM (512 columns, one block per SM): RS[0], RS[1] (running sums, double
+// buffered: the epilogue reads one while the next tile accumulates into the
+// other), IS (segments 1.. of the current tile), AC (corrections).  Columns
+// 0..Jw-1 of a region hold sum V_s Re E, columns Jw..2Jw-1 sum V_s Im E.
+//
+// Warp roles (14 warps): 0 = TMA producer, 1 = MMA issuer (+ TMEM owner), 2-5 =
+// converters (split the visibility box into K-major hi/lo blocks, and fold the
+// accumulators), 6-13 = epilogue (warp w reads TMEM lanes 32 (w % 4) ..; two
+// warps per quarter take 32 directions each).  Rings: kGrStages stages of
+// {visibility box, E window} (deep enough to cover HBM latency) and kGrAStages
+// packed A blocks.  Every wait is bounded; a timeout sets the error word, stops
+// every role, and the block still waits (bounded) for its copies and MMAs and
+// frees its TMEM.
+#pragma once
+
+#include "leap_common.cuh"
+#include "kernels_tc.cuh"
+
+namespace leapgb {
+
+constexpr int kGrTaps = 10;           // W, grid points per interpolation
+constexpr float kGrBeta = 23.0f;      // 2.3 W
+constexpr int kGrChunk = 16;          // channels per stage
+constexpr int kGrSegChunks = 4;       // chunks per hi*hi accumulation segment (64 channels)
+constexpr int kGrStages = 5;          // {visibility box, E window} ring
+constexpr int kGrAStages = 3;         // packed A ring
+constexpr int kGrJwMax = 64;          // grid points per pass (MMA N = 2 Jw <= 128)
+constexpr int kGrPassStride = 48;     // grid points between pass windows (multiple of 8)
+constexpr int kGrLoadCols = 16;       // TMEM columns one interpolation load reads
+constexpr int kGrDirs = 64;           // directions per unit (8 epilogue warps x 32 / 4 quarters)
+constexpr int kGrWarps = 14;
+constexpr int kGrThreads = kGrWarps * 32;
+constexpr int kGrVBytes = 32 * 4 * kGrChunk * 4;         // [16 ch][4 t][32 floats]
+constexpr int kGrEBytes = 2 * 2 * 2 * kGrJwMax * 32;     // [hl][ks][2 Jw rows x 32 B]
+constexpr int kGrStageBytes = kGrVBytes + kGrEBytes;
+constexpr int kGrABytes = 2 * 2 * 128 * 32;              // [hl][ks][128 rows x 32 B]
+constexpr int kGrRecWords = 24;                          // per (direction, timestep) record: 16-byte rows
+constexpr int kGrRecBytes = 8 * 8 * 4 * kGrRecWords * 4; // [8 warps][8 dirs][4 t][24]
+constexpr uint32_t kGrRegion = 128;                      // TMEM columns per region
+constexpr uint32_t kGrIS = 2 * kGrRegion, kGrAC = 3 * kGrRegion;
+constexpr int kGrWide = 1 << 16;                         // record flag: the 4 timesteps need separate loads
+constexpr int kGrNumBars = 2 * kGrStages + 2 * kGrAStages + 8;
+
+// A pass window must hold every stencil whose start falls in its stride, plus the
+// columns one load reads past the stencil.
+static_assert(kGrPassStride % 8 == 0 && kGrPassStride - 1 + kGrLoadCols <= kGrJwMax, "pass windows");
+static_assert(kGrTaps + 1 <= kGrLoadCols, "one load per stencil");
+
+__host__ __device__ constexpr int grid_smem_bytes() {
+  return kGrStages * kGrStageBytes + kGrAStages * kGrABytes + kTwiddleSize * 8 + kGrRecBytes + kGrNumBars * 8 + 16;
+}
+
+// Rows of the E table of channel count C: row r is grid point l = r - lbase.
+__host__ __device__ constexpr int grid_lbase(int C) { return ((C + kGrTaps + 8 + 7) / 8) * 8; }
+__host__ __device__ constexpr int grid_rows(int C) { return ((grid_lbase(C) + C + kGrJwMax + 8 + 7) / 8) * 8; }
+__host__ __device__ constexpr int grid_chunks(int C) { return (C + kGrChunk - 1) / kGrChunk; }
+// Floats of the E table: [chunk][ks][hl][re/im][row group][8 rows x 8 k].
+__host__ __device__ constexpr int64_t grid_table_floats(int C) {
+  return static_cast<int64_t>(grid_chunks(C)) * 2 * 2 * 2 * grid_rows(C) * 8;
+}
+
+// One item of a gridded launch (device memory; the tensor map needs 128-byte alignment).
+struct alignas(128) GridItem {
+  CUtensorMap map;       // [channel][timestep][nbl*8 floats], box 32 x 4 x kGrChunk
+  const float* uvw_f;    // [rows][6] split UVWs
+  const float* etab;     // E table of this channel count
+  double2* out;          // nslab == 1: avg + dir0*4*nbl; else this item's [nslab][ndir][4][nbl] partials
+  int32_t T, C, nchunk, tb_per_slab;
+  int32_t nslab, nquad, dgroups, dir0;
+  int32_t ndir, unit_begin, nrg, lbase;
+};
+
+// Grid window of one unit, written by grid_windows: table rows [8 rg0, 8 rg0 + jw)
+// in pass 0, shifted by kGrPassStride per pass.  npass == 0: nothing to do.
+struct GridWindow {
+  int32_t rg0, jw, npass, pad;
+};
+
+struct GridParams {
+  const GridItem* items;
+  const int32_t* order;    // [nslots]: block b visits units order[b], order[b + grid], ... until -1
+  GridWindow* win;         // [units]
+  const float* dirk;       // [ndir_total][12]
+  const float2* twiddle;   // [kTwiddleSize]
+  int* err;
+  int32_t nslots, nitems, units, nbl;
+};
+
+struct GridUnit {
+  int item, quad, dg, slab, t_lo, t_hi, ntb;
+};
+
+__device__ __forceinline__ int grid_find_item(const GridItem* items, int nitems, int u) {
+  int lo = 0, hi = nitems - 1;
+  while (lo < hi) {
+    const int mid = (lo + hi + 1) >> 1;
+    if (__ldg(&items[mid].unit_begin) <= u) lo = mid;
+    else hi = mid - 1;
+  }
+  return lo;
+}
+
+__device__ __forceinline__ GridUnit grid_unit(const GridParams& p, int u) {
+  GridUnit g;
+  g.item = grid_find_item(p.items, p.nitems, u);
+  const GridItem& I = p.items[g.item];
+  const int l = u - I.unit_begin;
+  g.quad = l / (I.dgroups * I.nslab);
+  g.dg = (l / I.nslab) % I.dgroups;
+  g.slab = l % I.nslab;
+  g.t_lo = g.slab * I.tb_per_slab * 4;
+  g.t_hi = min(I.T, g.t_lo + I.tb_per_slab * 4);
+  g.ntb = (g.t_hi - g.t_lo + 3) / 4;
+  return g;
+}
+
+// Grid position n*B of a phase slope B given as a 2^-32 fixed-point fraction of a
+// turn (its signed value is B reduced to [-1/2, 1/2), which leaves exp(2 pi i k B)
+// unchanged for integer k): returns floor(n B), and the fraction in f.
+__device__ __forceinline__ int grid_position(uint32_t pb, int n, float& f) {
+  const long long prod = static_cast<long long>(static_cast<int>(pb)) * n;
+  f = static_cast<float>(static_cast<uint32_t>(prod)) * 2.3283064365386963e-10f;
+  return static_cast<int>(prod >> 32);
+}
+
+__device__ __forceinline__ void tma_load_3d(void* smem_dst, const CUtensorMap* map, int x, int y, int z, uint64_t* bar) {
+  asm volatile(
+      "cp.async.bulk.tensor.3d.shared::cluster.global.tile.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, %4}], [%5];" ::"r"(
+          smem_u32(smem_dst)),
+      "l"(map), "r"(x), "r"(y), "r"(z), "r"(smem_u32(bar))
+      : "memory");
+}
+
+// Bounded wait that also gives up once another role has raised the abort flag.
+// Polls back off with a short sleep so that waiting warps leave the issue slots to
+// the working ones.
+__device__ __forceinline__ bool grid_wait(uint64_t* bar, uint32_t parity, volatile int* abort_flag) {
+  for (uint32_t i = 0; i < kMaxWaitPolls; ++i) {
+    if (mbar_try_wait(bar, parity)) return true;
+    if ((i & 63u) == 63u && *abort_flag) return false;
+    __nanosleep(i < 8 ? 20 : 100);
+  }
+  return false;
+}
+
+__device__ __forceinline__ void grid_fail(const GridParams& p, volatile int* abort_flag) {
+  atomicOr(p.err, kDevErrTimeout);
+  *abort_flag = 1;
+}
+
+// Per unit: the range of interpolation stencil starts over its valid rows and
+// directions, as a window of E-table rows (one warp per unit).
+static __global__ void grid_windows(const GridParams p) {
+  const int u = static_cast<int>((blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x) >> 5);
+  const int lane = threadIdx.x & 31;
+  if (u >= p.units) return;
+  const GridUnit g = grid_unit(p, u);
+  const GridItem& I = p.items[g.item];
+  const int n = 2 * I.C;
+  const int nd = min(kGrDirs, I.ndir - g.dg * kGrDirs);
+  const int nrow = (g.t_hi - g.t_lo) * 4;
+  int smin = 0x7fffffff, smax = -0x7fffffff;
+  for (int e = lane; e < nrow * nd; e += 32) {
+    const int ri = e / nd, dj = e % nd;
+    const int t = g.t_lo + (ri >> 2), b = g.quad * 4 + (ri & 3);
+    if (b >= p.nbl) continue;
+    const int64_t r = static_cast<int64_t>(t) * p.nbl + b;
+    const int d = I.dir0 + g.dg * kGrDirs + dj;
+    float x[6], kb[6];
+#pragma unroll
+    for (int i = 0; i < 6; ++i) {
+      x[i] = __ldg(I.uvw_f + 6 * r + i);
+      kb[i] = __ldg(p.dirk + 12 * d + 6 + i);
+    }
+    float f;
+    const int s = grid_position(df_dot3_turns_u32(kb, x), n, f) - kGrTaps / 2 + 1;
+    smin = min(smin, s);
+    smax = max(smax, s);
+  }
+  smin = __reduce_min_sync(0xffffffffu, smin);
+  smax = __reduce_max_sync(0xffffffffu, smax);
+  if (lane == 0) {
+    GridWindow w{0, 16, 0, 0};
+    if (smin <= smax) {
+      w.rg0 = (smin + I.lbase) >> 3;
+      const int r0 = w.rg0 * 8;
+      // Stencil starts lie in [smin, smax]; a load reads kGrLoadCols columns from a start.
+      const int need = smax + kGrLoadCols + I.lbase - r0;
+      if (need <= kGrJwMax) {
+        w.jw = max(16, (need + 7) & ~7);
+        w.npass = 1;
+      } else {
+        w.jw = kGrJwMax;
+        w.npass = (smax + I.lbase - r0) / kGrPassStride + 1;
+      }
+    }
+    p.win[u] = w;
+  }
+}
+
+template <int W>
+__device__ __forceinline__ void grid_weights(float y, float (&w)[W + 1]) {
+  constexpr float kInvHalf = 2.0f / W;
+  constexpr float kBeta2 = kGrBeta * 1.4426950408889634f;  // beta / ln 2
+#pragma unroll
+  for (int k = 0; k <= W; ++k) {
+    // sqrt(1 - z^2) - 1 = -z^2 / (1 + sqrt(1 - z^2)): no cancellation near the centre.
+    const float z = (y - static_cast<float>(k)) * kInvHalf;
+    const float z2 = z * z;
+    const float q = fmaxf(0.0f, 1.0f - z2);
+    w[k] = exp2f(-kBeta2 * __fdividef(z2, 1.0f + sqrtf(q)));
+  }
+}
+
+// One direction of one lane: W + 1 taps of the grid values at TMEM columns col..,
+// weighted by wt (the lane's record), combined with the partner lane's component,
+// rotated by (cr, sr); returns this lane's component of the rotated sum.
+template <int W>
+__device__ __forceinline__ float grid_tap_sum(uint32_t taddr, int jw, const float (&rj)[W + 3], int comp) {
+  uint32_t vr[16], vi[16];
+  asm volatile(
+      "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];"
+      : "=r"(vr[0]), "=r"(vr[1]), "=r"(vr[2]), "=r"(vr[3]), "=r"(vr[4]), "=r"(vr[5]), "=r"(vr[6]), "=r"(vr[7]),
+        "=r"(vr[8]), "=r"(vr[9]), "=r"(vr[10]), "=r"(vr[11]), "=r"(vr[12]), "=r"(vr[13]), "=r"(vr[14]), "=r"(vr[15])
+      : "r"(taddr)
+      : "memory");
+  asm volatile(
+      "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];"
+      : "=r"(vi[0]), "=r"(vi[1]), "=r"(vi[2]), "=r"(vi[3]), "=r"(vi[4]), "=r"(vi[5]), "=r"(vi[6]), "=r"(vi[7]),
+        "=r"(vi[8]), "=r"(vi[9]), "=r"(vi[10]), "=r"(vi[11]), "=r"(vi[12]), "=r"(vi[13]), "=r"(vi[14]), "=r"(vi[15])
+      : "r"(taddr + static_cast<uint32_t>(jw))
+      : "memory");
+  asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+  float P = 0.f, Q = 0.f;
+#pragma unroll
+  for (int k = 0; k <= W; ++k) {
+    P = fmaf(rj[k], __uint_as_float(vr[k]), P);
+    Q = fmaf(rj[k], __uint_as_float(vi[k]), Q);
+  }
+  // Lane re (comp 0): P = sum Vr ReE, Q = sum Vr ImE; lane im: P = sum Vi ReE, Q = sum Vi ImE.
+  // G = (P_re - Q_im) + i (Q_re + P_im); the lane's component of G * (cr + i sr).
+  const float o = __shfl_xor_sync(0xffffffffu, Q, 1);
+  const float gown = comp ? (o + P) : (P - o);
+  const float o2 = __shfl_xor_sync(0xffffffffu, gown, 1);
+  const float cr = rj[W + 1], sr = rj[W + 2];
+  return comp ? fmaf(o2, sr, gown * cr) : fmaf(-o2, sr, gown * cr);
+}
+
+// A direction whose 4 timesteps need separate grid windows: one load per timestep
+// (rare; kept out of line so that the common path stays small).
+template <int W>
+__device__ __noinline__ float grid_wide_sum(const float* rec_dir, uint32_t tbase, int jw, const float (&rw)[W + 3], int comp,
+                                            int tl, int pp) {
+  float acc = 0.f;
+  for (int tt = 0; tt < 4; ++tt) {
+    const int ct = __float_as_int(reinterpret_cast<const float4*>(rec_dir + tt * kGrRecWords)[3].y);
+    if ((ct & 0xFFFF) == 0xFFFF || ((ct >> 8) & 255) != pp) continue;  // same in every lane
+    const float v = grid_tap_sum<W>(tbase + static_cast<uint32_t>(ct & 255), jw, rw, comp);
+    if (tl == tt) acc += v;
+  }
+  return acc;
+}
+
+// Sum of TMEM regions into the first one, for this warp's 32 lanes and columns
+// [0, ncols): dst = a (+ b) (+ c), rounded FP32 adds.
+__device__ __forceinline__ void grid_fold(uint32_t lanes, uint32_t dst, uint32_t b, uint32_t c, bool use_b, bool use_c,
+                                          int ncols) {
+  for (int c0 = 0; c0 < ncols; c0 += 16) {
+    uint32_t x[16], y[16], z[16];
+    asm volatile(
+        "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];"
+        : "=r"(x[0]), "=r"(x[1]), "=r"(x[2]), "=r"(x[3]), "=r"(x[4]), "=r"(x[5]), "=r"(x[6]), "=r"(x[7]), "=r"(x[8]),
+          "=r"(x[9]), "=r"(x[10]), "=r"(x[11]), "=r"(x[12]), "=r"(x[13]), "=r"(x[14]), "=r"(x[15])
+        : "r"(lanes + dst + c0)
+        : "memory");
+    if (use_b)
+      asm volatile(
+          "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];"
+          : "=r"(y[0]), "=r"(y[1]), "=r"(y[2]), "=r"(y[3]), "=r"(y[4]), "=r"(y[5]), "=r"(y[6]), "=r"(y[7]), "=r"(y[8]),
+            "=r"(y[9]), "=r"(y[10]), "=r"(y[11]), "=r"(y[12]), "=r"(y[13]), "=r"(y[14]), "=r"(y[15])
+          : "r"(lanes + b + c0)
+          : "memory");
+    if (use_c)
+      asm volatile(
+          "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];"
+          : "=r"(z[0]), "=r"(z[1]), "=r"(z[2]), "=r"(z[3]), "=r"(z[4]), "=r"(z[5]), "=r"(z[6]), "=r"(z[7]), "=r"(z[8]),
+            "=r"(z[9]), "=r"(z[10]), "=r"(z[11]), "=r"(z[12]), "=r"(z[13]), "=r"(z[14]), "=r"(z[15])
+          : "r"(lanes + c + c0)
+          : "memory");
+    asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+#pragma unroll
+    for (int i = 0; i < 16; ++i) {
+      float v = __uint_as_float(x[i]);
+      if (use_b) v += __uint_as_float(y[i]);
+      if (use_c) v += __uint_as_float(z[i]);
+      x[i] = __float_as_uint(v);
+    }
+    asm volatile(
+        "tcgen05.st.sync.aligned.32x32b.x16.b32 [%0], {%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,%16};" ::"r"(
+            lanes + dst + c0),
+        "r"(x[0]), "r"(x[1]), "r"(x[2]), "r"(x[3]), "r"(x[4]), "r"(x[5]), "r"(x[6]), "r"(x[7]), "r"(x[8]), "r"(x[9]),
+        "r"(x[10]), "r"(x[11]), "r"(x[12]), "r"(x[13]), "r"(x[14]), "r"(x[15])
+        : "memory");
+  }
+  asm volatile("tcgen05.wait::st.sync.aligned;" ::: "memory");
+}
+
+__device__ __forceinline__ void tc_commit(uint64_t* bar) {
+  asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(smem_u32(bar))
+               : "memory");
+}
+
+template <int W>
+__global__ void __launch_bounds__(kGrThreads, 1) rotate_average_gridded(const GridParams p) {
+  extern __shared__ __align__(128) unsigned char grid_smem[];
+  unsigned char* smem = grid_smem;
+  unsigned char* ve = smem;                                          // [kGrStages][V | E]
+  unsigned char* abuf = smem + kGrStages * kGrStageBytes;            // [kGrAStages][hl][ks][128 x 32 B]
+  float2* tab = reinterpret_cast<float2*>(abuf + kGrAStages * kGrABytes);
+  float* rec_all = reinterpret_cast<float*>(tab + kTwiddleSize);
+  uint64_t* bars = reinterpret_cast<uint64_t*>(rec_all + kGrRecBytes / 4);
+  uint64_t* vfull = bars;                      // [kGrStages] TMA bytes landed
+  uint64_t* vempty = vfull + kGrStages;        // [kGrStages] converters read V and the MMAs read E
+  uint64_t* afull = vempty + kGrStages;        // [kGrAStages] converters wrote the A blocks
+  uint64_t* aempty = afull + kGrAStages;       // [kGrAStages] MMAs that read them completed
+  uint64_t* is_full = aempty + kGrAStages;     // a middle segment is complete in IS
+  uint64_t* is_empty = is_full + 1;            // ... and was folded into RS
+  uint64_t* blk_full = is_empty + 1;           // every MMA of a tile completed
+  uint64_t* ac_free = blk_full + 1;            // final fold of a tile done: IS and AC reusable
+  uint64_t* rs_full = ac_free + 1;             // [2] running sum final: epilogue may read
+  uint64_t* rs_free = rs_full + 2;             // [2] epilogue finished reading
+  uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(bars + kGrNumBars);
+  volatile int* abort_flag = reinterpret_cast<volatile int*>(tmem_slot + 1);
+
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  for (int i = threadIdx.x; i < kTwiddleSize; i += blockDim.x) tab[i] = __ldg(p.twiddle + i);
+  if (warp == 1) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(tmem_slot)), "r"(512)
+                 : "memory");
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+  }
+  if (threadIdx.x == 0) {
+    for (int i = 0; i < kGrStages; ++i) {
+      mbar_init(&vfull[i], 1);
+      mbar_init(&vempty[i], 5);  // 4 converter warps + 1 MMA commit
+    }
+    for (int i = 0; i < kGrAStages; ++i) {
+      mbar_init(&afull[i], 4);
+      mbar_init(&aempty[i], 1);
+    }
+    mbar_init(is_full, 1);
+    mbar_init(is_empty, 4);
+    mbar_init(blk_full, 1);
+    mbar_init(ac_free, 4);
+    for (int i = 0; i < 2; ++i) {
+      mbar_init(&rs_full[i], 4);
+      mbar_init(&rs_free[i], 8);
+    }
+    fence_mbar_init();
+    *abort_flag = 0;
+  }
+  asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+  __syncthreads();
+  asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+  const uint32_t tmem = *tmem_slot;
+
+  if (warp == 0) {
+    // ---------------- producer ----------------
+    if (lane == 0) {
+      uint32_t ctr = 0;
+      bool ok = true;
+      for (int sl = blockIdx.x; ok; sl += gridDim.x) {
+        const int u = sl < p.nslots ? __ldg(p.order + sl) : -1;
+        if (u < 0) break;
+        const GridUnit g = grid_unit(p, u);
+        const GridItem& I = p.items[g.item];
+        const GridWindow w = p.win[u];
+        for (int tb = 0; tb < g.ntb && ok; ++tb)
+          for (int ps = 0; ps < w.npass && ok; ++ps)
+            for (int q = 0; q < I.nchunk; ++q, ++ctr) {
+              const int s = ctr % kGrStages;
+              if (ctr >= kGrStages && !grid_wait(&vempty[s], ((ctr / kGrStages) - 1) & 1, abort_flag)) {
+                grid_fail(p, abort_flag);
+                ok = false;
+                break;
+              }
+              unsigned char* st = ve + s * kGrStageBytes;
+              mbar_arrive_expect_tx(&vfull[s], kGrVBytes + 8 * w.jw * 32);
+              tma_load_3d(st, &I.map, g.quad * 32, g.t_lo + tb * 4, q * kGrChunk, &vfull[s]);
+              const int rg = w.rg0 + ps * (kGrPassStride / 8);
+#pragma unroll
+              for (int ks = 0; ks < 2; ++ks)
+#pragma unroll
+                for (int hl = 0; hl < 2; ++hl)
+#pragma unroll
+                  for (int ri = 0; ri < 2; ++ri) {
+                    const float* src = I.etab + ((static_cast<int64_t>(((q * 2 + ks) * 2 + hl) * 2 + ri) * I.nrg) + rg) * 64;
+                    bulk_copy_g2s(st + kGrVBytes + ((hl * 2 + ks) * 2 * w.jw + ri * w.jw) * 32, src, w.jw * 32, &vfull[s]);
+                  }
+            }
+      }
+      // Do not leave while copies issued by this block may still land.
+      for (uint32_t j = (ctr > kGrStages ? ctr - kGrStages : 0); j < ctr; ++j)
+        if (!mbar_wait_bounded(&vfull[j % kGrStages], (j / kGrStages) & 1)) atomicOr(p.err, kDevErrTimeout);
+    }
+  } else if (warp == 1) {
+    // ---------------- MMA issuer ----------------
+    if (lane == 0) {
+      uint32_t ctr = 0, blk = 0, mids = 0;
+      bool ok = true, issued = false;
+      for (int sl = blockIdx.x; ok; sl += gridDim.x) {
+        const int u = sl < p.nslots ? __ldg(p.order + sl) : -1;
+        if (u < 0) break;
+        const GridUnit g = grid_unit(p, u);
+        const GridItem& I = p.items[g.item];
+        const GridWindow w = p.win[u];
+        const uint32_t idesc = tc_idesc_tf32(128, 2 * w.jw);
+        for (int tb = 0; tb < g.ntb && ok; ++tb)
+          for (int ps = 0; ps < w.npass && ok; ++ps, ++blk) {
+            const uint32_t b = blk & 1;
+            if ((blk >= 2 && !grid_wait(&rs_free[b], ((blk >> 1) - 1) & 1, abort_flag)) ||
+                (blk >= 1 && !grid_wait(ac_free, (blk - 1) & 1, abort_flag))) {
+              grid_fail(p, abort_flag);
+              ok = false;
+              break;
+            }
+            asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+            const uint32_t rs = tmem + b * kGrRegion;
+            for (int q = 0; q < I.nchunk; ++q, ++ctr) {
+              const int s = ctr % kGrStages, a = ctr % kGrAStages;
+              const int seg = q / kGrSegChunks, qs = q % kGrSegChunks;
+              if (!grid_wait(&vfull[s], (ctr / kGrStages) & 1, abort_flag) ||
+                  !grid_wait(&afull[a], (ctr / kGrAStages) & 1, abort_flag)) {
+                grid_fail(p, abort_flag);
+                ok = false;
+                break;
+              }
+              asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+              const unsigned char* eb = ve + s * kGrStageBytes + kGrVBytes;
+              const unsigned char* ab = abuf + a * kGrABytes;
+              uint64_t ah[2], al[2], bh[2], bl[2];
+#pragma unroll
+              for (int ks = 0; ks < 2; ++ks) {
+                ah[ks] = tc_smem_desc(ab + (0 * 2 + ks) * 4096, kTcLbo, kTcSbo);
+                al[ks] = tc_smem_desc(ab + (1 * 2 + ks) * 4096, kTcLbo, kTcSbo);
+                bh[ks] = tc_smem_desc(eb + (0 * 2 + ks) * 2 * w.jw * 32, kTcLbo, kTcSbo);
+                bl[ks] = tc_smem_desc(eb + (1 * 2 + ks) * 2 * w.jw * 32, kTcLbo, kTcSbo);
+              }
+              // Corrections first: they give the fold of the previous segment time to finish.
+#pragma unroll
+              for (int ks = 0; ks < 2; ++ks) {
+                tc_mma_tf32(tmem + kGrAC, al[ks], bh[ks], idesc, (q > 0 || ks > 0) ? 1u : 0u);
+                tc_mma_tf32(tmem + kGrAC, ah[ks], bl[ks], idesc, 1u);
+              }
+              if (seg >= 2 && qs == 0 && !grid_wait(is_empty, (mids - 1) & 1, abort_flag)) {
+                grid_fail(p, abort_flag);
+                ok = false;
+                break;
+              }
+              const uint32_t dst = seg == 0 ? rs : tmem + kGrIS;
+#pragma unroll
+              for (int ks = 0; ks < 2; ++ks) tc_mma_tf32(dst, ah[ks], bh[ks], idesc, (qs > 0 || ks > 0) ? 1u : 0u);
+              issued = true;
+              tc_commit(&vempty[s]);
+              tc_commit(&aempty[a]);
+              if (seg >= 1 && qs == kGrSegChunks - 1 && q != I.nchunk - 1) {
+                tc_commit(is_full);  // a middle segment, folded by the converters
+                ++mids;
+              }
+            }
+            if (ok) tc_commit(blk_full);
+          }
+      }
+      // No MMA of this block may be in flight when its TMEM is freed.
+      if (issued) {
+        const uint32_t j = ctr - 1;
+        if (!mbar_wait_bounded(&aempty[j % kGrAStages], (j / kGrAStages) & 1)) atomicOr(p.err, kDevErrTimeout);
+      }
+    }
+  } else if (warp < 6) {
+    // ---------------- converters: visibility box -> K-major hi/lo A blocks; folds ----------------
+    const int cw = warp - 2;
+    const uint32_t lanes = static_cast<uint32_t>((warp & 3) * 32) << 16;
+    uint32_t ctr = 0, blk = 0, mids = 0;
+    bool ok = true;
+    for (int sl = blockIdx.x; ok; sl += gridDim.x) {
+      const int u = sl < p.nslots ? __ldg(p.order + sl) : -1;
+      if (u < 0) break;
+      const GridUnit g = grid_unit(p, u);
+      const GridItem& I = p.items[g.item];
+      const GridWindow w = p.win[u];
+      const int nseg = (I.nchunk + kGrSegChunks - 1) / kGrSegChunks;
+      for (int tb = 0; tb < g.ntb && ok; ++tb)
+        for (int ps = 0; ps < w.npass && ok; ++ps, ++blk) {
+          const uint32_t b = blk & 1;
+          for (int q = 0; q < I.nchunk; ++q, ++ctr) {
+            const int s = ctr % kGrStages, a = ctr % kGrAStages;
+            if (!grid_wait(&vfull[s], (ctr / kGrStages) & 1, abort_flag) ||
+                (ctr >= kGrAStages && !grid_wait(&aempty[a], ((ctr / kGrAStages) - 1) & 1, abort_flag))) {
+              grid_fail(p, abort_flag);
+              ok = false;
+              break;
+            }
+            const float* vb = reinterpret_cast<const float*>(ve + s * kGrStageBytes);
+            unsigned char* ab = abuf + a * kGrABytes;
+#pragma unroll
+            for (int bi = 0; bi < 4; ++bi) {
+              const int blk4 = cw + 4 * bi;  // 16 blocks of (4 channels, 1 timestep)
+              const int cg = blk4 >> 2, tl = blk4 & 3;
+              float4 hi, lo;
+              float x[4];
+#pragma unroll
+              for (int j = 0; j < 4; ++j) x[j] = vb[(cg * 4 + j) * 128 + tl * 32 + lane];
+              hi.x = to_tf32(x[0]);
+              hi.y = to_tf32(x[1]);
+              hi.z = to_tf32(x[2]);
+              hi.w = to_tf32(x[3]);
+              lo.x = to_tf32(x[0] - hi.x);
+              lo.y = to_tf32(x[1] - hi.y);
+              lo.z = to_tf32(x[2] - hi.z);
+              lo.w = to_tf32(x[3] - hi.w);
+              const int m = (lane >> 3) * 32 + tl * 8 + (lane & 7);  // TMEM lane: baseline, timestep, pol, re/im
+              const int k = cg * 4;                                  // 0..15 within the chunk
+              const int off = (k >> 3) * 4096 + (((m >> 3) << 1) + ((k >> 2) & 1)) * 128 + (m & 7) * 16;
+              *reinterpret_cast<float4*>(ab + off) = hi;
+              *reinterpret_cast<float4*>(ab + 2 * 4096 + off) = lo;
+            }
+            asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+            __syncwarp();
+            if (lane == 0) {
+              mbar_arrive(&afull[a]);
+              mbar_arrive(&vempty[s]);
+            }
+            // Fold middle segment sg (1 <= sg <= nseg - 2) into RS once the next segment's
+            // second chunk is converted (its first if it has only one).
+            const int seg = q / kGrSegChunks, qs = q % kGrSegChunks;
+            const int nxt = min(kGrSegChunks, I.nchunk - seg * kGrSegChunks);
+            const int sg = seg - 1;
+            if (sg >= 1 && sg <= nseg - 2 && qs == min(1, nxt - 1)) {
+              if (!grid_wait(is_full, mids & 1, abort_flag)) {
+                grid_fail(p, abort_flag);
+                ok = false;
+                break;
+              }
+              asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+              grid_fold(lanes, tmem + b * kGrRegion, tmem + kGrIS, 0, true, false, 2 * w.jw);
+              asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+              __syncwarp();
+              if (lane == 0) mbar_arrive(is_empty);
+              ++mids;
+            }
+          }
+          if (!ok) break;
+          // Final fold: RS += last segment (if any beyond the first) + corrections.
+          if ((blk >= 2 && !grid_wait(&rs_free[b], ((blk >> 1) - 1) & 1, abort_flag)) ||
+              !grid_wait(blk_full, blk & 1, abort_flag)) {
+            grid_fail(p, abort_flag);
+            ok = false;
+            break;
+          }
+          asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+          grid_fold(lanes, tmem + b * kGrRegion, tmem + kGrIS, tmem + kGrAC, nseg >= 2, true, 2 * w.jw);
+          asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+          __syncwarp();
+          if (lane == 0) {
+            mbar_arrive(ac_free);
+            mbar_arrive(&rs_full[b]);
+          }
+        }
+    }
+  } else {
+    // ---------------- epilogue: interpolate, rotate, accumulate ----------------
+    const int e = warp - 6;
+    const int half = e >> 2;       // which 32 directions of the unit
+    const int quarter = warp & 3;  // TMEM lanes 32*quarter .. (hardware rule: warp id mod 4)
+    const int tl = lane >> 3, ps = lane & 7, comp = lane & 1;
+    float* rec = rec_all + e * (8 * 4 * kGrRecWords);
+    uint32_t blk = 0;
+    bool ok = true;
+    for (int sl = blockIdx.x; ok; sl += gridDim.x) {
+      const int u = sl < p.nslots ? __ldg(p.order + sl) : -1;
+      if (u < 0) break;
+      const GridUnit g = grid_unit(p, u);
+      const GridItem& I = p.items[g.item];
+      const GridWindow w = p.win[u];
+      if (w.npass == 0) continue;
+      const int n = 2 * I.C, c0 = I.C / 2;
+      const int r0 = w.rg0 * 8;
+      const int dbase = g.dg * kGrDirs + half * 32;  // item-relative first direction of this warp
+      const int nd = max(0, min(32, I.ndir - dbase));
+      const int b = g.quad * 4 + quarter;
+      const bool bval = b < p.nbl;
+      float acc[32];
+#pragma unroll
+      for (int j = 0; j < 32; ++j) acc[j] = 0.f;
+      for (int tb = 0; tb < g.ntb && ok; ++tb) {
+        const int t = g.t_lo + tb * 4 + tl;
+        const bool rval = bval && t < g.t_hi;
+        const int64_t r = rval ? static_cast<int64_t>(t) * p.nbl + b : 0;
+        float x[6];
+#pragma unroll
+        for (int i = 0; i < 6; ++i) x[i] = __ldg(I.uvw_f + 6 * r + i);
+        for (int pp = 0; pp < w.npass; ++pp, ++blk) {
+          const uint32_t rb = blk & 1;
+          if (!grid_wait(&rs_full[rb], (blk >> 1) & 1, abort_flag)) {
+            grid_fail(p, abort_flag);
+            ok = false;
+            break;
+          }
+          asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+          const uint32_t tbase = tmem + (static_cast<uint32_t>(quarter * 32) << 16) + rb * kGrRegion;
+#pragma unroll
+          for (int gi = 0; gi < 4; ++gi) {
+            if (gi * 8 >= nd) break;
+            {
+              // This lane's record: direction gi*8 + ps at timestep tl.
+              const int dj = gi * 8 + ps;
+              const bool dv = dj < nd;
+              const int d = I.dir0 + dbase + min(dj, nd - 1);
+              float ka[6], kb[6];
+#pragma unroll
+              for (int i = 0; i < 6; ++i) {
+                ka[i] = __ldg(p.dirk + 12 * d + i);
+                kb[i] = __ldg(p.dirk + 12 * d + 6 + i);
+              }
+              const uint32_t pa = df_dot3_turns_u32(ka, x);
+              const uint32_t pb = df_dot3_turns_u32(kb, x);
+              float f;
+              const int i0 = grid_position(pb, n, f);
+              const int st = i0 - W / 2 + 1;  // this row's stencil start
+              const int sl0 = rval ? st : 0x7fffffff, sh0 = rval ? st : -0x7fffffff;
+              int cw = min(sl0, __shfl_xor_sync(0xffffffffu, sl0, 8));
+              cw = min(cw, __shfl_xor_sync(0xffffffffu, cw, 16));
+              int cm = max(sh0, __shfl_xor_sync(0xffffffffu, sh0, 8));
+              cm = max(cm, __shfl_xor_sync(0xffffffffu, cm, 16));
+              const bool any = cw != 0x7fffffff;
+              // Normally the 4 timesteps' stencils start within one grid point of each other and
+              // share one load from the earliest start; otherwise each timestep loads its own.
+              const bool wide = any && cm - cw > 1;  // W + 1 taps from cw cover starts cw and cw + 1
+              const int base = wide ? st : cw;
+              int code = -1;
+              if (dv && any) {
+                if (wide && !rval) {
+                  code = kGrWide | 0xFFFF;
+                } else {
+                  const int rr = base + I.lbase - r0;
+                  const int pass = w.npass == 1 ? 0 : rr / kGrPassStride;
+                  code = (wide ? kGrWide : 0) | (pass << 8) | (rr - pass * kGrPassStride);
+                }
+              }
+              float wt[W + 1];
+              grid_weights<W>(any ? static_cast<float>(i0 - base) + f : 0.f, wt);
+              float cr, sr;
+              twiddle_turns(pa + static_cast<uint32_t>(c0) * pb, tab, cr, sr);
+              float4* my = reinterpret_cast<float4*>(rec + (ps * 4 + tl) * kGrRecWords);
+              my[0] = make_float4(wt[0], wt[1], wt[2], wt[3]);
+              my[1] = make_float4(wt[4], wt[5], wt[6], wt[7]);
+              my[2] = make_float4(wt[8], wt[9], wt[10], cr);
+              my[3] = make_float4(sr, __int_as_float(code), 0.f, 0.f);
+            }
+            __syncwarp();
+#pragma unroll
+            for (int jj = 0; jj < 8; ++jj) {
+              const float4* rq = reinterpret_cast<const float4*>(rec + (jj * 4 + tl) * kGrRecWords);
+              const float4 q3 = rq[3];
+              const int code = __float_as_int(q3.y);  // same in every lane
+              if (code < 0) continue;
+              const float4 q0 = rq[0], q1 = rq[1], q2 = rq[2];
+              const float rw[W + 3] = {q0.x, q0.y, q0.z, q0.w, q1.x, q1.y, q1.z, q1.w, q2.x, q2.y, q2.z, q2.w, q3.x};
+              if (!(code & kGrWide)) {
+                if (((code >> 8) & 255) != pp) continue;
+                acc[gi * 8 + jj] += grid_tap_sum<W>(tbase + static_cast<uint32_t>(code & 255), w.jw, rw, comp);
+              } else {
+                acc[gi * 8 + jj] += grid_wide_sum<W>(rec + jj * 4 * kGrRecWords, tbase, w.jw, rw, comp, tl, pp);
+              }
+            }
+            __syncwarp();
+          }
+          asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+          __syncwarp();
+          if (lane == 0) mbar_arrive(&rs_free[rb]);
+        }
+      }
+      if (!ok) break;
+      // Sum the 4 timesteps of the quad's lanes and write this unit's sums.
+      double2* out = I.out + static_cast<int64_t>(I.nslab > 1 ? g.slab : 0) * I.ndir * 4 * p.nbl;
+#pragma unroll
+      for (int j = 0; j < 32; ++j) {
+        float v = acc[j] + __shfl_xor_sync(0xffffffffu, acc[j], 8);
+        v += __shfl_xor_sync(0xffffffffu, v, 16);
+        if (tl == 0 && bval && j < nd) {
+          double* o = reinterpret_cast<double*>(out + (static_cast<int64_t>(dbase + j) * 4 + (ps >> 1)) * p.nbl + b);
+          o[comp] = static_cast<double>(v);
+        }
+      }
+    }
+  }
+  asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+  __syncthreads();
+  if (warp == 1) {
+    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(512) : "memory");
+  }
+}
+
+}  // namespace leapgb

@@ -23,6 +23,7 @@
 #include "kernels_ingest.cuh"
 #include "kernels_metadata.cuh"
 #include "kernels_mma.cuh"
+#include "kernels_grid.cuh"
 
 using namespace leapgb;
 
@@ -66,6 +67,8 @@ struct Integration {
   int32_t channels = 0, pols = 0;
   bool has_map = false;
   CUtensorMap map16, map8;  // [channel][row*8 floats] views of a 4-pol complex<float> integration, box heights 16 / 8
+  CUtensorMap map_g;        // [channel][timestep][nbl*8 floats] view for the gridded kernel (built on first use)
+  int32_t map_g_nbl = 0;    // baseline count map_g was built for (0: none)
   // Asynchronous ingestion: the upload runs on the context's copy stream and `ready`
   // marks its end; calibrate calls make their stream wait for it.
   cudaEvent_t ready = nullptr;
@@ -112,6 +115,12 @@ struct leap_ctx {
   bool autotune = true;               // tune new batched shapes on first use
   bool tc_gemm = true;                // mixed form: Ad contraction on the tensor cores (3xTF32)
   int mma_rotate = 1;                 // tensor-core rotate + average: 0 never, 1 autotuner candidate, 2 always
+  int gridded = 0;                    // gridded rotate + average (tcgen05 grid product): 0 off, 1 on
+  bool grid_attr = false;
+  std::map<int, DeviceBuffer> grid_tabs;  // grid matrix per channel count
+  std::vector<GridItem> grid_items_host;
+  std::vector<int32_t> grid_order_host;
+  DeviceBuffer grid_items, grid_order, grid_win;
   bool pipe_attr_mma = false;
   int tc_attr_set = 0;                // bit per N tile whose shared-memory size was raised
   DeviceBuffer dphi_tc;               // packed dphi operand of the tensor-core contraction
@@ -258,6 +267,174 @@ struct WorkItem {
   int32_t slot, dir0, ndir;
 };
 
+// Grid matrix of the gridded kernel for C channels (built once per channel count).
+const float* grid_table_for(leap_ctx* ctx, int C) {
+  auto it = ctx->grid_tabs.find(C);
+  if (it != ctx->grid_tabs.end()) return it->second.as<float>();
+  if (ctx->capturing) return nullptr;
+  std::vector<float> tab;
+  grid_table(C, kGrTaps, kGrBeta, grid_lbase(C), grid_rows(C), tab);
+  DeviceBuffer& b = ctx->grid_tabs[C];
+  if (b.ensure(sizeof(float) * tab.size()) != cudaSuccess) return nullptr;
+  if (cudaMemcpy(b.ptr, tab.data(), sizeof(float) * tab.size(), cudaMemcpyHostToDevice) != cudaSuccess) return nullptr;
+  return b.as<float>();
+}
+
+// Rotate + average of every item through the gridded kernel (4-pol complex<float>
+// integrations with a tensor map): a window pass over the units, then one
+// persistent launch, then the slab reduction where items were split.
+int gridded_stage(leap_ctx* ctx, const std::vector<WorkItem>& items, const double* d_dd, int32_t D, cudaStream_t s,
+                  int& kernels) {
+  Metadata& md = ctx->md;
+  const int32_t nbl = static_cast<int32_t>(md.k.nbaselines);
+  const int nquad = (nbl + 3) / 4;
+  auto enc = tensor_map_encoder();
+  if (!enc) return fail(ctx, LEAP_ERR_CUDA, "cuTensorMapEncodeTiled unavailable");
+  std::vector<GridItem>& git = ctx->grid_items_host;
+  std::vector<ReduceItem>& red = ctx->reduce_items_host;
+  git.assign(items.size(), GridItem{});
+  red.clear();
+  int64_t base_units = 0;
+  for (const auto& w : items) base_units += static_cast<int64_t>(nquad) * ((w.ndir + kGrDirs - 1) / kGrDirs);
+  // Timestep slabs only when the (quad, direction group) units alone would leave blocks idle.
+  const int64_t want_slabs = std::max<int64_t>(1, (4 * static_cast<int64_t>(ctx->sms) + base_units - 1) / base_units);
+  int units = 0;
+  int64_t partial_elems = 0;
+  std::vector<int64_t> partial_off(items.size(), -1);
+  for (size_t i = 0; i < items.size(); ++i) {
+    const WorkItem& w = items[i];
+    Integration& in = ctx->integ.at(w.slot);
+    const int T = static_cast<int>(in.rows / nbl);
+    const int C = in.channels;
+    if (in.map_g_nbl != nbl) {
+      cuuint64_t dims[3] = {static_cast<cuuint64_t>(nbl) * 8, static_cast<cuuint64_t>(T), static_cast<cuuint64_t>(C)};
+      cuuint64_t strides[2] = {static_cast<cuuint64_t>(nbl) * 32, static_cast<cuuint64_t>(in.rows) * 32};
+      cuuint32_t box[3] = {32, 4, static_cast<cuuint32_t>(kGrChunk)};
+      cuuint32_t estr[3] = {1, 1, 1};
+      CUresult r = enc(&in.map_g, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 3, in.vis.ptr, dims, strides, box, estr,
+                       CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+                       CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+      if (r != CUDA_SUCCESS) return fail(ctx, LEAP_ERR_CUDA, "cuTensorMapEncodeTiled (3-D) failed: " + std::to_string(r));
+      in.map_g_nbl = nbl;
+    }
+    const float* tab = grid_table_for(ctx, C);
+    if (!tab) return fail(ctx, LEAP_ERR_CUDA, "grid matrix unavailable for this channel count");
+    GridItem& it = git[i];
+    it.map = in.map_g;
+    it.uvw_f = in.uvw_f.as<float>();
+    it.etab = tab;
+    it.T = T;
+    it.C = C;
+    it.nchunk = grid_chunks(C);
+    const int ntb = (T + 3) / 4;
+    const int nslab_want = static_cast<int>(std::min<int64_t>(ntb, want_slabs));
+    it.tb_per_slab = (ntb + nslab_want - 1) / nslab_want;
+    it.nslab = (ntb + it.tb_per_slab - 1) / it.tb_per_slab;
+    it.nquad = nquad;
+    it.dgroups = (w.ndir + kGrDirs - 1) / kGrDirs;
+    it.dir0 = w.dir0;
+    it.ndir = w.ndir;
+    it.unit_begin = units;
+    it.nrg = grid_rows(C) / 8;
+    it.lbase = grid_lbase(C);
+    units += it.nquad * it.dgroups * it.nslab;
+    if (it.nslab > 1) {
+      partial_off[i] = partial_elems;
+      partial_elems += static_cast<int64_t>(it.nslab) * w.ndir * 4 * nbl;
+    }
+  }
+  if (units == 0) return LEAP_OK;
+  if (partial_elems) LEAP_CUDA(ctx->partial.ensure(sizeof(double2) * partial_elems), "alloc partial sums");
+  for (size_t i = 0; i < items.size(); ++i) {
+    GridItem& it = git[i];
+    if (it.nslab > 1) {
+      it.out = ctx->partial.as<double2>() + partial_off[i];
+      red.push_back(ReduceItem{it.out, static_cast<int64_t>(it.dir0) * 4 * nbl, it.nslab, it.ndir});
+    } else {
+      it.out = ctx->avg.as<double2>() + static_cast<int64_t>(it.dir0) * 4 * nbl;
+    }
+  }
+  // Longest unit first, each to the least-loaded block (cost: timestep blocks x chunks).
+  const int grid = std::min(units, ctx->sms);
+  {
+    std::vector<std::pair<int64_t, int>> cost;
+    cost.reserve(units);
+    for (const GridItem& it : git) {
+      const int per_item = it.nquad * it.dgroups * it.nslab;
+      for (int l = 0; l < per_item; ++l) {
+        const int slab = l % it.nslab;
+        const int t_lo = slab * it.tb_per_slab * 4, t_hi = std::min(it.T, t_lo + it.tb_per_slab * 4);
+        cost.emplace_back(-static_cast<int64_t>((t_hi - t_lo + 3) / 4) * (it.nchunk + 2), it.unit_begin + l);
+      }
+    }
+    std::stable_sort(cost.begin(), cost.end());
+    std::vector<std::vector<int32_t>> lists(grid);
+    std::priority_queue<std::pair<int64_t, int>, std::vector<std::pair<int64_t, int>>, std::greater<>> load;
+    for (int b = 0; b < grid; ++b) load.emplace(0, b);
+    for (const auto& c : cost) {
+      auto [l, b] = load.top();
+      load.pop();
+      lists[b].push_back(c.second);
+      load.emplace(l - c.first, b);
+    }
+    size_t rounds = 0;
+    for (const auto& l : lists) rounds = std::max(rounds, l.size());
+    std::vector<int32_t>& order = ctx->grid_order_host;
+    order.assign(rounds * grid + grid, -1);
+    for (int b = 0; b < grid; ++b)
+      for (size_t k = 0; k < lists[b].size(); ++k) order[k * grid + b] = lists[b][k];
+    LEAP_CUDA(ctx->grid_order.ensure(sizeof(int32_t) * order.size()), "alloc unit order");
+    if (!ctx->capturing)
+      LEAP_CUDA(cudaMemcpyAsync(ctx->grid_order.ptr, order.data(), sizeof(int32_t) * order.size(),
+                                cudaMemcpyHostToDevice, s),
+                "upload unit order");
+  }
+  LEAP_CUDA(ctx->grid_items.ensure(sizeof(GridItem) * git.size()), "alloc item table");
+  LEAP_CUDA(ctx->grid_win.ensure(sizeof(GridWindow) * units), "alloc grid windows");
+  if (!ctx->capturing)
+    LEAP_CUDA(cudaMemcpyAsync(ctx->grid_items.ptr, git.data(), sizeof(GridItem) * git.size(), cudaMemcpyHostToDevice, s),
+              "upload item table");
+  if (!red.empty() && !ctx->capturing) {
+    LEAP_CUDA(ctx->reduce_items.ensure(sizeof(ReduceItem) * red.size()), "alloc reduce table");
+    LEAP_CUDA(cudaMemcpyAsync(ctx->reduce_items.ptr, red.data(), sizeof(ReduceItem) * red.size(),
+                              cudaMemcpyHostToDevice, s),
+              "upload reduce table");
+  }
+  direction_constants<<<(D + 63) / 64, 64, 0, s>>>(d_dd, D, md.k.freq_start_hz, md.k.freq_inc_hz,
+                                                   ctx->dirk.as<float>());
+  ++kernels;
+  GridParams gp{};
+  gp.items = ctx->grid_items.as<GridItem>();
+  gp.order = ctx->grid_order.as<int32_t>();
+  gp.win = ctx->grid_win.as<GridWindow>();
+  gp.dirk = ctx->dirk.as<float>();
+  gp.twiddle = ctx->twiddle.as<float2>();
+  gp.err = ctx->dev_err.as<int>();
+  gp.nslots = static_cast<int32_t>(ctx->grid_order_host.size());
+  gp.nitems = static_cast<int32_t>(git.size());
+  gp.units = units;
+  gp.nbl = nbl;
+  grid_windows<<<static_cast<unsigned>((static_cast<int64_t>(units) * 32 + 255) / 256), 256, 0, s>>>(gp);
+  ++kernels;
+  if (!ctx->grid_attr) {
+    LEAP_CUDA(cudaFuncSetAttribute(rotate_average_gridded<kGrTaps>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                   grid_smem_bytes()),
+              "set shared memory size");
+    ctx->grid_attr = true;
+  }
+  rotate_average_gridded<kGrTaps><<<grid, kGrThreads, grid_smem_bytes(), s>>>(gp);
+  ++kernels;
+  if (!red.empty()) {
+    int64_t maxn = 0;
+    for (const auto& r : red) maxn = std::max<int64_t>(maxn, static_cast<int64_t>(r.ndir) * 4 * nbl);
+    const dim3 rg(static_cast<unsigned>(std::min<int64_t>((maxn + 255) / 256, 1024)), static_cast<unsigned>(red.size()));
+    reduce_item_slabs<<<rg, 256, 0, s>>>(ctx->reduce_items.as<ReduceItem>(), static_cast<int>(red.size()), 4 * nbl,
+                                          ctx->avg.as<double2>());
+    ++kernels;
+  }
+  return LEAP_OK;
+}
+
 // Rotate + average of every item into ctx->avg ([D][P][nbl]).
 int rotate_stage(leap_ctx* ctx, const std::vector<WorkItem>& items, const double* d_dd, int32_t D, int32_t precision,
                  int P, cudaStream_t s, int& kernels) {
@@ -286,6 +463,7 @@ int rotate_stage(leap_ctx* ctx, const std::vector<WorkItem>& items, const double
               "upload wavelengths");
   }
 
+  if (all_pipe && ctx->gridded) return gridded_stage(ctx, items, d_dd, D, s, kernels);
   if (all_pipe) {
     // Kernel: the tensor-core one (16 directions per unit) when the autotuner chose it or the
     // option forces it (items of at least 12 directions); else the CUDA-core one with 4 tiles
@@ -788,7 +966,7 @@ int calibrate_impl(leap_ctx* ctx, int32_t slot, const double* d_dd, int32_t ndir
 
 std::string batch_key(const leap_ctx* ctx, const std::vector<WorkItem>& items, int32_t D, int32_t precision) {
   std::string k = std::to_string(D) + ":" + std::to_string(precision) + (ctx->tc_gemm ? ":tc" : ":cc") +
-                  ":mma" + std::to_string(ctx->mma_rotate);
+                  ":mma" + std::to_string(ctx->mma_rotate) + ":grid" + std::to_string(ctx->gridded);
   for (const auto& w : items) k += "|" + std::to_string(w.slot) + "," + std::to_string(w.dir0) + "," + std::to_string(w.ndir);
   return k;
 }
@@ -926,6 +1104,7 @@ int finish_integration(leap_ctx* ctx, Integration& in, int32_t vis_type, int64_t
   in.channels = channels;
   in.pols = pols;
   in.has_map = false;
+  in.map_g_nbl = 0;
   if (vis_type == LEAP_VIS_C64 && pols == 4 && rows * 8 < (int64_t(1) << 31)) {
     // The pipelined kernels' view: 2-D floats [channels][rows*8], box 256 floats x 16 channels.
     auto enc = tensor_map_encoder();
@@ -1241,6 +1420,8 @@ void leap_destroy(leap_ctx* ctx) {
     ctx->dirk.release();
     ctx->twiddle.release();
     ctx->twiddle_df.release();
+    for (auto& kv : ctx->grid_tabs) kv.second.release();
+    ctx->grid_items.release(); ctx->grid_order.release(); ctx->grid_win.release();
     for (auto& tri : ctx->ring)
       for (auto& ev : tri)
         if (ev) cudaEventDestroy(ev);
@@ -1522,6 +1703,7 @@ int32_t leap_set_integration_ms_async(leap_ctx* ctx, int32_t slot, int32_t vis_t
   in.channels = channels;
   in.pols = pols;
   in.has_map = false;
+  in.map_g_nbl = 0;
   if (vis_type == LEAP_VIS_C64 && pols == 4 && rows * 8 < (int64_t(1) << 31)) {
     auto enc = tensor_map_encoder();
     if (!enc) return fail(ctx, LEAP_ERR_CUDA, "cuTensorMapEncodeTiled unavailable");
@@ -1742,6 +1924,10 @@ int32_t leap_set_option(leap_ctx* ctx, int32_t option, int32_t value) {
     case LEAP_OPTION_TENSOR_CORE_ROTATION:
       if (value < 0 || value > 2) return fail(ctx, LEAP_ERR_INVALID_ARGUMENT, "rotation option must be 0, 1 or 2");
       ctx->mma_rotate = value;
+      return LEAP_OK;
+    case LEAP_OPTION_GRIDDED_ROTATION:
+      if (value < 0 || value > 1) return fail(ctx, LEAP_ERR_INVALID_ARGUMENT, "gridded option must be 0 or 1");
+      ctx->gridded = value;
       return LEAP_OK;
     default: return fail(ctx, LEAP_ERR_INVALID_ARGUMENT, "unknown option");
   }

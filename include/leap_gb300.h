@@ -219,6 +219,12 @@ int32_t leap_set_autotune(leap_ctx* ctx, int32_t enable);
                                                     multiply-accumulate as 3xTF32 mma.sync for items of >= 12
                                                     directions.  0: never; 1 (default): only where the batched
                                                     autotuner measures it faster; 2: always */
+#define LEAP_OPTION_GRIDDED_ROTATION 4         /* mixed form, 4-pol complex<float>: evaluate each row's channel sum
+                                                    at every direction's phase slope through a 2x-oversampled grid
+                                                    (a type-2 non-uniform DFT): the grid values are one 3xTF32
+                                                    tcgen05 product per tile, shared by all directions, then a
+                                                    10-point interpolation per (row, direction).  0: off (default);
+                                                    1: on */
 int32_t leap_set_option(leap_ctx* ctx, int32_t option, int32_t value);
 
 /* Copy the avgData of `direction` from the last calibrate call to host memory
