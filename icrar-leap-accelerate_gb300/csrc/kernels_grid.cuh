@@ -25,11 +25,11 @@
 // positions differ by far less than a grid step: one warp-uniform tcgen05.ld of
 // W + 1 columns serves all 32 lanes of a direction.
 //
-// The product runs in 3xTF32.  The tensor cores accumulate FP32 with truncation,
-// whose error grows with the number of accumulation steps and the size of the
-// accumulator; so the large hi*hi products restart in a fresh accumulator every
-// 64 channels (a "segment") and the small lo*hi + hi*lo corrections go to an
-// accumulator of their own.  Converter warps add the segments together with
+// The product runs in 3xTF32 (V E ~ V_hi E_hi + V_lo E_hi + V_hi E_lo with hi = tf32(x),
+// lo = tf32(x - hi)).  The tensor cores accumulate FP32 with truncation, whose error
+// grows with the number of accumulation steps and the size of the accumulator; so the
+// large hi*hi products restart in a fresh accumulator every 64 channels (a "segment")
+// and the small corrections go to an accumulator of their own.  Converter warps add the segments together with
 // rounded FP32 adds.  Measured on 128 antennas x 384 channels this keeps the
 // averages within ~5e-7 of the FP64 sums (relative to the sum of |terms|).
 //
@@ -41,9 +41,10 @@
 // Warp roles (14 warps): 0 = TMA producer, 1 = MMA issuer (+ TMEM owner), 2-5 =
 // converters (split the visibility box into K-major hi/lo blocks, and fold the
 // accumulators), 6-13 = epilogue (warp w reads TMEM lanes 32 (w % 4) ..; two
-// warps per quarter take 32 directions each).  Rings: kGrStages stages of
-// {visibility box, E window} (deep enough to cover HBM latency) and kGrAStages
-// packed A blocks.  Every wait is bounded; a timeout sets the error word, stops
+// warps per quarter take 32 directions each).  One ring of kGrStages stages of
+// {visibility box, E window, packed A}, released by one MMA commit per stage: the
+// single MMA-issuing thread shares its scheduler with epilogue warps, so its
+// per-chunk instruction count bounds the kernel.  Every wait is bounded; a timeout sets the error word, stops
 // every role, and the block still waits (bounded) for its copies and MMAs and
 // frees its TMEM.
 #pragma once
@@ -57,24 +58,30 @@ constexpr int kGrTaps = 10;           // W, grid points per interpolation
 constexpr float kGrBeta = 23.0f;      // 2.3 W
 constexpr int kGrChunk = 16;          // channels per stage
 constexpr int kGrSegChunks = 4;       // chunks per hi*hi accumulation segment (64 channels)
-constexpr int kGrStages = 5;          // {visibility box, E window} ring
-constexpr int kGrAStages = 3;         // packed A ring
+constexpr int kGrStages = 6;          // {visibility box / A hi, A lo, E window} ring
+constexpr int kGrMacro = 2;           // chunks handed over per barrier round (stages go in pairs)
+constexpr int kGrMacroStages = kGrStages / kGrMacro;
 constexpr int kGrJwMax = 64;          // grid points per pass (MMA N = 2 Jw <= 128)
 constexpr int kGrPassStride = 48;     // grid points between pass windows (multiple of 8)
 constexpr int kGrLoadCols = 16;       // TMEM columns one interpolation load reads
-constexpr int kGrDirs = 64;           // directions per unit (8 epilogue warps x 32 / 4 quarters)
-constexpr int kGrWarps = 14;
+constexpr int kGrDirs = 64;           // directions per unit (16 epilogue warps x 16 / 4 quarters)
+constexpr int kGrEpiWarps = 8;
+constexpr int kGrWarpDirs = kGrDirs * 4 / kGrEpiWarps;  // directions per epilogue warp
+constexpr int kGrWarps = 6 + kGrEpiWarps;
 constexpr int kGrThreads = kGrWarps * 32;
 constexpr int kGrVBytes = 32 * 4 * kGrChunk * 4;         // [16 ch][4 t][32 floats]
 constexpr int kGrEBytes = 2 * 2 * 2 * kGrJwMax * 32;     // [hl][ks][2 Jw rows x 32 B]
-constexpr int kGrStageBytes = kGrVBytes + kGrEBytes;
-constexpr int kGrABytes = 2 * 2 * 128 * 32;              // [hl][ks][128 rows x 32 B]
-constexpr int kGrRecWords = 24;                          // per (direction, timestep) record: 16-byte rows
-constexpr int kGrRecBytes = 8 * 8 * 4 * kGrRecWords * 4; // [8 warps][8 dirs][4 t][24]
+constexpr int kGrAHalf = 2 * 128 * 32;                   // one split of A: [ks][128 rows x 32 B]
+static_assert(kGrAHalf == kGrVBytes, "the hi blocks are written over the visibility box");
+// Stage: [visibility box, then A hi][A lo][E]
+constexpr int kGrStageBytes = kGrVBytes + kGrAHalf + kGrEBytes;
+constexpr int kGrEOffset = kGrVBytes + kGrAHalf;
+constexpr int kGrRecWords = 20;                          // per (direction, timestep) record: 16-byte rows
+constexpr int kGrRecBytes = kGrEpiWarps * 32 * kGrRecWords * 4;  // [warps][4 t][8 dirs][20]
 constexpr uint32_t kGrRegion = 128;                      // TMEM columns per region
 constexpr uint32_t kGrIS = 2 * kGrRegion, kGrAC = 3 * kGrRegion;
 constexpr int kGrWide = 1 << 16;                         // record flag: the 4 timesteps need separate loads
-constexpr int kGrNumBars = 2 * kGrStages + 2 * kGrAStages + 8;
+constexpr int kGrNumBars = 4 * kGrMacroStages + 8;
 
 // A pass window must hold every stencil whose start falls in its stride, plus the
 // columns one load reads past the stencil.
@@ -82,7 +89,7 @@ static_assert(kGrPassStride % 8 == 0 && kGrPassStride - 1 + kGrLoadCols <= kGrJw
 static_assert(kGrTaps + 1 <= kGrLoadCols, "one load per stencil");
 
 __host__ __device__ constexpr int grid_smem_bytes() {
-  return kGrStages * kGrStageBytes + kGrAStages * kGrABytes + kTwiddleSize * 8 + kGrRecBytes + kGrNumBars * 8 + 16;
+  return kGrStages * kGrStageBytes + kTwiddleSize * 8 + kGrRecBytes + kGrNumBars * 8 + 16;
 }
 
 // Rows of the E table of channel count C: row r is grid point l = r - lbase.
@@ -240,10 +247,12 @@ __device__ __forceinline__ void grid_weights(float y, float (&w)[W + 1]) {
 #pragma unroll
   for (int k = 0; k <= W; ++k) {
     // sqrt(1 - z^2) - 1 = -z^2 / (1 + sqrt(1 - z^2)): no cancellation near the centre.
+    // Hardware reciprocal square root and exp2 (~2 ulp): weight error below 1e-7 of the
+    // largest weight.
     const float z = (y - static_cast<float>(k)) * kInvHalf;
     const float z2 = z * z;
-    const float q = fmaxf(0.0f, 1.0f - z2);
-    w[k] = exp2f(-kBeta2 * __fdividef(z2, 1.0f + sqrtf(q)));
+    const float q = fmaxf(1e-30f, 1.0f - z2);
+    w[k] = exp2f(-kBeta2 * __fdividef(z2, fmaf(q, rsqrtf(q), 1.0f)));
   }
 }
 
@@ -252,20 +261,17 @@ __device__ __forceinline__ void grid_weights(float y, float (&w)[W + 1]) {
 // rotated by (cr, sr); returns this lane's component of the rotated sum.
 template <int W>
 __device__ __forceinline__ float grid_tap_sum(uint32_t taddr, int jw, const float (&rj)[W + 3], int comp) {
+  // Both loads and the wait in one statement: the results are defined only after the wait.
   uint32_t vr[16], vi[16];
   asm volatile(
-      "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];"
+      "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%32];\n\t"
+      "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%16,%17,%18,%19,%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31}, [%33];\n\t"
+      "tcgen05.wait::ld.sync.aligned;"
       : "=r"(vr[0]), "=r"(vr[1]), "=r"(vr[2]), "=r"(vr[3]), "=r"(vr[4]), "=r"(vr[5]), "=r"(vr[6]), "=r"(vr[7]),
-        "=r"(vr[8]), "=r"(vr[9]), "=r"(vr[10]), "=r"(vr[11]), "=r"(vr[12]), "=r"(vr[13]), "=r"(vr[14]), "=r"(vr[15])
-      : "r"(taddr)
-      : "memory");
-  asm volatile(
-      "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];"
-      : "=r"(vi[0]), "=r"(vi[1]), "=r"(vi[2]), "=r"(vi[3]), "=r"(vi[4]), "=r"(vi[5]), "=r"(vi[6]), "=r"(vi[7]),
+        "=r"(vr[8]), "=r"(vr[9]), "=r"(vr[10]), "=r"(vr[11]), "=r"(vr[12]), "=r"(vr[13]), "=r"(vr[14]), "=r"(vr[15]),
+        "=r"(vi[0]), "=r"(vi[1]), "=r"(vi[2]), "=r"(vi[3]), "=r"(vi[4]), "=r"(vi[5]), "=r"(vi[6]), "=r"(vi[7]),
         "=r"(vi[8]), "=r"(vi[9]), "=r"(vi[10]), "=r"(vi[11]), "=r"(vi[12]), "=r"(vi[13]), "=r"(vi[14]), "=r"(vi[15])
-      : "r"(taddr + static_cast<uint32_t>(jw))
-      : "memory");
-  asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+      : "r"(taddr), "r"(taddr + static_cast<uint32_t>(jw)));
   float P = 0.f, Q = 0.f;
 #pragma unroll
   for (int k = 0; k <= W; ++k) {
@@ -288,7 +294,7 @@ __device__ __noinline__ float grid_wide_sum(const float* rec_dir, uint32_t tbase
                                             int tl, int pp) {
   float acc = 0.f;
   for (int tt = 0; tt < 4; ++tt) {
-    const int ct = __float_as_int(reinterpret_cast<const float4*>(rec_dir + tt * kGrRecWords)[3].y);
+    const int ct = __float_as_int(reinterpret_cast<const float4*>(rec_dir + tt * 8 * kGrRecWords)[3].y);
     if ((ct & 0xFFFF) == 0xFFFF || ((ct >> 8) & 255) != pp) continue;  // same in every lane
     const float v = grid_tap_sum<W>(tbase + static_cast<uint32_t>(ct & 255), jw, rw, comp);
     if (tl == tt) acc += v;
@@ -349,16 +355,15 @@ template <int W>
 __global__ void __launch_bounds__(kGrThreads, 1) rotate_average_gridded(const GridParams p) {
   extern __shared__ __align__(128) unsigned char grid_smem[];
   unsigned char* smem = grid_smem;
-  unsigned char* ve = smem;                                          // [kGrStages][V | E]
-  unsigned char* abuf = smem + kGrStages * kGrStageBytes;            // [kGrAStages][hl][ks][128 x 32 B]
-  float2* tab = reinterpret_cast<float2*>(abuf + kGrAStages * kGrABytes);
+  unsigned char* ve = smem;                                          // [kGrStages][V | E | A]
+  float2* tab = reinterpret_cast<float2*>(smem + kGrStages * kGrStageBytes);
   float* rec_all = reinterpret_cast<float*>(tab + kTwiddleSize);
   uint64_t* bars = reinterpret_cast<uint64_t*>(rec_all + kGrRecBytes / 4);
-  uint64_t* vfull = bars;                      // [kGrStages] TMA bytes landed
-  uint64_t* vempty = vfull + kGrStages;        // [kGrStages] converters read V and the MMAs read E
-  uint64_t* afull = vempty + kGrStages;        // [kGrAStages] converters wrote the A blocks
-  uint64_t* aempty = afull + kGrAStages;       // [kGrAStages] MMAs that read them completed
-  uint64_t* is_full = aempty + kGrAStages;     // a middle segment is complete in IS
+  uint64_t* vfull = bars;                      // [kGrMacroStages] TMA bytes of a stage pair landed
+  uint64_t* afull = vfull + kGrMacroStages;    // [kGrMacroStages] converters wrote its A blocks
+  uint64_t* sdone = afull + kGrMacroStages;    // [kGrMacroStages] MMAs that read it completed
+  uint64_t* vread = sdone + kGrMacroStages;    // [kGrMacroStages] every converter warp read the boxes
+  uint64_t* is_full = vread + kGrMacroStages;  // a middle segment is complete in IS
   uint64_t* is_empty = is_full + 1;            // ... and was folded into RS
   uint64_t* blk_full = is_empty + 1;           // every MMA of a tile completed
   uint64_t* ac_free = blk_full + 1;            // final fold of a tile done: IS and AC reusable
@@ -375,21 +380,19 @@ __global__ void __launch_bounds__(kGrThreads, 1) rotate_average_gridded(const Gr
     asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
   }
   if (threadIdx.x == 0) {
-    for (int i = 0; i < kGrStages; ++i) {
+    for (int i = 0; i < kGrMacroStages; ++i) {
       mbar_init(&vfull[i], 1);
-      mbar_init(&vempty[i], 5);  // 4 converter warps + 1 MMA commit
-    }
-    for (int i = 0; i < kGrAStages; ++i) {
       mbar_init(&afull[i], 4);
-      mbar_init(&aempty[i], 1);
+      mbar_init(&sdone[i], 1);
     }
+    for (int i = 0; i < kGrMacroStages; ++i) mbar_init(&vread[i], 4);
     mbar_init(is_full, 1);
     mbar_init(is_empty, 4);
     mbar_init(blk_full, 1);
     mbar_init(ac_free, 4);
     for (int i = 0; i < 2; ++i) {
       mbar_init(&rs_full[i], 4);
-      mbar_init(&rs_free[i], 8);
+      mbar_init(&rs_free[i], kGrEpiWarps);
     }
     fence_mbar_init();
     *abort_flag = 0;
@@ -412,31 +415,37 @@ __global__ void __launch_bounds__(kGrThreads, 1) rotate_average_gridded(const Gr
         const GridWindow w = p.win[u];
         for (int tb = 0; tb < g.ntb && ok; ++tb)
           for (int ps = 0; ps < w.npass && ok; ++ps)
-            for (int q = 0; q < I.nchunk; ++q, ++ctr) {
-              const int s = ctr % kGrStages;
-              if (ctr >= kGrStages && !grid_wait(&vempty[s], ((ctr / kGrStages) - 1) & 1, abort_flag)) {
+            for (int q0 = 0; q0 < I.nchunk; q0 += kGrMacro, ++ctr) {
+              const int m = ctr % kGrMacroStages;
+              const int nq = min(kGrMacro, I.nchunk - q0);
+              if (ctr >= kGrMacroStages && !grid_wait(&sdone[m], ((ctr / kGrMacroStages) - 1) & 1, abort_flag)) {
                 grid_fail(p, abort_flag);
                 ok = false;
                 break;
               }
-              unsigned char* st = ve + s * kGrStageBytes;
-              mbar_arrive_expect_tx(&vfull[s], kGrVBytes + 8 * w.jw * 32);
-              tma_load_3d(st, &I.map, g.quad * 32, g.t_lo + tb * 4, q * kGrChunk, &vfull[s]);
+              mbar_arrive_expect_tx(&vfull[m], nq * (kGrVBytes + 8 * w.jw * 32));
               const int rg = w.rg0 + ps * (kGrPassStride / 8);
+              for (int i = 0; i < nq; ++i) {
+                const int q = q0 + i;
+                unsigned char* st = ve + (m * kGrMacro + i) * kGrStageBytes;
+                tma_load_3d(st, &I.map, g.quad * 32, g.t_lo + tb * 4, q * kGrChunk, &vfull[m]);
 #pragma unroll
-              for (int ks = 0; ks < 2; ++ks)
+                for (int ks = 0; ks < 2; ++ks)
 #pragma unroll
-                for (int hl = 0; hl < 2; ++hl)
+                  for (int hl = 0; hl < 2; ++hl)
 #pragma unroll
-                  for (int ri = 0; ri < 2; ++ri) {
-                    const float* src = I.etab + ((static_cast<int64_t>(((q * 2 + ks) * 2 + hl) * 2 + ri) * I.nrg) + rg) * 64;
-                    bulk_copy_g2s(st + kGrVBytes + ((hl * 2 + ks) * 2 * w.jw + ri * w.jw) * 32, src, w.jw * 32, &vfull[s]);
-                  }
+                    for (int ri = 0; ri < 2; ++ri) {
+                      const float* src =
+                          I.etab + ((static_cast<int64_t>(((q * 2 + ks) * 2 + hl) * 2 + ri) * I.nrg) + rg) * 64;
+                      bulk_copy_g2s(st + kGrEOffset + ((hl * 2 + ks) * 2 * w.jw + ri * w.jw) * 32, src, w.jw * 32,
+                                    &vfull[m]);
+                    }
+              }
             }
       }
       // Do not leave while copies issued by this block may still land.
-      for (uint32_t j = (ctr > kGrStages ? ctr - kGrStages : 0); j < ctr; ++j)
-        if (!mbar_wait_bounded(&vfull[j % kGrStages], (j / kGrStages) & 1)) atomicOr(p.err, kDevErrTimeout);
+      for (uint32_t j = (ctr > kGrMacroStages ? ctr - kGrMacroStages : 0); j < ctr; ++j)
+        if (!mbar_wait_bounded(&vfull[j % kGrMacroStages], (j / kGrMacroStages) & 1)) atomicOr(p.err, kDevErrTimeout);
     }
   } else if (warp == 1) {
     // ---------------- MMA issuer ----------------
@@ -450,6 +459,8 @@ __global__ void __launch_bounds__(kGrThreads, 1) rotate_average_gridded(const Gr
         const GridItem& I = p.items[g.item];
         const GridWindow w = p.win[u];
         const uint32_t idesc = tc_idesc_tf32(128, 2 * w.jw);
+        const uint64_t adesc0 = tc_smem_desc(ve, kTcLbo, kTcSbo);
+        const uint64_t edesc0 = tc_smem_desc(ve + kGrEOffset, kTcLbo, kTcSbo);
         for (int tb = 0; tb < g.ntb && ok; ++tb)
           for (int ps = 0; ps < w.npass && ok; ++ps, ++blk) {
             const uint32_t b = blk & 1;
@@ -461,47 +472,44 @@ __global__ void __launch_bounds__(kGrThreads, 1) rotate_average_gridded(const Gr
             }
             asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
             const uint32_t rs = tmem + b * kGrRegion;
-            for (int q = 0; q < I.nchunk; ++q, ++ctr) {
-              const int s = ctr % kGrStages, a = ctr % kGrAStages;
-              const int seg = q / kGrSegChunks, qs = q % kGrSegChunks;
-              if (!grid_wait(&vfull[s], (ctr / kGrStages) & 1, abort_flag) ||
-                  !grid_wait(&afull[a], (ctr / kGrAStages) & 1, abort_flag)) {
+            for (int q0 = 0; q0 < I.nchunk && ok; q0 += kGrMacro, ++ctr) {
+              const int m = ctr % kGrMacroStages;
+              const int nq = min(kGrMacro, I.nchunk - q0);
+              if (!grid_wait(&afull[m], (ctr / kGrMacroStages) & 1, abort_flag)) {
                 grid_fail(p, abort_flag);
                 ok = false;
                 break;
               }
               asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-              const unsigned char* eb = ve + s * kGrStageBytes + kGrVBytes;
-              const unsigned char* ab = abuf + a * kGrABytes;
-              uint64_t ah[2], al[2], bh[2], bl[2];
-#pragma unroll
-              for (int ks = 0; ks < 2; ++ks) {
-                ah[ks] = tc_smem_desc(ab + (0 * 2 + ks) * 4096, kTcLbo, kTcSbo);
-                al[ks] = tc_smem_desc(ab + (1 * 2 + ks) * 4096, kTcLbo, kTcSbo);
-                bh[ks] = tc_smem_desc(eb + (0 * 2 + ks) * 2 * w.jw * 32, kTcLbo, kTcSbo);
-                bl[ks] = tc_smem_desc(eb + (1 * 2 + ks) * 2 * w.jw * 32, kTcLbo, kTcSbo);
+              for (int i = 0; i < nq; ++i) {
+                const int q = q0 + i;
+                const int seg = q / kGrSegChunks, qs = q % kGrSegChunks;
+                // Descriptors of this stage: A hi/lo at +0 / +2*4096, E hi/lo at +0 / +4*jw*32 from
+                // their bases; k-step 1 is 4096 (A) or 2*jw*32 (E) bytes further (address field >> 4).
+                const uint64_t so = static_cast<uint64_t>((m * kGrMacro + i) * (kGrStageBytes >> 4));
+                const uint64_t ah = adesc0 + so, bh = edesc0 + so;
+                const uint64_t al = ah + (2 * 4096 >> 4), bl = bh + static_cast<uint64_t>(4 * w.jw * 2);
+                const uint64_t ka = 4096 >> 4, kb = static_cast<uint64_t>(2 * w.jw * 2);
+                // Corrections first: they give the fold of the previous segment time to finish.
+                tc_mma_tf32(tmem + kGrAC, al, bh, idesc, q > 0 ? 1u : 0u);
+                tc_mma_tf32(tmem + kGrAC, ah, bl, idesc, 1u);
+                tc_mma_tf32(tmem + kGrAC, al + ka, bh + kb, idesc, 1u);
+                tc_mma_tf32(tmem + kGrAC, ah + ka, bl + kb, idesc, 1u);
+                if (seg >= 2 && qs == 0 && !grid_wait(is_empty, (mids - 1) & 1, abort_flag)) {
+                  grid_fail(p, abort_flag);
+                  ok = false;
+                  break;
+                }
+                const uint32_t dst = seg == 0 ? rs : tmem + kGrIS;
+                tc_mma_tf32(dst, ah, bh, idesc, qs > 0 ? 1u : 0u);
+                tc_mma_tf32(dst, ah + ka, bh + kb, idesc, 1u);
+                issued = true;
+                if (seg >= 1 && qs == kGrSegChunks - 1 && q != I.nchunk - 1) {
+                  tc_commit(is_full);  // a middle segment, folded by the converters
+                  ++mids;
+                }
               }
-              // Corrections first: they give the fold of the previous segment time to finish.
-#pragma unroll
-              for (int ks = 0; ks < 2; ++ks) {
-                tc_mma_tf32(tmem + kGrAC, al[ks], bh[ks], idesc, (q > 0 || ks > 0) ? 1u : 0u);
-                tc_mma_tf32(tmem + kGrAC, ah[ks], bl[ks], idesc, 1u);
-              }
-              if (seg >= 2 && qs == 0 && !grid_wait(is_empty, (mids - 1) & 1, abort_flag)) {
-                grid_fail(p, abort_flag);
-                ok = false;
-                break;
-              }
-              const uint32_t dst = seg == 0 ? rs : tmem + kGrIS;
-#pragma unroll
-              for (int ks = 0; ks < 2; ++ks) tc_mma_tf32(dst, ah[ks], bh[ks], idesc, (qs > 0 || ks > 0) ? 1u : 0u);
-              issued = true;
-              tc_commit(&vempty[s]);
-              tc_commit(&aempty[a]);
-              if (seg >= 1 && qs == kGrSegChunks - 1 && q != I.nchunk - 1) {
-                tc_commit(is_full);  // a middle segment, folded by the converters
-                ++mids;
-              }
+              if (issued) tc_commit(&sdone[m]);
             }
             if (ok) tc_commit(blk_full);
           }
@@ -509,7 +517,7 @@ __global__ void __launch_bounds__(kGrThreads, 1) rotate_average_gridded(const Gr
       // No MMA of this block may be in flight when its TMEM is freed.
       if (issued) {
         const uint32_t j = ctr - 1;
-        if (!mbar_wait_bounded(&aempty[j % kGrAStages], (j / kGrAStages) & 1)) atomicOr(p.err, kDevErrTimeout);
+        if (!mbar_wait_bounded(&sdone[j % kGrMacroStages], (j / kGrMacroStages) & 1)) atomicOr(p.err, kDevErrTimeout);
       }
     }
   } else if (warp < 6) {
@@ -528,62 +536,89 @@ __global__ void __launch_bounds__(kGrThreads, 1) rotate_average_gridded(const Gr
       for (int tb = 0; tb < g.ntb && ok; ++tb)
         for (int ps = 0; ps < w.npass && ok; ++ps, ++blk) {
           const uint32_t b = blk & 1;
-          for (int q = 0; q < I.nchunk; ++q, ++ctr) {
-            const int s = ctr % kGrStages, a = ctr % kGrAStages;
-            if (!grid_wait(&vfull[s], (ctr / kGrStages) & 1, abort_flag) ||
-                (ctr >= kGrAStages && !grid_wait(&aempty[a], ((ctr / kGrAStages) - 1) & 1, abort_flag))) {
+          for (int q0 = 0; q0 < I.nchunk; q0 += kGrMacro, ++ctr) {
+            // The stages' previous MMAs completed before the producer refilled them, so a full
+            // stage pair's A blocks are free to overwrite.
+            const int m = ctr % kGrMacroStages;
+            const int nq = min(kGrMacro, I.nchunk - q0);
+            if (!grid_wait(&vfull[m], (ctr / kGrMacroStages) & 1, abort_flag)) {
               grid_fail(p, abort_flag);
               ok = false;
               break;
             }
-            const float* vb = reinterpret_cast<const float*>(ve + s * kGrStageBytes);
-            unsigned char* ab = abuf + a * kGrABytes;
+            // Read both boxes of the round; the hi blocks overwrite them, so every converter
+            // warp must have read them before any warp writes.
+            float x[kGrMacro][4][4];
 #pragma unroll
-            for (int bi = 0; bi < 4; ++bi) {
-              const int blk4 = cw + 4 * bi;  // 16 blocks of (4 channels, 1 timestep)
-              const int cg = blk4 >> 2, tl = blk4 & 3;
-              float4 hi, lo;
-              float x[4];
+            for (int i = 0; i < kGrMacro; ++i) {
+              if (i < nq) {
+                const float* vb = reinterpret_cast<const float*>(ve + (m * kGrMacro + i) * kGrStageBytes);
 #pragma unroll
-              for (int j = 0; j < 4; ++j) x[j] = vb[(cg * 4 + j) * 128 + tl * 32 + lane];
-              hi.x = to_tf32(x[0]);
-              hi.y = to_tf32(x[1]);
-              hi.z = to_tf32(x[2]);
-              hi.w = to_tf32(x[3]);
-              lo.x = to_tf32(x[0] - hi.x);
-              lo.y = to_tf32(x[1] - hi.y);
-              lo.z = to_tf32(x[2] - hi.z);
-              lo.w = to_tf32(x[3] - hi.w);
-              const int m = (lane >> 3) * 32 + tl * 8 + (lane & 7);  // TMEM lane: baseline, timestep, pol, re/im
-              const int k = cg * 4;                                  // 0..15 within the chunk
-              const int off = (k >> 3) * 4096 + (((m >> 3) << 1) + ((k >> 2) & 1)) * 128 + (m & 7) * 16;
-              *reinterpret_cast<float4*>(ab + off) = hi;
-              *reinterpret_cast<float4*>(ab + 2 * 4096 + off) = lo;
+                for (int bi = 0; bi < 4; ++bi) {
+                  const int blk4 = cw + 4 * bi;  // 16 blocks of (4 channels, 1 timestep)
+                  const int cg = blk4 >> 2, tl = blk4 & 3;
+#pragma unroll
+                  for (int j = 0; j < 4; ++j) x[i][bi][j] = vb[(cg * 4 + j) * 128 + tl * 32 + lane];
+                }
+              }
+            }
+            __syncwarp();
+            if (lane == 0) mbar_arrive(&vread[m]);
+            if (!grid_wait(&vread[m], (ctr / kGrMacroStages) & 1, abort_flag)) {
+              grid_fail(p, abort_flag);
+              ok = false;
+              break;
+            }
+#pragma unroll
+            for (int i = 0; i < kGrMacro; ++i) {
+              if (i < nq) {
+                unsigned char* sb = ve + (m * kGrMacro + i) * kGrStageBytes;
+#pragma unroll
+                for (int bi = 0; bi < 4; ++bi) {
+                  const int blk4 = cw + 4 * bi;
+                  const int cg = blk4 >> 2, tl = blk4 & 3;
+                  float4 hi, lo;
+                  hi.x = to_tf32(x[i][bi][0]);
+                  hi.y = to_tf32(x[i][bi][1]);
+                  hi.z = to_tf32(x[i][bi][2]);
+                  hi.w = to_tf32(x[i][bi][3]);
+                  lo.x = to_tf32(x[i][bi][0] - hi.x);
+                  lo.y = to_tf32(x[i][bi][1] - hi.y);
+                  lo.z = to_tf32(x[i][bi][2] - hi.z);
+                  lo.w = to_tf32(x[i][bi][3] - hi.w);
+                  const int mrow = (lane >> 3) * 32 + tl * 8 + (lane & 7);  // TMEM lane: baseline, timestep, pol, re/im
+                  const int k = cg * 4;                                     // 0..15 within the chunk
+                  const int off = (k >> 3) * 4096 + (((mrow >> 3) << 1) + ((k >> 2) & 1)) * 128 + (mrow & 7) * 16;
+                  *reinterpret_cast<float4*>(sb + off) = hi;
+                  *reinterpret_cast<float4*>(sb + kGrAHalf + off) = lo;
+                }
+              }
             }
             asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
             __syncwarp();
-            if (lane == 0) {
-              mbar_arrive(&afull[a]);
-              mbar_arrive(&vempty[s]);
-            }
+            if (lane == 0) mbar_arrive(&afull[m]);
             // Fold middle segment sg (1 <= sg <= nseg - 2) into RS once the next segment's
             // second chunk is converted (its first if it has only one).
-            const int seg = q / kGrSegChunks, qs = q % kGrSegChunks;
-            const int nxt = min(kGrSegChunks, I.nchunk - seg * kGrSegChunks);
-            const int sg = seg - 1;
-            if (sg >= 1 && sg <= nseg - 2 && qs == min(1, nxt - 1)) {
-              if (!grid_wait(is_full, mids & 1, abort_flag)) {
-                grid_fail(p, abort_flag);
-                ok = false;
-                break;
+            for (int i = 0; i < nq && ok; ++i) {
+              const int q = q0 + i;
+              const int seg = q / kGrSegChunks, qs = q % kGrSegChunks;
+              const int nxt = min(kGrSegChunks, I.nchunk - seg * kGrSegChunks);
+              const int sg = seg - 1;
+              if (sg >= 1 && sg <= nseg - 2 && qs == min(1, nxt - 1)) {
+                if (!grid_wait(is_full, mids & 1, abort_flag)) {
+                  grid_fail(p, abort_flag);
+                  ok = false;
+                  break;
+                }
+                asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+                grid_fold(lanes, tmem + b * kGrRegion, tmem + kGrIS, 0, true, false, 2 * w.jw);
+                asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+                __syncwarp();
+                if (lane == 0) mbar_arrive(is_empty);
+                ++mids;
               }
-              asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-              grid_fold(lanes, tmem + b * kGrRegion, tmem + kGrIS, 0, true, false, 2 * w.jw);
-              asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
-              __syncwarp();
-              if (lane == 0) mbar_arrive(is_empty);
-              ++mids;
             }
+            if (!ok) break;
           }
           if (!ok) break;
           // Final fold: RS += last segment (if any beyond the first) + corrections.
@@ -606,10 +641,10 @@ __global__ void __launch_bounds__(kGrThreads, 1) rotate_average_gridded(const Gr
   } else {
     // ---------------- epilogue: interpolate, rotate, accumulate ----------------
     const int e = warp - 6;
-    const int half = e >> 2;       // which 32 directions of the unit
+    const int half = e >> 2;       // which kGrWarpDirs directions of the unit
     const int quarter = warp & 3;  // TMEM lanes 32*quarter .. (hardware rule: warp id mod 4)
     const int tl = lane >> 3, ps = lane & 7, comp = lane & 1;
-    float* rec = rec_all + e * (8 * 4 * kGrRecWords);
+    float* rec = rec_all + e * (32 * kGrRecWords);  // record (t, direction jj) at (8 t + jj) * kGrRecWords
     uint32_t blk = 0;
     bool ok = true;
     for (int sl = blockIdx.x; ok; sl += gridDim.x) {
@@ -621,13 +656,13 @@ __global__ void __launch_bounds__(kGrThreads, 1) rotate_average_gridded(const Gr
       if (w.npass == 0) continue;
       const int n = 2 * I.C, c0 = I.C / 2;
       const int r0 = w.rg0 * 8;
-      const int dbase = g.dg * kGrDirs + half * 32;  // item-relative first direction of this warp
-      const int nd = max(0, min(32, I.ndir - dbase));
+      const int dbase = g.dg * kGrDirs + half * kGrWarpDirs;  // item-relative first direction of this warp
+      const int nd = max(0, min(kGrWarpDirs, I.ndir - dbase));
       const int b = g.quad * 4 + quarter;
       const bool bval = b < p.nbl;
-      float acc[32];
+      float acc[kGrWarpDirs];
 #pragma unroll
-      for (int j = 0; j < 32; ++j) acc[j] = 0.f;
+      for (int j = 0; j < kGrWarpDirs; ++j) acc[j] = 0.f;
       for (int tb = 0; tb < g.ntb && ok; ++tb) {
         const int t = g.t_lo + tb * 4 + tl;
         const bool rval = bval && t < g.t_hi;
@@ -645,7 +680,7 @@ __global__ void __launch_bounds__(kGrThreads, 1) rotate_average_gridded(const Gr
           asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
           const uint32_t tbase = tmem + (static_cast<uint32_t>(quarter * 32) << 16) + rb * kGrRegion;
 #pragma unroll
-          for (int gi = 0; gi < 4; ++gi) {
+          for (int gi = 0; gi < kGrWarpDirs / 8; ++gi) {
             if (gi * 8 >= nd) break;
             {
               // This lane's record: direction gi*8 + ps at timestep tl.
@@ -687,7 +722,7 @@ __global__ void __launch_bounds__(kGrThreads, 1) rotate_average_gridded(const Gr
               grid_weights<W>(any ? static_cast<float>(i0 - base) + f : 0.f, wt);
               float cr, sr;
               twiddle_turns(pa + static_cast<uint32_t>(c0) * pb, tab, cr, sr);
-              float4* my = reinterpret_cast<float4*>(rec + (ps * 4 + tl) * kGrRecWords);
+              float4* my = reinterpret_cast<float4*>(rec + (tl * 8 + ps) * kGrRecWords);
               my[0] = make_float4(wt[0], wt[1], wt[2], wt[3]);
               my[1] = make_float4(wt[4], wt[5], wt[6], wt[7]);
               my[2] = make_float4(wt[8], wt[9], wt[10], cr);
@@ -696,7 +731,7 @@ __global__ void __launch_bounds__(kGrThreads, 1) rotate_average_gridded(const Gr
             __syncwarp();
 #pragma unroll
             for (int jj = 0; jj < 8; ++jj) {
-              const float4* rq = reinterpret_cast<const float4*>(rec + (jj * 4 + tl) * kGrRecWords);
+              const float4* rq = reinterpret_cast<const float4*>(rec + (tl * 8 + jj) * kGrRecWords);
               const float4 q3 = rq[3];
               const int code = __float_as_int(q3.y);  // same in every lane
               if (code < 0) continue;
@@ -706,7 +741,7 @@ __global__ void __launch_bounds__(kGrThreads, 1) rotate_average_gridded(const Gr
                 if (((code >> 8) & 255) != pp) continue;
                 acc[gi * 8 + jj] += grid_tap_sum<W>(tbase + static_cast<uint32_t>(code & 255), w.jw, rw, comp);
               } else {
-                acc[gi * 8 + jj] += grid_wide_sum<W>(rec + jj * 4 * kGrRecWords, tbase, w.jw, rw, comp, tl, pp);
+                acc[gi * 8 + jj] += grid_wide_sum<W>(rec + jj * kGrRecWords, tbase, w.jw, rw, comp, tl, pp);
               }
             }
             __syncwarp();
@@ -720,7 +755,7 @@ __global__ void __launch_bounds__(kGrThreads, 1) rotate_average_gridded(const Gr
       // Sum the 4 timesteps of the quad's lanes and write this unit's sums.
       double2* out = I.out + static_cast<int64_t>(I.nslab > 1 ? g.slab : 0) * I.ndir * 4 * p.nbl;
 #pragma unroll
-      for (int j = 0; j < 32; ++j) {
+      for (int j = 0; j < kGrWarpDirs; ++j) {
         float v = acc[j] + __shfl_xor_sync(0xffffffffu, acc[j], 8);
         v += __shfl_xor_sync(0xffffffffu, v, 16);
         if (tl == 0 && bval && j < nd) {
