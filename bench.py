@@ -239,6 +239,34 @@ def fma_slots(rows: float, channels_x_rows: float, ndir: int, pols: int) -> floa
     return ndir * channels_x_rows * (pols * 4 + 5)
 
 
+def grid_mma_flops(obs, dds: np.ndarray, taps: int = 10, jw_max: int = 64, stride: int = 48, dirs_per_unit: int = 64):
+    """Tensor-core FLOPs of one call of the gridded kernel: the grid windows of its units
+    (quad of 4 baselines x all timesteps x up to 64 directions), computed as the kernel
+    computes them, times the 3xTF32 MMAs (6 per 16-channel chunk, M = 128, N = 2 jw, K = 8)."""
+    C, nbl, T = obs.channels, obs.nbaselines, obs.timesteps
+    n, lbase = 2 * C, ((C + taps + 8 + 7) // 8) * 8
+    nchunk = (C + 15) // 16
+    kb = -(dds[:, 2, :] - np.array([0.0, 0.0, 1.0])) * obs.freq_inc_hz / 299792458.0  # (D, 3) turns per metre
+    uvw = obs.uvw.reshape(T, nbl, 3)
+    nquad = (nbl + 3) // 4
+    flops = 0.0
+    for d0 in range(0, dds.shape[0], dirs_per_unit):
+        B = np.einsum("tbj,dj->tbd", uvw, kb[d0:d0 + dirs_per_unit])          # turns per channel
+        B = B - np.rint(B)
+        s = np.floor(B * n).astype(np.int64) - taps // 2 + 1
+        pad = nquad * 4 - nbl
+        smin = np.pad(s.min(axis=(0, 2)), (0, pad), constant_values=1 << 40).reshape(nquad, 4).min(axis=1)
+        smax = np.pad(s.max(axis=(0, 2)), (0, pad), constant_values=-(1 << 40)).reshape(nquad, 4).max(axis=1)
+        r0 = ((smin + lbase) >> 3) * 8
+        need = smax + 16 + lbase - r0
+        single = need <= jw_max
+        jw = np.where(single, np.maximum(16, (need + 7) & ~7), jw_max)
+        npass = np.where(single, 1, (smax + lbase - r0) // stride + 1)
+        ntb = (T + 3) // 4
+        flops += float((ntb * npass * nchunk * 6 * 2 * 128 * 2 * jw * 8).sum())
+    return flops
+
+
 def setup_single(args, ctx, lg, torch, local, rank, kind: str):
     """One integration, all directions in one leap_calibrate_async call (MWA or SKA-Low)."""
     from leap_gb300 import synth
@@ -283,6 +311,15 @@ def setup_single(args, ctx, lg, torch, local, rank, kind: str):
     w.step = step
     w.result = lambda: cal_dev.cpu().numpy().copy()
     w.obs, w.dirs, w.md, w.D, w.S = obs, dirs, md, D, S
+    w.min_ndir = D
+    w.grid_flops = grid_mma_flops(obs, dds)
+    w.vis_bytes_resident = obs.rows * obs.channels * obs.pols * 8
+    # DRAM traffic of one launch of the gridded kernel, from an ncu capture
+    # (dram__bytes_read.sum + dram__bytes_write.sum) of the 4-timestep case of the
+    # MWA workload: 101.8 MB read per timestep (the visibilities, once) + 26.9 MB of
+    # sum writes, scaled to the timesteps of this run.
+    if kind == "mwa" and obs.nbaselines == 8256 and obs.channels == 384 and D == 64:
+        w.grid_traffic = 101.80e6 * obs.timesteps + 26.94e6
     w.units = vis_dirs(obs, D)
     w.b_alg = alg_bytes(obs.pols * obs.rows * obs.channels, obs.rows, D, obs.nbaselines, obs.pols, 8)
     w.f_alg = fma_slots(obs.rows, obs.rows * obs.channels, D, obs.pols)
@@ -342,7 +379,7 @@ def setup_single(args, ctx, lg, torch, local, rank, kind: str):
     return w
 
 
-def setup_batched(args, ctx, lg, torch, local, rank):
+def setup_batched(args, ctx, lg, torch, local, rank):  # noqa: C901
     """32 uneven integration chunks, 256 directions, one leap_calibrate_batched call per step."""
     from leap_gb300 import synth
     dev = f"cuda:{local}"
@@ -377,6 +414,7 @@ def setup_batched(args, ctx, lg, torch, local, rank):
     w.result = lambda: holder["cal"].copy()
     w.kernel_timing = "total"
     w.obs, w.dirs, w.md, w.D, w.S, w.items, w.dds = obs_list[0], dirs, md, D, S, items, dds
+    w.min_ndir = min(it[2] for it in items)
     w.units = sum(float(obs_list[sl].pols) * obs_list[sl].rows * obs_list[sl].channels * n for sl, _, n in items)
     w.b_alg = sum(alg_bytes(4.0 * obs_list[sl].rows * obs_list[sl].channels, obs_list[sl].rows, n,
                             obs_list[sl].nbaselines, 4, 8) for sl, _, n in items)
@@ -442,6 +480,7 @@ def setup_differentiable(args, ctx, lg, torch, local, rank):
     w.kernel_timing = "events"
     w.extra_launches = 8  # leap_backward: 2 transposed contractions, cal1, 2 avgData, (l, m, n) + reduce, vis
     w.obs, w.dirs, w.md, w.D, w.S = obs, None, md, nd, md.A.shape[1]
+    w.min_ndir = nd
     w.units = vis_dirs(obs, nd)
     w.b_alg = alg_bytes(4.0 * obs.rows * obs.channels, obs.rows, nd, obs.nbaselines, 4, 8)
     w.f_alg = fma_slots(obs.rows, obs.rows * obs.channels, nd, 4)
@@ -517,6 +556,20 @@ def run_gpu(args, rank: int, world: int):
     value = w.units * world / (ms / 1e3)
     cal_main = w.result()
     gpu_launches = (int(tim.kernels) + getattr(w, "extra_launches", 0)) * args.steps
+
+    # The rotate + average kernel this run used (the library's choice for LEAP_OPTION_GRIDDED_ROTATION).
+    gridded = prec == lg.LEAP_PRECISION_MIXED and (
+        args.gridded == 1 or (args.gridded in (-1, 2) and args.tc_rotation != 2 and w.min_ndir >= 32))
+    alt_kernel = None
+    if gridded and args.gridded != 1 and args.workload in ("mwa", "ska_low"):
+        # The same call through the FP32 CUDA-core pipelined kernel, for comparison.
+        ctx.set_option(_abi.LEAP_OPTION_GRIDDED_ROTATION, 0)
+        ms_alt, _ = timed(prec, max(1, min(args.steps, 5)), 2)
+        cal_alt = w.result()
+        ctx.set_option(_abi.LEAP_OPTION_GRIDDED_ROTATION, 2)
+        alt_kernel = {"kernel": "rotate_average_mixed_pipe (FP32 CUDA cores, compensated sums)", "ms_per_step": ms_alt,
+                      "value": w.units * world / (ms_alt / 1e3),
+                      "max_cal_diff_vs_gridded_rad": wrapped_max_diff(cal_main, cal_alt)}
 
     checks = {}
     plain = None
@@ -594,7 +647,9 @@ def run_gpu(args, rank: int, world: int):
     peak = peaks["hbm_gbs"] if peaks else 6800.0
     if w.kernel_timing == "rotate":
         k_ms = tim.rotate_ms / max(1, tim.calls)
-        k_name = "rotate_average (mixed: persistent TMA-pipelined kernel + compensated reference-antenna pass)"
+        k_name = ("rotate_average (mixed: gridded kernel, 3xTF32 tcgen05 grid product + 10-point interpolation per "
+                  "direction; compensated reference-antenna pass)" if gridded else
+                  "rotate_average (mixed: persistent TMA-pipelined kernel + compensated reference-antenna pass)")
     elif w.kernel_timing == "events":
         k_ms = ms
         k_name = "whole forward + backward step"
@@ -608,11 +663,25 @@ def run_gpu(args, rank: int, world: int):
             "note": "B_alg counts the visibilities once per direction; the kernel reads them once for all directions",
             "compute": {"fp32_issue_per_s": w.f_alg / (k_ms / 1e3), "fp32_peak_fma_per_s": 3.6e13,
                         "frac": w.f_alg / (k_ms / 1e3) / 3.6e13}}
+    if gridded and getattr(w, "grid_flops", None):
+        # Tensor pipe: the kernel's 3xTF32 MMA FLOPs (from its grid windows) against the TF32
+        # rate, half the measured dense BF16 rate.
+        tf32_peak = (peaks["bf16_tflops"] / 2 if peaks and "bf16_tflops" in peaks else 950.0) * 1e12
+        roof["compute"] = {"tensor_tf32_flops_per_s": w.grid_flops / (k_ms / 1e3), "tf32_peak_flops_per_s": tf32_peak,
+                           "frac": w.grid_flops / (k_ms / 1e3) / tf32_peak, "mma_flops_per_call": w.grid_flops,
+                           "peak_source": "half of MEASURED_PEAKS.json bf16_tflops (of measured)" if peaks else
+                                          "half of the 1.9 PFLOP/s bf16 fallback (of fallback)"}
+        roof["note"] = ("B_alg counts the visibilities once per direction (the reference's per-direction loop); the "
+                        "gridded kernel reads them once for all directions (hbm_read_once_frac)")
     if hasattr(w, "vis_bytes_resident"):
         roof["hbm_read_once_frac"] = w.vis_bytes_resident / (k_ms / 1e3) / 1e9 / peak
-    if w.traffic:
+    if gridded and getattr(w, "grid_traffic", None):
+        roof["traffic"] = w.grid_traffic
+    elif gridded:
+        roof["traffic"] = None
+    if roof["traffic"]:
         # the DRAM bytes the kernel actually moves (ncu-measured traffic) over its event time
-        roof["dram_traffic_frac"] = w.traffic / (k_ms / 1e3) / 1e9 / peak
+        roof["dram_traffic_frac"] = roof["traffic"] / (k_ms / 1e3) / 1e9 / peak
 
     cpu = None
     if rank == 0 and world == 1 and not args.skip_cpu:
@@ -642,6 +711,7 @@ def run_gpu(args, rank: int, world: int):
             "cpu_baseline": cpu,
             "plain_fp64": plain,
             "checks": checks or None,
+            "alternative_kernel": alt_kernel,
             "metadata_build_s": round(getattr(w, "metadata_s", 0.0), 3),
             "metadata_build": "leap_build_metadata (device pseudo-inverse) + host copies of A and Ad for the checks",
             "clocks": clocks,

@@ -115,7 +115,8 @@ struct leap_ctx {
   bool autotune = true;               // tune new batched shapes on first use
   bool tc_gemm = true;                // mixed form: Ad contraction on the tensor cores (3xTF32)
   int mma_rotate = 1;                 // tensor-core rotate + average: 0 never, 1 autotuner candidate, 2 always
-  int gridded = 0;                    // gridded rotate + average (tcgen05 grid product): 0 off, 1 on
+  int gridded = 2;                    // gridded rotate + average (tcgen05 grid product): 0 never, 1 always,
+                                      // 2 when every item has >= kGridAutoDirs directions
   bool grid_attr = false;
   std::map<int, DeviceBuffer> grid_tabs;  // grid matrix per channel count
   std::vector<GridItem> grid_items_host;
@@ -195,6 +196,10 @@ struct DeviceGuard {
 };
 
 constexpr int kPipeNC = 8;   // warps of the pipelined kernel
+// Directions per item from which the gridded kernel is the default: its grid product costs
+// about as much as ~25 directions of the pipelined kernel's per-direction work (measured on
+// 128 antennas x 384 channels: 64 directions 1.29 vs 2.86 ms; 8 per item 35 vs 14 ms).
+constexpr int kGridAutoDirs = 32;
 constexpr int kPipeDPW = 4;  // directions per warp
 
 int grid_1d(int64_t n, int threads) {
@@ -463,7 +468,10 @@ int rotate_stage(leap_ctx* ctx, const std::vector<WorkItem>& items, const double
               "upload wavelengths");
   }
 
-  if (all_pipe && ctx->gridded) return gridded_stage(ctx, items, d_dd, D, s, kernels);
+  // Gridded kernel: forced on, or by default when every item has enough directions to
+  // amortise the grid product (the tensor-core rotation option, when forced, wins).
+  if (all_pipe && (ctx->gridded == 1 || (ctx->gridded == 2 && ctx->mma_rotate != 2 && min_ndir >= kGridAutoDirs)))
+    return gridded_stage(ctx, items, d_dd, D, s, kernels);
   if (all_pipe) {
     // Kernel: the tensor-core one (16 directions per unit) when the autotuner chose it or the
     // option forces it (items of at least 12 directions); else the CUDA-core one with 4 tiles
@@ -1926,7 +1934,7 @@ int32_t leap_set_option(leap_ctx* ctx, int32_t option, int32_t value) {
       ctx->mma_rotate = value;
       return LEAP_OK;
     case LEAP_OPTION_GRIDDED_ROTATION:
-      if (value < 0 || value > 1) return fail(ctx, LEAP_ERR_INVALID_ARGUMENT, "gridded option must be 0 or 1");
+      if (value < 0 || value > 2) return fail(ctx, LEAP_ERR_INVALID_ARGUMENT, "gridded option must be 0, 1 or 2");
       ctx->gridded = value;
       return LEAP_OK;
     default: return fail(ctx, LEAP_ERR_INVALID_ARGUMENT, "unknown option");

@@ -223,8 +223,9 @@ int32_t leap_set_autotune(leap_ctx* ctx, int32_t enable);
                                                     at every direction's phase slope through a 2x-oversampled grid
                                                     (a type-2 non-uniform DFT): the grid values are one 3xTF32
                                                     tcgen05 product per tile, shared by all directions, then a
-                                                    10-point interpolation per (row, direction).  0: off (default);
-                                                    1: on */
+                                                    10-point interpolation per (row, direction).  0: never;
+                                                    1: always; 2 (default): when every work item has at least
+                                                    32 directions (unless the tensor-core rotation is forced) */
 int32_t leap_set_option(leap_ctx* ctx, int32_t option, int32_t value);
 
 /* Copy the avgData of `direction` from the last calibrate call to host memory

@@ -26,7 +26,7 @@ def _gridded(ctx, fn):
     try:
         return fn()
     finally:
-        ctx.set_option(LEAP_OPTION_GRIDDED_ROTATION, 0)
+        ctx.set_option(LEAP_OPTION_GRIDDED_ROTATION, 2)
 
 
 def _scale(obs):
@@ -113,6 +113,7 @@ def test_gridded_agrees_with_pipelined_kernel(ctx):
     ctx.set_metadata(md)
     ctx.set_integration(0, obs.vis, obs.uvw)
     dds = _dds(md, dirs)
+    ctx.set_option(LEAP_OPTION_GRIDDED_ROTATION, 0)
     ref = ctx.calibrate(0, dds, lg.LEAP_PRECISION_MIXED)
     got = _gridded(ctx, lambda: ctx.calibrate(0, dds, lg.LEAP_PRECISION_MIXED))
     assert np.abs(got - ref).max() <= 2 * MIXED_CAL_TOL
@@ -137,7 +138,7 @@ def test_gridded_batched_graph(ctx):
         cal = ctx.calibrate_batched(items, dds, lg.LEAP_PRECISION_MIXED)
         again = ctx.calibrate_batched(items, dds, lg.LEAP_PRECISION_MIXED)
     finally:
-        ctx.set_option(LEAP_OPTION_GRIDDED_ROTATION, 0)
+        ctx.set_option(LEAP_OPTION_GRIDDED_ROTATION, 2)
     for slot, (obs, dirs, d0) in enumerate(chunks):
         exp, avg_o = oracle.calibrate_interval(obs.vis, obs.uvw, dds[d0:d0 + len(dirs)], mdo, return_avg=True)
         assert_cal_close(cal[d0:d0 + len(dirs)], exp, avg_o, mdo, MIXED_CAL_TOL, 1e-4)
@@ -148,4 +149,21 @@ def test_gridded_batched_graph(ctx):
 
 def test_gridded_option_is_validated(ctx):
     with pytest.raises(lg.InvalidArgument):
-        ctx.set_option(LEAP_OPTION_GRIDDED_ROTATION, 2)
+        ctx.set_option(LEAP_OPTION_GRIDDED_ROTATION, 3)
+
+
+def test_gridded_auto_selection(ctx):
+    """Default (auto): items of >= 32 directions take the gridded kernel, fewer the
+    pipelined one; both agree with the oracle."""
+    obs, dirs = synth.small_case(stations=40, timesteps=6, channels=48, directions=40, vis_dtype=np.complex64,
+                                 seed_shift=21)
+    md = lg.build_metadata(obs)
+    mdo = oracle.metadata(obs)
+    ctx.set_metadata(md)
+    ctx.set_integration(0, obs.vis, obs.uvw)
+    dds = _dds(md, dirs)
+    cal_o, avg_o = oracle.calibrate_interval(obs.vis, obs.uvw, dds, mdo, return_avg=True)
+    for nd in (40, 8):
+        cal = ctx.calibrate(0, dds[:nd], lg.LEAP_PRECISION_MIXED)
+        assert_cal_close(cal, cal_o[:nd], avg_o[:nd], mdo, MIXED_CAL_TOL, 1e-4)
+    ctx.release_integration(0)
