@@ -174,13 +174,11 @@ __device__ __forceinline__ void tma_load_3d(void* smem_dst, const CUtensorMap* m
 }
 
 // Bounded wait that also gives up once another role has raised the abort flag.
-// Polls back off with a short sleep so that waiting warps leave the issue slots to
-// the working ones.
+// (mbarrier.try_wait itself suspends the thread for a while when the phase is not complete.)
 __device__ __forceinline__ bool grid_wait(uint64_t* bar, uint32_t parity, volatile int* abort_flag) {
   for (uint32_t i = 0; i < kMaxWaitPolls; ++i) {
     if (mbar_try_wait(bar, parity)) return true;
     if ((i & 63u) == 63u && *abort_flag) return false;
-    __nanosleep(i < 8 ? 20 : 100);
   }
   return false;
 }
