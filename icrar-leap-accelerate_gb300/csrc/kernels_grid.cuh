@@ -344,6 +344,35 @@ __device__ __forceinline__ void grid_fold(uint32_t lanes, uint32_t dst, uint32_t
   asm volatile("tcgen05.wait::st.sync.aligned;" ::: "memory");
 }
 
+// The four correction MMAs of a 16-channel chunk (lo*hi and hi*lo of both k-steps) into one
+// accumulator, from one statement: acc0 = 0 overwrites the accumulator with the first.
+__device__ __forceinline__ void grid_mma_corrections(uint32_t d, uint64_t ah, uint64_t al, uint64_t bh, uint64_t bl,
+                                                     uint64_t ka, uint64_t kb, uint32_t idesc, uint32_t acc0) {
+  asm volatile(
+      "{\n\t.reg .pred p, t;\n\t"
+      "setp.ne.b32 p, %9, 0;\n\t"
+      "setp.eq.b32 t, %9, %9;\n\t"
+      "tcgen05.mma.cta_group::1.kind::tf32 [%0], %1, %2, %8, p;\n\t"
+      "tcgen05.mma.cta_group::1.kind::tf32 [%0], %3, %4, %8, t;\n\t"
+      "tcgen05.mma.cta_group::1.kind::tf32 [%0], %5, %6, %8, t;\n\t"
+      "tcgen05.mma.cta_group::1.kind::tf32 [%0], %7, %10, %8, t;\n\t}" ::"r"(d),
+      "l"(al), "l"(bh), "l"(ah), "l"(bl), "l"(al + ka), "l"(bh + kb), "l"(ah + ka), "r"(idesc), "r"(acc0), "l"(bl + kb)
+      : "memory");
+}
+
+// The two hi*hi MMAs (both k-steps) of a chunk.
+__device__ __forceinline__ void grid_mma_hihi(uint32_t d, uint64_t ah, uint64_t bh, uint64_t ka, uint64_t kb,
+                                              uint32_t idesc, uint32_t acc0) {
+  asm volatile(
+      "{\n\t.reg .pred p, t;\n\t"
+      "setp.ne.b32 p, %6, 0;\n\t"
+      "setp.eq.b32 t, %6, %6;\n\t"
+      "tcgen05.mma.cta_group::1.kind::tf32 [%0], %1, %2, %5, p;\n\t"
+      "tcgen05.mma.cta_group::1.kind::tf32 [%0], %3, %4, %5, t;\n\t}" ::"r"(d),
+      "l"(ah), "l"(bh), "l"(ah + ka), "l"(bh + kb), "r"(idesc), "r"(acc0)
+      : "memory");
+}
+
 __device__ __forceinline__ void tc_commit(uint64_t* bar) {
   asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(smem_u32(bar))
                : "memory");
@@ -489,18 +518,14 @@ __global__ void __launch_bounds__(kGrThreads, 1) rotate_average_gridded(const Gr
                 const uint64_t al = ah + (2 * 4096 >> 4), bl = bh + static_cast<uint64_t>(4 * w.jw * 2);
                 const uint64_t ka = 4096 >> 4, kb = static_cast<uint64_t>(2 * w.jw * 2);
                 // Corrections first: they give the fold of the previous segment time to finish.
-                tc_mma_tf32(tmem + kGrAC, al, bh, idesc, q > 0 ? 1u : 0u);
-                tc_mma_tf32(tmem + kGrAC, ah, bl, idesc, 1u);
-                tc_mma_tf32(tmem + kGrAC, al + ka, bh + kb, idesc, 1u);
-                tc_mma_tf32(tmem + kGrAC, ah + ka, bl + kb, idesc, 1u);
+                grid_mma_corrections(tmem + kGrAC, ah, al, bh, bl, ka, kb, idesc, q > 0 ? 1u : 0u);
                 if (seg >= 2 && qs == 0 && !grid_wait(is_empty, (mids - 1) & 1, abort_flag)) {
                   grid_fail(p, abort_flag);
                   ok = false;
                   break;
                 }
                 const uint32_t dst = seg == 0 ? rs : tmem + kGrIS;
-                tc_mma_tf32(dst, ah, bh, idesc, qs > 0 ? 1u : 0u);
-                tc_mma_tf32(dst, ah + ka, bh + kb, idesc, 1u);
+                grid_mma_hihi(dst, ah, bh, ka, kb, idesc, qs > 0 ? 1u : 0u);
                 issued = true;
                 if (seg >= 1 && qs == kGrSegChunks - 1 && q != I.nchunk - 1) {
                   tc_commit(is_full);  // a middle segment, folded by the converters
