@@ -22,16 +22,17 @@
 // Tile: M = 128 rows of the product = 4 baselines x 4 timesteps x 4 pols x
 // (re, im).  TMEM lane m = 32 q + 8 t + 2 p + s holds baseline q of the quad, so
 // each 32-lane quarter is one baseline at 4 neighbouring timesteps, whose grid
-// positions differ by far less than a grid step: one warp-uniform tcgen05.ld of
-// W + 1 columns serves all 32 lanes of a direction.
+// positions differ by far less than a grid step: one warp-uniform 16-column
+// tcgen05.ld per accumulator half serves all 32 lanes of a direction.
 //
 // The product runs in 3xTF32 (V E ~ V_hi E_hi + V_lo E_hi + V_hi E_lo with hi = tf32(x),
 // lo = tf32(x - hi)).  The tensor cores accumulate FP32 with truncation, whose error
 // grows with the number of accumulation steps and the size of the accumulator; so the
 // large hi*hi products restart in a fresh accumulator every 64 channels (a "segment")
-// and the small corrections go to an accumulator of their own.  Converter warps add the segments together with
-// rounded FP32 adds.  Measured on 128 antennas x 384 channels this keeps the
-// averages within ~5e-7 of the FP64 sums (relative to the sum of |terms|).
+// and the small corrections go to an accumulator of their own.  Converter warps add
+// the segments together with rounded FP32 adds.  Measured on 128 antennas x 384
+// channels this keeps the averages within ~5e-7 of the FP64 sums (relative to the
+// sum of |terms|).
 //
 // TMEM (512 columns, one block per SM): RS[0], RS[1] (running sums, double
 // buffered: the epilogue reads one while the next tile accumulates into the
@@ -42,11 +43,10 @@
 // converters (split the visibility box into K-major hi/lo blocks, and fold the
 // accumulators), 6-13 = epilogue (warp w reads TMEM lanes 32 (w % 4) ..; two
 // warps per quarter take 32 directions each).  One ring of kGrStages stages of
-// {visibility box, E window, packed A}, released by one MMA commit per stage: the
-// single MMA-issuing thread shares its scheduler with epilogue warps, so its
-// per-chunk instruction count bounds the kernel.  Every wait is bounded; a timeout sets the error word, stops
-// every role, and the block still waits (bounded) for its copies and MMAs and
-// frees its TMEM.
+// {visibility box (overwritten by A hi), A lo, E window}, handed over in pairs and
+// released by one MMA commit per pair.  Every wait is bounded; a timeout sets the
+// error word, stops every role, and the block still waits (bounded) for its copies
+// and MMAs and frees its TMEM.
 #pragma once
 
 #include "leap_common.cuh"
@@ -64,7 +64,7 @@ constexpr int kGrMacroStages = kGrStages / kGrMacro;
 constexpr int kGrJwMax = 64;          // grid points per pass (MMA N = 2 Jw <= 128)
 constexpr int kGrPassStride = 48;     // grid points between pass windows (multiple of 8)
 constexpr int kGrLoadCols = 16;       // TMEM columns one interpolation load reads
-constexpr int kGrDirs = 64;           // directions per unit (16 epilogue warps x 16 / 4 quarters)
+constexpr int kGrDirs = 64;           // directions per unit (8 epilogue warps x 32 / 4 quarters)
 constexpr int kGrEpiWarps = 8;
 constexpr int kGrWarpDirs = kGrDirs * 4 / kGrEpiWarps;  // directions per epilogue warp
 constexpr int kGrWarps = 6 + kGrEpiWarps;
@@ -382,7 +382,7 @@ template <int W>
 __global__ void __launch_bounds__(kGrThreads, 1) rotate_average_gridded(const GridParams p) {
   extern __shared__ __align__(128) unsigned char grid_smem[];
   unsigned char* smem = grid_smem;
-  unsigned char* ve = smem;                                          // [kGrStages][V | E | A]
+  unsigned char* ve = smem;                                          // [kGrStages][V then A hi | A lo | E]
   float2* tab = reinterpret_cast<float2*>(smem + kGrStages * kGrStageBytes);
   float* rec_all = reinterpret_cast<float*>(tab + kTwiddleSize);
   uint64_t* bars = reinterpret_cast<uint64_t*>(rec_all + kGrRecBytes / 4);
