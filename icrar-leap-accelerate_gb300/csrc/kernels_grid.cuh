@@ -198,24 +198,38 @@ static __global__ void grid_windows(const GridParams p) {
   const GridItem& I = p.items[g.item];
   const int n = 2 * I.C;
   const int nd = min(kGrDirs, I.ndir - g.dg * kGrDirs);
-  const int nrow = (g.t_hi - g.t_lo) * 4;
-  int smin = 0x7fffffff, smax = -0x7fffffff;
-  for (int e = lane; e < nrow * nd; e += 32) {
-    const int ri = e / nd, dj = e % nd;
-    const int t = g.t_lo + (ri >> 2), b = g.quad * 4 + (ri & 3);
-    if (b >= p.nbl) continue;
-    const int64_t r = static_cast<int64_t>(t) * p.nbl + b;
-    const int d = I.dir0 + g.dg * kGrDirs + dj;
-    float x[6], kb[6];
+  // Lanes hold the slopes of directions lane and lane + 32 and walk the unit's rows;
+  // a row's UVWs are one broadcast load for the warp.
+  static_assert(kGrDirs == 64, "two directions per lane");
+  float kb[2][6];
+  bool has[2];
 #pragma unroll
-    for (int i = 0; i < 6; ++i) {
-      x[i] = __ldg(I.uvw_f + 6 * r + i);
-      kb[i] = __ldg(p.dirk + 12 * d + 6 + i);
+  for (int h = 0; h < 2; ++h) {
+    const int dj = lane + 32 * h;
+    has[h] = dj < nd;
+    const int d = I.dir0 + g.dg * kGrDirs + min(dj, nd - 1);
+#pragma unroll
+    for (int i = 0; i < 6; ++i) kb[h][i] = __ldg(p.dirk + 12 * d + 6 + i);
+  }
+  int smin = 0x7fffffff, smax = -0x7fffffff;
+  for (int t = g.t_lo; t < g.t_hi; ++t) {
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+      const int b = g.quad * 4 + q;
+      if (b >= p.nbl) continue;
+      const int64_t r = static_cast<int64_t>(t) * p.nbl + b;
+      float x[6];
+#pragma unroll
+      for (int i = 0; i < 6; ++i) x[i] = __ldg(I.uvw_f + 6 * r + i);
+#pragma unroll
+      for (int h = 0; h < 2; ++h) {
+        if (!has[h]) continue;
+        float f;
+        const int s = grid_position(df_dot3_turns_u32(kb[h], x), n, f) - kGrTaps / 2 + 1;
+        smin = min(smin, s);
+        smax = max(smax, s);
+      }
     }
-    float f;
-    const int s = grid_position(df_dot3_turns_u32(kb, x), n, f) - kGrTaps / 2 + 1;
-    smin = min(smin, s);
-    smax = max(smax, s);
   }
   smin = __reduce_min_sync(0xffffffffu, smin);
   smax = __reduce_max_sync(0xffffffffu, smax);

@@ -139,48 +139,55 @@ __device__ __forceinline__ void issue_chunk(const ChunkCursor& k, const PipePara
     tma_load_2d(dst + ts * CH * kPipeItemBytes, &it.map, (k.t * p.nbl + (tg * TPB + ts) * 32) * 8, k.cb, &full[st]);
 }
 
-// One channel of the complex multiply-accumulate for DPW directions and 4 pols; each
-// accumulator and phasor is a (re, im) float2.  PAIRED: on paired FP32 FMAs (FFMA2), one
-// __ffma2_rn per product pair and for the phasor step z <- z * w; else on scalar FMAs.
-// Measured on GB300: the 4-tile / 8-direction kernel runs faster paired (batched workload
-// 14.16 -> 13.84 ms), the 1-tile / 32-direction kernel slower (2.86 -> 3.04 ms per call).
-template <int DPW, bool PAIRED>
+// One channel of the complex multiply-accumulate for DPW directions and 4 pols on scalar
+// FMAs; each accumulator and phasor is a (re, im) float2.  The 4-tile kernel uses the
+// paired form below (FFMA2).
+template <int DPW>
 __device__ __forceinline__ void mac_channel(const unsigned char* src, int h, float2 (&acc)[DPW][4], float2 (&z)[DPW],
-                                            const float2 (&w)[DPW], const float2 (&wn)[DPW]) {
+                                            const float2 (&w)[DPW]) {
   const float4 x0 = *reinterpret_cast<const float4*>(src + 16 * h);
   const float4 x1 = *reinterpret_cast<const float4*>(src + 16 * (1 - h));
   const float vr[4] = {x0.x, x0.z, x1.x, x1.z};
   const float vi[4] = {x0.y, x0.w, x1.y, x1.w};
-  if (!PAIRED) {
-#pragma unroll
-    for (int j = 0; j < DPW; ++j) {
-#pragma unroll
-      for (int q = 0; q < 4; ++q) {
-        acc[j][q].x = fmaf(vr[q], z[j].x, fmaf(-vi[q], z[j].y, acc[j][q].x));
-        acc[j][q].y = fmaf(vr[q], z[j].y, fmaf(vi[q], z[j].x, acc[j][q].y));
-      }
-      const float nr = fmaf(z[j].x, w[j].x, -z[j].y * w[j].y);
-      z[j].y = fmaf(z[j].x, w[j].y, z[j].y * w[j].x);
-      z[j].x = nr;
-    }
-    return;
-  }
-  float2 vrr[4], vni[4];
-#pragma unroll
-  for (int q = 0; q < 4; ++q) {
-    vrr[q] = make_float2(vr[q], vr[q]);
-    vni[q] = make_float2(-vi[q], vi[q]);
-  }
 #pragma unroll
   for (int j = 0; j < DPW; ++j) {
-    const float2 zs = make_float2(z[j].y, z[j].x);
 #pragma unroll
     for (int q = 0; q < 4; ++q) {
-      acc[j][q] = __ffma2_rn(vrr[q], z[j], acc[j][q]);  // (vr zr, vr zi)
-      acc[j][q] = __ffma2_rn(vni[q], zs, acc[j][q]);    // (-vi zi, vi zr)
+      acc[j][q].x = fmaf(vr[q], z[j].x, fmaf(-vi[q], z[j].y, acc[j][q].x));
+      acc[j][q].y = fmaf(vr[q], z[j].y, fmaf(vi[q], z[j].x, acc[j][q].y));
     }
-    // z' = zr (wr, wi) + zi (-wi, wr)
-    z[j] = __ffma2_rn(make_float2(z[j].x, z[j].x), w[j], __fmul2_rn(make_float2(z[j].y, z[j].y), wn[j]));
+    const float nr = fmaf(z[j].x, w[j].x, -z[j].y * w[j].y);
+    z[j].y = fmaf(z[j].x, w[j].y, z[j].y * w[j].x);
+    z[j].x = nr;
+  }
+}
+
+// Paired form: each visibility enters as its natural (re, im) register pair from the
+// shared-memory load, and the phasor and step are held twice over, zr2 = (zr, zr),
+// zi2 = (zi, zi), wr2 = (wr, wr), wi2 = (wi, wi), wm2 = (-wi, -wi), so that no FFMA2
+// operand needs a register move:
+//     acc_a += (vr, vi) * zr2 = (vr zr, vi zr),   acc_b += (vr, vi) * zi2 = (vr zi, vi zi),
+// and the fold takes re = acc_a.x - acc_b.y, im = acc_b.x + acc_a.y.  The phasor step
+// rounds exactly as in mac_channel (zr' = fma(zr, wr, zi * -wi), zi' = fma(zr, wi, zi * wr)).
+template <int DPW>
+__device__ __forceinline__ void mac_channel_paired(const unsigned char* src, int h, float2 (&acc_a)[DPW][4],
+                                                   float2 (&acc_b)[DPW][4], float2 (&zr2)[DPW], float2 (&zi2)[DPW],
+                                                   const float2 (&wr2)[DPW], const float2 (&wi2)[DPW],
+                                                   const float2 (&wm2)[DPW]) {
+  const float4 x0 = *reinterpret_cast<const float4*>(src + 16 * h);
+  const float4 x1 = *reinterpret_cast<const float4*>(src + 16 * (1 - h));
+  const float2 v[4] = {make_float2(x0.x, x0.y), make_float2(x0.z, x0.w), make_float2(x1.x, x1.y),
+                       make_float2(x1.z, x1.w)};
+#pragma unroll
+  for (int j = 0; j < DPW; ++j) {
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+      acc_a[j][q] = __ffma2_rn(v[q], zr2[j], acc_a[j][q]);
+      acc_b[j][q] = __ffma2_rn(v[q], zi2[j], acc_b[j][q]);
+    }
+    const float2 nr = __ffma2_rn(zr2[j], wr2[j], __fmul2_rn(zi2[j], wm2[j]));
+    zi2[j] = __ffma2_rn(zr2[j], wi2[j], __fmul2_rn(zi2[j], wr2[j]));
+    zr2[j] = nr;
   }
 }
 
@@ -189,6 +196,7 @@ __global__ void __launch_bounds__(NC * 32, 1) rotate_average_mixed_pipe(const Pi
   constexpr int CH = PipeShape<TPB>::CH;
   constexpr int NS = PipeShape<TPB>::STAGES;
   constexpr int WPT = NC / TPB;  // warps (direction groups of DPW) per tile
+  constexpr bool PAIRED = TPB > 1;  // FFMA2 multiply-accumulate (mac_channel_paired)
   static_assert(NC % TPB == 0, "warps must divide among tiles");
   extern __shared__ __align__(128) unsigned char smem[];
   unsigned char* stage_mem = smem;
@@ -250,7 +258,7 @@ __global__ void __launch_bounds__(NC * 32, 1) rotate_average_mixed_pipe(const Pi
 
     for (int t = t_lo; t < t_hi && ok; ++t) {
       uint32_t pa[DPW], pb[DPW];
-      float2 w[DPW], wn[DPW];
+      float2 w[DPW], wr2[DPW], wi2[DPW], wm2[DPW];
       if (active) {
         // turns(c) = A + c*B, A = -(l*u + m*v + (n-1)*w)*f0/c, B likewise with df.
         const int64_t r = static_cast<int64_t>(t) * p.nbl + (valid ? b : 0);
@@ -271,15 +279,18 @@ __global__ void __launch_bounds__(NC * 32, 1) rotate_average_mixed_pipe(const Pi
           float wr, wi;
           twiddle_turns(pb[j], tab, wr, wi);
           w[j] = make_float2(wr, wi);
-          wn[j] = make_float2(-wi, wr);
+          wr2[j] = make_float2(wr, wr);
+          wi2[j] = make_float2(wi, wi);
+          wm2[j] = make_float2(-wi, -wi);
         }
       }
       // FP32 partial sums of up to kPipeFold channels, then a Kahan fold.
-      float2 acc[DPW][4];
+      // Paired form: acc holds (vr zr, vi zr) and acc_b (vr zi, vi zi); else acc = (re, im).
+      float2 acc[DPW][4], acc_b[DPW][4];
 #pragma unroll
       for (int j = 0; j < DPW; ++j)
 #pragma unroll
-        for (int q = 0; q < 4; ++q) acc[j][q] = make_float2(0.f, 0.f);
+        for (int q = 0; q < 4; ++q) acc[j][q] = acc_b[j][q] = make_float2(0.f, 0.f);
       for (int cb = 0; cb < C; cb += CH, ++it) {
         const int n = min(CH, C - cb);
         const int st = it % NS;
@@ -289,26 +300,39 @@ __global__ void __launch_bounds__(NC * 32, 1) rotate_average_mixed_pipe(const Pi
           break;
         }
         if (active) {
-          float2 z[DPW];
+          float2 z[DPW], zr2[DPW], zi2[DPW];
           const unsigned char* src = stage_mem + st * pipe_stage_bytes<TPB>() + ts * CH * kPipeItemBytes + lane * 32;
           if (n == CH) {
 #pragma unroll
             for (int sub = 0; sub < CH; sub += kPipeReseed) {
 #pragma unroll
-              for (int j = 0; j < DPW; ++j)
+              for (int j = 0; j < DPW; ++j) {
                 twiddle_turns(pa[j] + static_cast<uint32_t>(cb + sub) * pb[j], tab, z[j].x, z[j].y);
+                zr2[j] = make_float2(z[j].x, z[j].x);
+                zi2[j] = make_float2(z[j].y, z[j].y);
+              }
 #pragma unroll
-              for (int k = 0; k < kPipeReseed; ++k)
-                mac_channel<DPW, (TPB > 1)>(src + (sub + k) * kPipeItemBytes, h, acc, z, w, wn);
+              for (int k = 0; k < kPipeReseed; ++k) {
+                if constexpr (PAIRED)
+                  mac_channel_paired<DPW>(src + (sub + k) * kPipeItemBytes, h, acc, acc_b, zr2, zi2, wr2, wi2, wm2);
+                else
+                  mac_channel<DPW>(src + (sub + k) * kPipeItemBytes, h, acc, z, w);
+              }
             }
           } else {
             for (int k = 0; k < n; ++k) {
               if (k % kPipeReseed == 0) {
 #pragma unroll
-                for (int j = 0; j < DPW; ++j)
+                for (int j = 0; j < DPW; ++j) {
                   twiddle_turns(pa[j] + static_cast<uint32_t>(cb + k) * pb[j], tab, z[j].x, z[j].y);
+                  zr2[j] = make_float2(z[j].x, z[j].x);
+                  zi2[j] = make_float2(z[j].y, z[j].y);
+                }
               }
-              mac_channel<DPW, (TPB > 1)>(src + k * kPipeItemBytes, h, acc, z, w, wn);
+              if constexpr (PAIRED)
+                mac_channel_paired<DPW>(src + k * kPipeItemBytes, h, acc, acc_b, zr2, zi2, wr2, wi2, wm2);
+              else
+                mac_channel<DPW>(src + k * kPipeItemBytes, h, acc, z, w);
             }
           }
           if ((cb + CH) % kPipeFold == 0 || cb + CH >= C) {
@@ -316,15 +340,17 @@ __global__ void __launch_bounds__(NC * 32, 1) rotate_average_mixed_pipe(const Pi
             for (int j = 0; j < DPW; ++j)
 #pragma unroll
               for (int q = 0; q < 4; ++q) {
-                float y = acc[j][q].x - cr[j][q];
+                const float re = PAIRED ? acc[j][q].x - acc_b[j][q].y : acc[j][q].x;
+                const float im = PAIRED ? acc_b[j][q].x + acc[j][q].y : acc[j][q].y;
+                float y = re - cr[j][q];
                 float tt = sr[j][q] + y;
                 cr[j][q] = (tt - sr[j][q]) - y;
                 sr[j][q] = tt;
-                y = acc[j][q].y - ci[j][q];
+                y = im - ci[j][q];
                 tt = si[j][q] + y;
                 ci[j][q] = (tt - si[j][q]) - y;
                 si[j][q] = tt;
-                acc[j][q] = make_float2(0.f, 0.f);
+                acc[j][q] = acc_b[j][q] = make_float2(0.f, 0.f);
               }
           }
         }

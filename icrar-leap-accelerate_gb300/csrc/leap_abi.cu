@@ -702,10 +702,16 @@ int refant_stage(leap_ctx* ctx, const std::vector<WorkItem>& items, const double
   int64_t partial_elems = 0;
   std::vector<int64_t> off;
   int blocks = 0;
-  // Each block sums <= 4*DPW directions of 32 reference baselines over a slab;
-  // about 8 blocks per SM in total.
-  int64_t base_total = 0;
-  for (const auto& w : items) base_total += static_cast<int64_t>(rtiles) * ((w.ndir + 7) / 8);
+  // Each block sums 4*DPW directions of 32 reference baselines over a slab of
+  // (timestep, channel) pairs.  Slabs are sized to one budget across items (about
+  // 16 blocks per SM in total), so that chunks of 1 x 48 and 64 x 384 samples give
+  // blocks of similar length instead of the same number of blocks each.
+  int64_t work_total = 0;
+  for (const auto& w : items) {
+    const Integration& in = ctx->integ.at(w.slot);
+    work_total += (in.rows / nbl) * in.channels * rtiles * ((w.ndir + 7) / 8);
+  }
+  const int64_t slab_budget = std::max<int64_t>(64, (work_total + 16 * ctx->sms - 1) / (16 * ctx->sms));
   for (const auto& w : items) {
     Integration& in = ctx->integ.at(w.slot);
     const int T = static_cast<int>(in.rows / nbl);
@@ -755,13 +761,15 @@ int refant_stage(leap_ctx* ctx, const std::vector<WorkItem>& items, const double
     r.pols = in.pols;
     r.ndir = w.ndir;
     r.dgroups = (w.ndir + 7) / 8;  // 4 warps x 2 directions
-    const int64_t want = std::max<int64_t>(1, (8 * static_cast<int64_t>(ctx->sms) + base_total - 1) / base_total);
+    const int64_t want =
+        std::max<int64_t>(1, (static_cast<int64_t>(T) * in.channels + slab_budget - 1) / slab_budget);
     r.n_tslab = static_cast<int>(std::min<int64_t>(T, want));
     r.t_per_slab = (T + r.n_tslab - 1) / r.n_tslab;
     r.n_tslab = (T + r.t_per_slab - 1) / r.t_per_slab;
     const int64_t rest = (want + r.n_tslab - 1) / r.n_tslab;
     r.n_cslab = static_cast<int>(std::min<int64_t>(rest, std::max(1, in.channels / 16)));
     r.c_per_slab = (in.channels + r.n_cslab - 1) / r.n_cslab;
+    if (r.n_cslab > 1) r.c_per_slab = (r.c_per_slab + 15) / 16 * 16;  // whole blocks of kRefantPrefetch loads
     r.n_cslab = (in.channels + r.c_per_slab - 1) / r.c_per_slab;
     r.block_begin = blocks;
     blocks += rtiles * r.dgroups * r.n_tslab * r.n_cslab;
