@@ -581,6 +581,9 @@ def run_gpu(args, rank: int, world: int):
         near = margin < 1e-5
         plain = {"value": w.units * world / (ms64 / 1e3), "ms_per_step": ms64, "dtype": "f64",
                  "mixed_vs_fp64_max_cal_err_rad": float(per_dir[~near].max()) if (~near).any() else None,
+                 "mixed_vs_fp64_cal_err_rad_median_p99": ([float(np.median(per_dir[~near])),
+                                                           float(np.percentile(per_dir[~near], 99))]
+                                                          if (~near).any() else None),
                  "directions_near_branch_cut": int(near.sum()),
                  "max_cal_err_rad_incl_branch_cut_directions": float(per_dir.max()),
                  "speedup_mixed_over_fp64": ms64 / ms,

@@ -29,10 +29,11 @@
 // every kPipeReseed channels and advanced by one FP32 complex multiply per
 // channel in between (drift over 16 steps ~1e-6; it reaches the cal phases
 // only through baselines that the reference-antenna pass does not cover, with
-// weight ~1/S).  Sums: FP32 over two 16-channel chunks, folded into Kahan
-// pairs.  Reseeding every 16 rather than 8 channels and folding every 32 rather
-// than 16 cut the 128-antenna call from 3.00 to 2.85 ms and moved its cal-phase
-// difference from the FP64 form from 5.5e-7 to 2.1e-6 rad (bar: 1e-5).
+// weight ~1/S).  Sums: FP32 over 32 (1 tile) or 64 (4 tiles) channels, folded
+// into Kahan pairs.  Reseeding every 16 rather than 8 channels and folding
+// every 32 rather than 16 cut the 128-antenna call from 3.00 to 2.85 ms and
+// moved its cal-phase difference from the FP64 form from 5.5e-7 to 2.1e-6 rad
+// (bar: 1e-5).
 //
 // Shared-memory reads: lane i reads its 32 bytes as two 16-byte halves; lanes
 // with bit 2 set read the upper half first so that each quarter-warp covers
@@ -68,14 +69,18 @@ struct PipeParams {
 
 constexpr int kPipeMaxItems = 128;
 constexpr int kPipeReseed = 16;         // channels between table-accurate twiddles
-constexpr int kPipeFold = 32;           // channels summed in FP32 before a Kahan fold
 constexpr int kPipeItemBytes = 32 * 4 * 8;  // one channel of one tile: 32 baselines x 4 pols x complex<float>
 
 // Channels per chunk and ring depth: 1 tile x 16 channels = 16 KB stages, 4 deep; 4 tiles x
-// 16 channels = 64 KB stages, 3 deep (192 KB of the 227 KB of shared memory).
+// 16 channels = 64 KB stages, 3 deep (192 KB of the 227 KB of shared memory).  FOLD: channels
+// summed in FP32 before a Kahan fold.  The 4-tile kernel folds every 64 channels: its fold is
+// ~6% of its FMA-pipe work at 32, and the FP32 partial sums over 64 channels (~2e-8 of the
+// sum of |terms|) stay far below the phasor drift between reseeds (~1e-6).  Measured on the
+// 32-chunk batched workload: 11.47 -> 11.10 ms per call; cal-phase difference from the FP64
+// form over 256 directions: median 1.1e-7 -> 1.2e-7 rad, maximum 4.7e-6 -> 4.2e-6 rad.
 template <int TPB> struct PipeShape;
-template <> struct PipeShape<1> { static constexpr int CH = 16, STAGES = 4; };
-template <> struct PipeShape<4> { static constexpr int CH = 16, STAGES = 3; };
+template <> struct PipeShape<1> { static constexpr int CH = 16, STAGES = 4, FOLD = 32; };
+template <> struct PipeShape<4> { static constexpr int CH = 16, STAGES = 3, FOLD = 64; };
 
 template <int TPB>
 __host__ __device__ constexpr int pipe_stage_bytes() { return TPB * PipeShape<TPB>::CH * kPipeItemBytes; }
@@ -162,32 +167,32 @@ __device__ __forceinline__ void mac_channel(const unsigned char* src, int h, flo
   }
 }
 
-// Paired form: each visibility enters as its natural (re, im) register pair from the
-// shared-memory load, and the phasor and step are held twice over, zr2 = (zr, zr),
-// zi2 = (zi, zi), wr2 = (wr, wr), wi2 = (wi, wi), wm2 = (-wi, -wi), so that no FFMA2
-// operand needs a register move:
-//     acc_a += (vr, vi) * zr2 = (vr zr, vi zr),   acc_b += (vr, vi) * zi2 = (vr zi, vi zi),
-// and the fold takes re = acc_a.x - acc_b.y, im = acc_b.x + acc_a.y.  The phasor step
-// rounds exactly as in mac_channel (zr' = fma(zr, wr, zi * -wi), zi' = fma(zr, wi, zi * wr)).
+// Paired form: each visibility enters as its natural (re, im) register pair v from the
+// shared-memory load and once swapped, vs = (im, re), shared by the DPW directions; the
+// phasor stays a natural (zr, zi) pair advanced by the scalar step of mac_channel.  Then
+//     acc_a += v * z = (vr zr, vi zi),   acc_b += vs * z = (vi zr, vr zi),
+// and the fold takes re = acc_a.x - acc_a.y, im = acc_b.x + acc_b.y: 16 paired FMAs (32
+// FMA-pipe cycles) and 4 scalar ones per direction and channel, no per-direction moves.
 template <int DPW>
 __device__ __forceinline__ void mac_channel_paired(const unsigned char* src, int h, float2 (&acc_a)[DPW][4],
-                                                   float2 (&acc_b)[DPW][4], float2 (&zr2)[DPW], float2 (&zi2)[DPW],
-                                                   const float2 (&wr2)[DPW], const float2 (&wi2)[DPW],
-                                                   const float2 (&wm2)[DPW]) {
+                                                   float2 (&acc_b)[DPW][4], float2 (&z)[DPW],
+                                                   const float2 (&w)[DPW]) {
   const float4 x0 = *reinterpret_cast<const float4*>(src + 16 * h);
   const float4 x1 = *reinterpret_cast<const float4*>(src + 16 * (1 - h));
   const float2 v[4] = {make_float2(x0.x, x0.y), make_float2(x0.z, x0.w), make_float2(x1.x, x1.y),
                        make_float2(x1.z, x1.w)};
+  const float2 vs[4] = {make_float2(x0.y, x0.x), make_float2(x0.w, x0.z), make_float2(x1.y, x1.x),
+                        make_float2(x1.w, x1.z)};
 #pragma unroll
   for (int j = 0; j < DPW; ++j) {
 #pragma unroll
     for (int q = 0; q < 4; ++q) {
-      acc_a[j][q] = __ffma2_rn(v[q], zr2[j], acc_a[j][q]);
-      acc_b[j][q] = __ffma2_rn(v[q], zi2[j], acc_b[j][q]);
+      acc_a[j][q] = __ffma2_rn(v[q], z[j], acc_a[j][q]);
+      acc_b[j][q] = __ffma2_rn(vs[q], z[j], acc_b[j][q]);
     }
-    const float2 nr = __ffma2_rn(zr2[j], wr2[j], __fmul2_rn(zi2[j], wm2[j]));
-    zi2[j] = __ffma2_rn(zr2[j], wi2[j], __fmul2_rn(zi2[j], wr2[j]));
-    zr2[j] = nr;
+    const float nr = fmaf(z[j].x, w[j].x, -z[j].y * w[j].y);
+    z[j].y = fmaf(z[j].x, w[j].y, z[j].y * w[j].x);
+    z[j].x = nr;
   }
 }
 
@@ -248,7 +253,9 @@ __global__ void __launch_bounds__(NC * 32, 1) rotate_average_mixed_pipe(const Pi
     const int b = (tg * TPB + ts) * 32 + lane;
     const bool valid = b < p.nbl;
     const int jd0 = (dg * WPT + dsub) * DPW;  // first direction of this warp within the item
-    const bool active = jd0 < I.ndir;
+    // A tile wholly past the last baseline (the last tile group when nbl is not a multiple
+    // of 32 * TPB) only takes part in the stage hand-over.
+    const bool active = jd0 < I.ndir && (tg * TPB + ts) * 32 < p.nbl;
 
     float sr[DPW][4], si[DPW][4], cr[DPW][4], ci[DPW][4];
 #pragma unroll
@@ -256,15 +263,25 @@ __global__ void __launch_bounds__(NC * 32, 1) rotate_average_mixed_pipe(const Pi
 #pragma unroll
       for (int q = 0; q < 4; ++q) sr[j][q] = si[j][q] = cr[j][q] = ci[j][q] = 0.f;
 
+    // The row's split UVWs are loaded one timestep ahead, so that the set-up of a
+    // timestep does not wait on a global load.
+    float xn[6];
+#pragma unroll
+    for (int i = 0; i < 6; ++i)
+      xn[i] = active ? __ldg(I.uvw_f + 6 * (static_cast<int64_t>(t_lo) * p.nbl + (valid ? b : 0)) + i) : 0.f;
     for (int t = t_lo; t < t_hi && ok; ++t) {
       uint32_t pa[DPW], pb[DPW];
-      float2 w[DPW], wr2[DPW], wi2[DPW], wm2[DPW];
+      float2 w[DPW];
       if (active) {
         // turns(c) = A + c*B, A = -(l*u + m*v + (n-1)*w)*f0/c, B likewise with df.
-        const int64_t r = static_cast<int64_t>(t) * p.nbl + (valid ? b : 0);
         float x[6];
 #pragma unroll
-        for (int i = 0; i < 6; ++i) x[i] = __ldg(I.uvw_f + 6 * r + i);
+        for (int i = 0; i < 6; ++i) x[i] = xn[i];
+        if (t + 1 < t_hi) {
+          const int64_t rn = static_cast<int64_t>(t + 1) * p.nbl + (valid ? b : 0);
+#pragma unroll
+          for (int i = 0; i < 6; ++i) xn[i] = __ldg(I.uvw_f + 6 * rn + i);
+        }
 #pragma unroll
         for (int j = 0; j < DPW; ++j) {
           const int d = I.dir0 + min(jd0 + j, I.ndir - 1);
@@ -279,13 +296,10 @@ __global__ void __launch_bounds__(NC * 32, 1) rotate_average_mixed_pipe(const Pi
           float wr, wi;
           twiddle_turns(pb[j], tab, wr, wi);
           w[j] = make_float2(wr, wi);
-          wr2[j] = make_float2(wr, wr);
-          wi2[j] = make_float2(wi, wi);
-          wm2[j] = make_float2(-wi, -wi);
         }
       }
-      // FP32 partial sums of up to kPipeFold channels, then a Kahan fold.
-      // Paired form: acc holds (vr zr, vi zr) and acc_b (vr zi, vi zi); else acc = (re, im).
+      // FP32 partial sums of up to FOLD channels, then a Kahan fold.
+      // Paired form: acc holds (vr zr, vi zi) and acc_b (vi zr, vr zi); else acc = (re, im).
       float2 acc[DPW][4], acc_b[DPW][4];
 #pragma unroll
       for (int j = 0; j < DPW; ++j)
@@ -300,21 +314,18 @@ __global__ void __launch_bounds__(NC * 32, 1) rotate_average_mixed_pipe(const Pi
           break;
         }
         if (active) {
-          float2 z[DPW], zr2[DPW], zi2[DPW];
+          float2 z[DPW];
           const unsigned char* src = stage_mem + st * pipe_stage_bytes<TPB>() + ts * CH * kPipeItemBytes + lane * 32;
           if (n == CH) {
 #pragma unroll
             for (int sub = 0; sub < CH; sub += kPipeReseed) {
 #pragma unroll
-              for (int j = 0; j < DPW; ++j) {
+              for (int j = 0; j < DPW; ++j)
                 twiddle_turns(pa[j] + static_cast<uint32_t>(cb + sub) * pb[j], tab, z[j].x, z[j].y);
-                zr2[j] = make_float2(z[j].x, z[j].x);
-                zi2[j] = make_float2(z[j].y, z[j].y);
-              }
 #pragma unroll
               for (int k = 0; k < kPipeReseed; ++k) {
                 if constexpr (PAIRED)
-                  mac_channel_paired<DPW>(src + (sub + k) * kPipeItemBytes, h, acc, acc_b, zr2, zi2, wr2, wi2, wm2);
+                  mac_channel_paired<DPW>(src + (sub + k) * kPipeItemBytes, h, acc, acc_b, z, w);
                 else
                   mac_channel<DPW>(src + (sub + k) * kPipeItemBytes, h, acc, z, w);
               }
@@ -323,25 +334,22 @@ __global__ void __launch_bounds__(NC * 32, 1) rotate_average_mixed_pipe(const Pi
             for (int k = 0; k < n; ++k) {
               if (k % kPipeReseed == 0) {
 #pragma unroll
-                for (int j = 0; j < DPW; ++j) {
+                for (int j = 0; j < DPW; ++j)
                   twiddle_turns(pa[j] + static_cast<uint32_t>(cb + k) * pb[j], tab, z[j].x, z[j].y);
-                  zr2[j] = make_float2(z[j].x, z[j].x);
-                  zi2[j] = make_float2(z[j].y, z[j].y);
-                }
               }
               if constexpr (PAIRED)
-                mac_channel_paired<DPW>(src + k * kPipeItemBytes, h, acc, acc_b, zr2, zi2, wr2, wi2, wm2);
+                mac_channel_paired<DPW>(src + k * kPipeItemBytes, h, acc, acc_b, z, w);
               else
                 mac_channel<DPW>(src + k * kPipeItemBytes, h, acc, z, w);
             }
           }
-          if ((cb + CH) % kPipeFold == 0 || cb + CH >= C) {
+          if ((cb + CH) % PipeShape<TPB>::FOLD == 0 || cb + CH >= C) {
 #pragma unroll
             for (int j = 0; j < DPW; ++j)
 #pragma unroll
               for (int q = 0; q < 4; ++q) {
-                const float re = PAIRED ? acc[j][q].x - acc_b[j][q].y : acc[j][q].x;
-                const float im = PAIRED ? acc_b[j][q].x + acc[j][q].y : acc[j][q].y;
+                const float re = PAIRED ? acc[j][q].x - acc[j][q].y : acc[j][q].x;
+                const float im = PAIRED ? acc_b[j][q].x + acc_b[j][q].y : acc[j][q].y;
                 float y = re - cr[j][q];
                 float tt = sr[j][q] + y;
                 cr[j][q] = (tt - sr[j][q]) - y;

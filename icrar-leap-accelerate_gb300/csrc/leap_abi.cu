@@ -704,14 +704,15 @@ int refant_stage(leap_ctx* ctx, const std::vector<WorkItem>& items, const double
   int blocks = 0;
   // Each block sums 4*DPW directions of 32 reference baselines over a slab of
   // (timestep, channel) pairs.  Slabs are sized to one budget across items (about
-  // 16 blocks per SM in total), so that chunks of 1 x 48 and 64 x 384 samples give
-  // blocks of similar length instead of the same number of blocks each.
+  // 32 blocks per SM in total, several waves of the 5 resident blocks), so that chunks
+  // of 1 x 48 and 64 x 384 samples give blocks of similar length instead of the same
+  // number of blocks each, and the last wave is a small part of the pass.
   int64_t work_total = 0;
   for (const auto& w : items) {
     const Integration& in = ctx->integ.at(w.slot);
     work_total += (in.rows / nbl) * in.channels * rtiles * ((w.ndir + 7) / 8);
   }
-  const int64_t slab_budget = std::max<int64_t>(64, (work_total + 16 * ctx->sms - 1) / (16 * ctx->sms));
+  const int64_t slab_budget = std::max<int64_t>(64, (work_total + 32 * ctx->sms - 1) / (32 * ctx->sms));
   for (const auto& w : items) {
     Integration& in = ctx->integ.at(w.slot);
     const int T = static_cast<int>(in.rows / nbl);
