@@ -352,34 +352,54 @@ __global__ void __launch_bounds__(128) refant_average_fp64(RotateArgs a, const i
 //    plus a correction (absolute error ~5e-10) and renormalised with TwoSum so
 //    that the low part is below one FP32 ulp;
 //  * product v*z_hi is exact (TwoProd), v*z_lo is rounded (error <= 4e-10 |v|),
-//    and the running sum is a TwoSum pair, so the sum carries no FP32 rounding.
+//    and the running sum is a TwoSum pair, so the sum carries no FP32 rounding;
+//  * a warp's two directions run as the two halves of paired FP32 instructions
+//    (FFMA2, FADD2, FMUL2), which round each half exactly as the scalar
+//    operation; a - b is formed as fma(b, -1, a) (one rounding, as the
+//    subtraction) and a negated product as fma(a, -b, c) = fma(-a, b, c), so
+//    each half carries the scalar sequence's sums bit for bit, at about half
+//    the instructions.
 // ---------------------------------------------------------------------------
-struct DfAcc {
-  float s, c;  // value = s + c
+struct DfAcc2 {
+  float2 s, c;  // value = s + c, one direction per half
 };
 
-__device__ __forceinline__ void df_add_product(DfAcc& acc, float x, float yh, float yl) {
-  const float p = x * yh;
-  const float e = fmaf(x, yh, -p);       // x*yh = p + e exactly
-  const float sum = acc.s + p;           // TwoSum(acc.s, p)
-  const float bb = sum - acc.s;
-  const float err = (acc.s - (sum - bb)) + (p - bb);
-  acc.s = sum;
-  acc.c += err + fmaf(x, yl, e);
+__device__ __forceinline__ float2 df_sub2(float2 a, float2 b) { return __ffma2_rn(b, make_float2(-1.f, -1.f), a); }
+
+__device__ __forceinline__ void two_sum2(float2 a, float2 b, float2& s, float2& e) {
+  s = __fadd2_rn(a, b);
+  const float2 bb = df_sub2(s, a);
+  e = __fadd2_rn(df_sub2(a, df_sub2(s, bb)), df_sub2(b, bb));
 }
 
-__device__ __forceinline__ void df_twiddle(uint64_t turns, const float4* __restrict__ tab, float& zrh, float& zrl,
-                                           float& zih, float& zil) {
-  const float4 t = tab[turns >> 54];                                   // (cos_hi, cos_lo, sin_hi, sin_lo)
-  const uint32_t r24 = static_cast<uint32_t>(turns >> 30) & 0xFFFFFFu;
-  const float d = __uint2float_rn(r24) * 3.657295198167899e-10f;     // 2*pi / 2^34
-  const float d2 = d * d;
-  const float c2 = 0.5f * d2;                                          // 1 - cos(d) (d^4/24 < 6e-11 dropped)
-  const float sd = d * fmaf(d2, -0.16666667f, 1.0f);                   // sin(d)
-  const float lr = fmaf(-t.x, c2, fmaf(-t.z, sd, t.y));  // z_re - entry_hi
-  const float li = fmaf(-t.z, c2, fmaf(t.x, sd, t.w));   // z_im - entry_hi
-  two_sum(t.x, lr, zrh, zrl);
-  two_sum(t.z, li, zih, zil);
+// acc += x * (yh + yl) per half (nx = -x): x*yh = p + e exactly (TwoProd), TwoSum of
+// acc.s and p, and err + (x*yl + e) into acc.c.
+__device__ __forceinline__ void df_add_product2(DfAcc2& acc, float2 x, float2 nx, float2 yh, float2 yl) {
+  const float2 p = __fmul2_rn(x, yh);
+  const float2 en = __ffma2_rn(nx, yh, p);  // p - x*yh = -e, exact
+  float2 sum, err;
+  two_sum2(acc.s, p, sum, err);
+  acc.s = sum;
+  acc.c = __fadd2_rn(acc.c, df_sub2(err, __ffma2_rn(nx, yl, en)));  // -(x*yl + e) from nx, en
+}
+
+// Twiddles of two phases (one per half) as (hi, lo) pairs.
+__device__ __forceinline__ void df_twiddle2(uint64_t t0, uint64_t t1, const float4* __restrict__ tab, float2& zrh,
+                                            float2& zrl, float2& zih, float2& zil) {
+  const float4 a = tab[t0 >> 54], b = tab[t1 >> 54];  // (cos_hi, cos_lo, sin_hi, sin_lo)
+  const float2 tx = make_float2(a.x, b.x), ty = make_float2(a.y, b.y);
+  const float2 tz = make_float2(a.z, b.z), tw = make_float2(a.w, b.w);
+  const float2 r24 = make_float2(__uint2float_rn(static_cast<uint32_t>(t0 >> 30) & 0xFFFFFFu),
+                                 __uint2float_rn(static_cast<uint32_t>(t1 >> 30) & 0xFFFFFFu));
+  const float2 d = __fmul2_rn(r24, make_float2(3.657295198167899e-10f, 3.657295198167899e-10f));  // 2*pi / 2^34
+  const float2 d2 = __fmul2_rn(d, d);
+  const float2 nc2 = __fmul2_rn(make_float2(-0.5f, -0.5f), d2);  // cos(d) - 1 (d^4/24 < 6e-11 dropped)
+  const float2 sd = __fmul2_rn(d, __ffma2_rn(d2, make_float2(-0.16666667f, -0.16666667f), make_float2(1.f, 1.f)));
+  const float2 nsd = __fmul2_rn(sd, make_float2(-1.f, -1.f));      // -sin(d)
+  const float2 lr = __ffma2_rn(tx, nc2, __ffma2_rn(tz, nsd, ty));  // z_re - entry_hi
+  const float2 li = __ffma2_rn(tz, nc2, __ffma2_rn(tx, sd, tw));   // z_im - entry_hi
+  two_sum2(tx, lr, zrh, zrl);
+  two_sum2(tz, li, zih, zil);
 }
 
 // Fractional part of x (turns) as a 2^-64 fixed-point value.
@@ -435,10 +455,10 @@ struct RefantItem {
 constexpr int kRefantPrefetch = 16;  // channel loads in flight per lane in the compensated pass
 
 template <int DPW>
-__global__ void __launch_bounds__(128) refant_average_df_items(const RefantItem* __restrict__ items, int nitems,
-                                                              int nbl, double f0, double df,
-                                                              const int32_t* __restrict__ I1, int nI1,
-                                                              const float4* __restrict__ df_tab) {
+__global__ void __launch_bounds__(128, 5) refant_average_df_items(const RefantItem* __restrict__ items, int nitems,
+                                                                 int nbl, double f0, double df,
+                                                                 const int32_t* __restrict__ I1, int nI1,
+                                                                 const float4* __restrict__ df_tab) {
   __shared__ float4 tab[kTwiddleSize];
   for (int i = threadIdx.x; i < kTwiddleSize; i += blockDim.x) tab[i] = __ldg(df_tab + i);
   __syncthreads();
@@ -461,9 +481,8 @@ __global__ void __launch_bounds__(128) refant_average_df_items(const RefantItem*
   int b = __ldg(I1 + k);
   if (b < 0) b += nbl;  // VectorRangeSelect wrap-around (LA/math/cpu/vector.h:97-104)
   const double kA = f0 / kSpeedOfLight, kB = df / kSpeedOfLight;
-  DfAcc re[DPW], im[DPW];
-#pragma unroll
-  for (int j = 0; j < DPW; ++j) re[j] = im[j] = DfAcc{0.f, 0.f};
+  static_assert(DPW == 2, "the two directions of a warp are the halves of paired instructions");
+  DfAcc2 re{make_float2(0.f, 0.f), make_float2(0.f, 0.f)}, im = re;
   for (int t = t_lo; t < t_hi; ++t) {
     const int64_t r = static_cast<int64_t>(t) * nbl + b;
     const double uu = __ldg(it.uvw + 3 * r), vv = __ldg(it.uvw + 3 * r + 1), ww = __ldg(it.uvw + 3 * r + 2);
@@ -490,26 +509,24 @@ __global__ void __launch_bounds__(128) refant_average_df_items(const RefantItem*
       for (int i = 0; i < kRefantPrefetch; ++i) {
         if (c0 + i >= c_hi) break;
         const float2 v = vb[i];
-#pragma unroll
-        for (int j = 0; j < DPW; ++j) {
-          float zrh, zrl, zih, zil;
-          df_twiddle(pa[j] + static_cast<uint64_t>(c0 + i) * pb[j], tab, zrh, zrl, zih, zil);
-          df_add_product(re[j], v.x, zrh, zrl);
-          df_add_product(re[j], -v.y, zih, zil);
-          df_add_product(im[j], v.x, zih, zil);
-          df_add_product(im[j], v.y, zrh, zrl);
-        }
+        const float2 vx = make_float2(v.x, v.x), nvx = make_float2(-v.x, -v.x);
+        const float2 vy = make_float2(v.y, v.y), nvy = make_float2(-v.y, -v.y);
+        float2 zrh, zrl, zih, zil;
+        df_twiddle2(pa[0] + static_cast<uint64_t>(c0 + i) * pb[0], pa[1] + static_cast<uint64_t>(c0 + i) * pb[1], tab,
+                    zrh, zrl, zih, zil);
+        df_add_product2(re, vx, nvx, zrh, zrl);  // re += vr zr - vi zi
+        df_add_product2(re, nvy, vy, zih, zil);
+        df_add_product2(im, vx, nvx, zih, zil);  // im += vr zi + vi zr
+        df_add_product2(im, vy, nvy, zrh, zrl);
       }
     }
   }
   double2* out = it.out + static_cast<int64_t>(slab) * it.ndir * nI1;
-#pragma unroll
-  for (int j = 0; j < DPW; ++j) {
-    const int jd = j0 + j;
-    if (jd < it.ndir)
-      out[static_cast<int64_t>(jd) * nI1 + k] = make_double2(static_cast<double>(re[j].s) + static_cast<double>(re[j].c),
-                                                             static_cast<double>(im[j].s) + static_cast<double>(im[j].c));
-  }
+  out[static_cast<int64_t>(j0) * nI1 + k] = make_double2(static_cast<double>(re.s.x) + static_cast<double>(re.c.x),
+                                                         static_cast<double>(im.s.x) + static_cast<double>(im.c.x));
+  if (j0 + 1 < it.ndir)
+    out[static_cast<int64_t>(j0 + 1) * nI1 + k] = make_double2(static_cast<double>(re.s.y) + static_cast<double>(re.c.y),
+                                                               static_cast<double>(im.s.y) + static_cast<double>(im.c.y));
 }
 
 // Sum of slab partials in slab order: avg[i] = sum_s partial[s][i].
