@@ -29,11 +29,12 @@
 // every kPipeReseed channels and advanced by one FP32 complex multiply per
 // channel in between (drift over 16 steps ~1e-6; it reaches the cal phases
 // only through baselines that the reference-antenna pass does not cover, with
-// weight ~1/S).  Sums: FP32 over 32 (1 tile) or 64 (4 tiles) channels, folded
-// into Kahan pairs.  Reseeding every 16 rather than 8 channels and folding
-// every 32 rather than 16 cut the 128-antenna call from 3.00 to 2.85 ms and
-// moved its cal-phase difference from the FP64 form from 5.5e-7 to 2.1e-6 rad
-// (bar: 1e-5).
+// weight ~1/S).  Sums: FP32 over 64 channels, folded into Kahan pairs.
+// Reseeding every 16 rather than 8 channels and folding every 32 rather than 16
+// cut the 128-antenna call from 3.00 to 2.85 ms and moved its cal-phase
+// difference from the FP64 form from 5.5e-7 to 2.1e-6 rad (bar: 1e-5); the
+// paired multiply-accumulate below and folds every 64 then took it to 2.49 ms
+// and 1.6e-6 rad.
 //
 // Shared-memory reads: lane i reads its 32 bytes as two 16-byte halves; lanes
 // with bit 2 set read the upper half first so that each quarter-warp covers
@@ -69,18 +70,19 @@ struct PipeParams {
 
 constexpr int kPipeMaxItems = 128;
 constexpr int kPipeReseed = 16;         // channels between table-accurate twiddles
+// Channels summed in FP32 before a Kahan fold.  At 32 the fold was ~6% of the FMA-pipe work;
+// FP32 partial sums over 64 channels (~2e-8 of the sum of |terms|) stay far below the phasor
+// drift between reseeds (~1e-6).  Measured: 32-chunk batched workload 11.47 -> 11.10 ms per
+// call (cal-phase difference from the FP64 form over 256 directions: median 1.1e-7 -> 1.2e-7
+// rad, maximum 4.7e-6 -> 4.2e-6); 128-antenna 1-tile call 2.58 -> 2.49 ms.
+constexpr int kPipeFold = 64;
 constexpr int kPipeItemBytes = 32 * 4 * 8;  // one channel of one tile: 32 baselines x 4 pols x complex<float>
 
 // Channels per chunk and ring depth: 1 tile x 16 channels = 16 KB stages, 4 deep; 4 tiles x
-// 16 channels = 64 KB stages, 3 deep (192 KB of the 227 KB of shared memory).  FOLD: channels
-// summed in FP32 before a Kahan fold.  The 4-tile kernel folds every 64 channels: its fold is
-// ~6% of its FMA-pipe work at 32, and the FP32 partial sums over 64 channels (~2e-8 of the
-// sum of |terms|) stay far below the phasor drift between reseeds (~1e-6).  Measured on the
-// 32-chunk batched workload: 11.47 -> 11.10 ms per call; cal-phase difference from the FP64
-// form over 256 directions: median 1.1e-7 -> 1.2e-7 rad, maximum 4.7e-6 -> 4.2e-6 rad.
+// 16 channels = 64 KB stages, 3 deep (192 KB of the 227 KB of shared memory).
 template <int TPB> struct PipeShape;
-template <> struct PipeShape<1> { static constexpr int CH = 16, STAGES = 4, FOLD = 32; };
-template <> struct PipeShape<4> { static constexpr int CH = 16, STAGES = 3, FOLD = 64; };
+template <> struct PipeShape<1> { static constexpr int CH = 16, STAGES = 4; };
+template <> struct PipeShape<4> { static constexpr int CH = 16, STAGES = 3; };
 
 template <int TPB>
 __host__ __device__ constexpr int pipe_stage_bytes() { return TPB * PipeShape<TPB>::CH * kPipeItemBytes; }
@@ -144,37 +146,15 @@ __device__ __forceinline__ void issue_chunk(const ChunkCursor& k, const PipePara
     tma_load_2d(dst + ts * CH * kPipeItemBytes, &it.map, (k.t * p.nbl + (tg * TPB + ts) * 32) * 8, k.cb, &full[st]);
 }
 
-// One channel of the complex multiply-accumulate for DPW directions and 4 pols on scalar
-// FMAs; each accumulator and phasor is a (re, im) float2.  The 4-tile kernel uses the
-// paired form below (FFMA2).
-template <int DPW>
-__device__ __forceinline__ void mac_channel(const unsigned char* src, int h, float2 (&acc)[DPW][4], float2 (&z)[DPW],
-                                            const float2 (&w)[DPW]) {
-  const float4 x0 = *reinterpret_cast<const float4*>(src + 16 * h);
-  const float4 x1 = *reinterpret_cast<const float4*>(src + 16 * (1 - h));
-  const float vr[4] = {x0.x, x0.z, x1.x, x1.z};
-  const float vi[4] = {x0.y, x0.w, x1.y, x1.w};
-#pragma unroll
-  for (int j = 0; j < DPW; ++j) {
-#pragma unroll
-    for (int q = 0; q < 4; ++q) {
-      acc[j][q].x = fmaf(vr[q], z[j].x, fmaf(-vi[q], z[j].y, acc[j][q].x));
-      acc[j][q].y = fmaf(vr[q], z[j].y, fmaf(vi[q], z[j].x, acc[j][q].y));
-    }
-    const float nr = fmaf(z[j].x, w[j].x, -z[j].y * w[j].y);
-    z[j].y = fmaf(z[j].x, w[j].y, z[j].y * w[j].x);
-    z[j].x = nr;
-  }
-}
-
-// Paired form: each visibility enters as its natural (re, im) register pair v from the
+// One channel of the complex multiply-accumulate for DPW directions and 4 pols, on paired
+// FP32 FMAs (FFMA2): each visibility enters as its natural (re, im) register pair v from the
 // shared-memory load and once swapped, vs = (im, re), shared by the DPW directions; the
-// phasor stays a natural (zr, zi) pair advanced by the scalar step of mac_channel.  Then
+// phasor stays a natural (zr, zi) pair advanced by 4 scalar FMAs.  Then
 //     acc_a += v * z = (vr zr, vi zi),   acc_b += vs * z = (vi zr, vr zi),
 // and the fold takes re = acc_a.x - acc_a.y, im = acc_b.x + acc_b.y: 16 paired FMAs (32
 // FMA-pipe cycles) and 4 scalar ones per direction and channel, no per-direction moves.
 template <int DPW>
-__device__ __forceinline__ void mac_channel_paired(const unsigned char* src, int h, float2 (&acc_a)[DPW][4],
+__device__ __forceinline__ void mac_channel(const unsigned char* src, int h, float2 (&acc_a)[DPW][4],
                                                    float2 (&acc_b)[DPW][4], float2 (&z)[DPW],
                                                    const float2 (&w)[DPW]) {
   const float4 x0 = *reinterpret_cast<const float4*>(src + 16 * h);
@@ -201,7 +181,6 @@ __global__ void __launch_bounds__(NC * 32, 1) rotate_average_mixed_pipe(const Pi
   constexpr int CH = PipeShape<TPB>::CH;
   constexpr int NS = PipeShape<TPB>::STAGES;
   constexpr int WPT = NC / TPB;  // warps (direction groups of DPW) per tile
-  constexpr bool PAIRED = TPB > 1;  // FFMA2 multiply-accumulate (mac_channel_paired)
   static_assert(NC % TPB == 0, "warps must divide among tiles");
   extern __shared__ __align__(128) unsigned char smem[];
   unsigned char* stage_mem = smem;
@@ -298,8 +277,8 @@ __global__ void __launch_bounds__(NC * 32, 1) rotate_average_mixed_pipe(const Pi
           w[j] = make_float2(wr, wi);
         }
       }
-      // FP32 partial sums of up to FOLD channels, then a Kahan fold.
-      // Paired form: acc holds (vr zr, vi zi) and acc_b (vi zr, vr zi); else acc = (re, im).
+      // FP32 partial sums of up to kPipeFold channels, then a Kahan fold.
+      // acc holds (vr zr, vi zi) and acc_b (vi zr, vr zi) per direction and pol.
       float2 acc[DPW][4], acc_b[DPW][4];
 #pragma unroll
       for (int j = 0; j < DPW; ++j)
@@ -324,10 +303,7 @@ __global__ void __launch_bounds__(NC * 32, 1) rotate_average_mixed_pipe(const Pi
                 twiddle_turns(pa[j] + static_cast<uint32_t>(cb + sub) * pb[j], tab, z[j].x, z[j].y);
 #pragma unroll
               for (int k = 0; k < kPipeReseed; ++k) {
-                if constexpr (PAIRED)
-                  mac_channel_paired<DPW>(src + (sub + k) * kPipeItemBytes, h, acc, acc_b, z, w);
-                else
-                  mac_channel<DPW>(src + (sub + k) * kPipeItemBytes, h, acc, z, w);
+                mac_channel<DPW>(src + (sub + k) * kPipeItemBytes, h, acc, acc_b, z, w);
               }
             }
           } else {
@@ -337,19 +313,16 @@ __global__ void __launch_bounds__(NC * 32, 1) rotate_average_mixed_pipe(const Pi
                 for (int j = 0; j < DPW; ++j)
                   twiddle_turns(pa[j] + static_cast<uint32_t>(cb + k) * pb[j], tab, z[j].x, z[j].y);
               }
-              if constexpr (PAIRED)
-                mac_channel_paired<DPW>(src + k * kPipeItemBytes, h, acc, acc_b, z, w);
-              else
-                mac_channel<DPW>(src + k * kPipeItemBytes, h, acc, z, w);
+              mac_channel<DPW>(src + k * kPipeItemBytes, h, acc, acc_b, z, w);
             }
           }
-          if ((cb + CH) % PipeShape<TPB>::FOLD == 0 || cb + CH >= C) {
+          if ((cb + CH) % kPipeFold == 0 || cb + CH >= C) {
 #pragma unroll
             for (int j = 0; j < DPW; ++j)
 #pragma unroll
               for (int q = 0; q < 4; ++q) {
-                const float re = PAIRED ? acc[j][q].x - acc[j][q].y : acc[j][q].x;
-                const float im = PAIRED ? acc_b[j][q].x + acc_b[j][q].y : acc[j][q].y;
+                const float re = acc[j][q].x - acc[j][q].y;
+                const float im = acc_b[j][q].x + acc_b[j][q].y;
                 float y = re - cr[j][q];
                 float tt = sr[j][q] + y;
                 cr[j][q] = (tt - sr[j][q]) - y;
