@@ -441,6 +441,20 @@ int gridded_stage(leap_ctx* ctx, const std::vector<WorkItem>& items, const doubl
 }
 
 // Rotate + average of every item into ctx->avg ([D][P][nbl]).
+// The gridded kernel runs when it is forced on, or by default when every item has enough
+// directions to amortise the grid product (the tensor-core rotation option, when forced, wins);
+// it needs the 4-pol complex<float> mixed form with TMA maps on every item.
+bool uses_gridded(const leap_ctx* ctx, const std::vector<WorkItem>& items, int32_t D, int32_t precision, int P) {
+  if (precision != LEAP_PRECISION_MIXED || P != 4 || ctx->gridded == 0) return false;
+  int min_ndir = D;
+  for (const auto& w : items) {
+    const Integration& in = ctx->integ.at(w.slot);
+    if (in.vis_type != LEAP_VIS_C64 || !in.has_map) return false;
+    min_ndir = std::min(min_ndir, w.ndir);
+  }
+  return ctx->gridded == 1 || (ctx->mma_rotate != 2 && min_ndir >= kGridAutoDirs);
+}
+
 int rotate_stage(leap_ctx* ctx, const std::vector<WorkItem>& items, const double* d_dd, int32_t D, int32_t precision,
                  int P, cudaStream_t s, int& kernels) {
   Metadata& md = ctx->md;
@@ -468,10 +482,7 @@ int rotate_stage(leap_ctx* ctx, const std::vector<WorkItem>& items, const double
               "upload wavelengths");
   }
 
-  // Gridded kernel: forced on, or by default when every item has enough directions to
-  // amortise the grid product (the tensor-core rotation option, when forced, wins).
-  if (all_pipe && (ctx->gridded == 1 || (ctx->gridded == 2 && ctx->mma_rotate != 2 && min_ndir >= kGridAutoDirs)))
-    return gridded_stage(ctx, items, d_dd, D, s, kernels);
+  if (uses_gridded(ctx, items, D, precision, P)) return gridded_stage(ctx, items, d_dd, D, s, kernels);
   if (all_pipe) {
     // Kernel: the tensor-core one (16 directions per unit) when the autotuner chose it or the
     // option forces it (items of at least 12 directions); else the CUDA-core one with 4 tiles
@@ -951,10 +962,20 @@ int calibrate_items(leap_ctx* ctx, const std::vector<WorkItem>& items, const dou
     LEAP_CUDA(cudaEventRecord(ctx->fork, s), "fork");
     LEAP_CUDA(cudaStreamWaitEvent(ctx->aux, ctx->fork, 0), "fork");
   }
-  int rc = rotate_stage(ctx, items, d_dd, D, precision, P, s, kernels);
+  // The reference-antenna pass cannot share an SM with either bulk kernel (registers or shared
+  // memory).  Beside the gridded kernel it goes first, so that it overlaps the small kernels
+  // that set up the grid windows; beside the pipelined kernel it goes after it, so that the
+  // persistent blocks, whose unit schedule assumes they start together, take the SMs first.
+  const bool refant_first = refant && uses_gridded(ctx, items, D, precision, P);
+  int rc = LEAP_OK;
+  if (refant_first) {
+    rc = refant_stage(ctx, items, d_dd, D, kernels);
+    if (rc != LEAP_OK) return rc;
+    LEAP_CUDA(cudaEventRecord(ctx->join, ctx->aux), "join");
+  }
+  rc = rotate_stage(ctx, items, d_dd, D, precision, P, s, kernels);
   if (rc != LEAP_OK) return rc;
-  if (refant) {
-    // Launched after the bulk kernel so that the persistent blocks take the SMs first.
+  if (refant && !refant_first) {
     rc = refant_stage(ctx, items, d_dd, D, kernels);
     if (rc != LEAP_OK) return rc;
     LEAP_CUDA(cudaEventRecord(ctx->join, ctx->aux), "join");
