@@ -32,10 +32,15 @@ struct SolveArgs {
   const double2* avg_i1;    // optional [ndir][A1rows-1]: FP64 pol-0 sums of the I1 baselines
 };
 
-// K3 + K4: phi1 and cal1 = Ad1 * phi1, one block per direction.  With FP64
-// sums of the I1 baselines (mixed form) those replace pol 0 of avgData first.
-static __global__ void solve_cal1(SolveArgs a) {
-  extern __shared__ double sphi[];
+// K3 + K4: phi1 and cal1 = Ad1 * phi1.  Grid (directions, ceil(S / kCal1Cols)): each block
+// forms its direction's phi1 and kCal1Cols outputs of cal1, each output as 4 k-quarters of
+// the dot product combined in a fixed order, so the FP64 work spreads over more SMs than
+// one block per direction.  With FP64 sums of the I1 baselines (mixed form) those replace
+// pol 0 of avgData first (written by the direction's first block; the others read avg_i1).
+constexpr int kCal1Cols = 64;
+static __global__ void __launch_bounds__(256) solve_cal1(SolveArgs a) {
+  extern __shared__ double sphi[];  // [A1rows] phi1, then [4][kCal1Cols] partial sums
+  double* part = sphi + a.A1rows;
   const int d = blockIdx.x;
   double2* avg0 = const_cast<double2*>(a.avg) + static_cast<int64_t>(d) * a.pols * a.nbl;  // pol 0 column
   for (int k = threadIdx.x; k < a.A1rows; k += blockDim.x) {
@@ -46,7 +51,7 @@ static __global__ void solve_cal1(SolveArgs a) {
       double2 z;
       if (a.avg_i1) {
         z = a.avg_i1[static_cast<int64_t>(d) * (a.A1rows - 1) + k];
-        avg0[idx] = z;  // duplicate I1 entries carry the same value
+        if (blockIdx.y == 0) avg0[idx] = z;  // duplicate I1 entries carry the same value
       } else {
         z = avg0[idx];
       }
@@ -55,11 +60,17 @@ static __global__ void solve_cal1(SolveArgs a) {
     sphi[k] = v;
   }
   __syncthreads();
-  for (int s = threadIdx.x; s < a.S; s += blockDim.x) {
-    double acc = 0.0;
-    for (int k = 0; k < a.A1rows; ++k) acc += a.Ad1[s + static_cast<int64_t>(a.S) * k] * sphi[k];
-    a.cal1[static_cast<int64_t>(d) * a.S + s] = acc;
-  }
+  const int col = threadIdx.x % kCal1Cols, qk = threadIdx.x / kCal1Cols;
+  const int s = blockIdx.y * kCal1Cols + col;
+  const int kq = (a.A1rows + 3) / 4, k0 = qk * kq, k1 = min(a.A1rows, k0 + kq);
+  double acc = 0.0;
+  if (s < a.S)
+    for (int k = k0; k < k1; ++k) acc += a.Ad1[s + static_cast<int64_t>(a.S) * k] * sphi[k];
+  part[qk * kCal1Cols + col] = acc;
+  __syncthreads();
+  if (qk == 0 && s < a.S)
+    a.cal1[static_cast<int64_t>(d) * a.S + s] =
+        ((part[col] + part[kCal1Cols + col]) + part[2 * kCal1Cols + col]) + part[3 * kCal1Cols + col];
 }
 
 // K5 + K6-prep: dphi[d][n] for n < Kpad (zero past |I|).  FP64 form.
@@ -150,14 +161,27 @@ static __global__ void __launch_bounds__(256) gemm_ad_partial(const T* __restric
 }
 
 // cal[d][s] = sum_kc partial[kc][d][s] (fixed order) + cal1[d][s].
-static __global__ void gemm_ad_finish(const double* __restrict__ partial, int nk, int ndir, int S,
-                               const double* __restrict__ cal1, double* __restrict__ cal) {
-  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+// A block covers kFinishCols consecutive outputs; its 8 warps sum interleaved k-chunks and
+// the partial sums are combined in warp order (deterministic), so each dependent chain of
+// FP64 adds is nk/8 long and the grid spans the SMs even for a few directions.
+constexpr int kFinishCols = 32;
+static __global__ void __launch_bounds__(256) gemm_ad_finish(const double* __restrict__ partial, int nk, int ndir,
+                                                             int S, const double* __restrict__ cal1,
+                                                             double* __restrict__ cal) {
+  __shared__ double part[8][kFinishCols];
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
   const int n = ndir * S;
-  if (i >= n) return;
+  const int i = blockIdx.x * kFinishCols + lane;
   double acc = 0.0;
-  for (int kc = 0; kc < nk; ++kc) acc += partial[static_cast<int64_t>(kc) * n + i];
-  cal[i] = acc + cal1[i];
+  if (i < n)
+    for (int kc = w; kc < nk; kc += 8) acc += partial[static_cast<int64_t>(kc) * n + i];
+  part[w][lane] = acc;
+  __syncthreads();
+  if (w == 0 && i < n) {
+    double sum = part[0][lane];
+    for (int j = 1; j < 8; ++j) sum += part[j][lane];
+    cal[i] = sum + cal1[i];
+  }
 }
 
 }  // namespace leapgb

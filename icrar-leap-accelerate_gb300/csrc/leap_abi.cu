@@ -857,8 +857,8 @@ int tc_contraction(leap_ctx* ctx, int32_t D, double* d_cal, cudaStream_t s, int&
     default: rc = launch_tc_gemm<256>(ctx, D, ntiles, nkc, kb_per_cta, s, 8); break;
   }
   if (rc != LEAP_OK) return rc;
-  gemm_ad_finish<<<(D * md.S + 255) / 256, 256, 0, s>>>(ctx->gemm_partial.as<double>(), nkc, D, md.S,
-                                                        ctx->cal1.as<double>(), d_cal);
+  gemm_ad_finish<<<(D * md.S + kFinishCols - 1) / kFinishCols, 256, 0, s>>>(ctx->gemm_partial.as<double>(), nkc, D,
+                                                                          md.S, ctx->cal1.as<double>(), d_cal);
   kernels += 5;  // solve_dint, pack, gemm, finish (+ solve_cal1 counted by the caller)
   return LEAP_OK;
 }
@@ -886,7 +886,8 @@ int solve_stage(leap_ctx* ctx, int32_t D, int32_t precision, int P, bool refant,
   sa.cal1 = ctx->cal1.as<double>();
   sa.dphi = ctx->dphi.ptr;
   sa.avg_i1 = refant ? ctx->avg_i1.as<double2>() : nullptr;
-  solve_cal1<<<D, 256, sizeof(double) * md.A1rows, s>>>(sa);
+  solve_cal1<<<dim3(D, (md.S + kCal1Cols - 1) / kCal1Cols), 4 * kCal1Cols, sizeof(double) * (md.A1rows + 4 * kCal1Cols),
+               s>>>(sa);
   ++kernels;
   const dim3 gd((md.Kpad + 255) / 256, D);
   const dim3 gg((md.S + 63) / 64, (D + 15) / 16, nk);
@@ -902,8 +903,8 @@ int solve_stage(leap_ctx* ctx, int32_t D, int32_t precision, int P, bool refant,
     solve_dint_mixed<<<gd, 256, 0, s>>>(sa);
     return tc_contraction(ctx, D, d_cal, s, kernels);
   }
-  gemm_ad_finish<<<(D * md.S + 255) / 256, 256, 0, s>>>(ctx->gemm_partial.as<double>(), nk, D, md.S,
-                                                        ctx->cal1.as<double>(), d_cal);
+  gemm_ad_finish<<<(D * md.S + kFinishCols - 1) / kFinishCols, 256, 0, s>>>(ctx->gemm_partial.as<double>(), nk, D,
+                                                                          md.S, ctx->cal1.as<double>(), d_cal);
   kernels += 3;
   return LEAP_OK;
 }
