@@ -89,7 +89,7 @@ def test_phase_matrix_structure_and_ref_row():
     fg = (a1 == a2).astype(np.uint8)
     fg[3] = 1  # one flagged cross baseline
     # refAnt 0 would be "flagged": the reference checks fg[refAnt], i.e. the flag
-    # of BASELINE refAnt (here the flagged autocorrelation (0, 0)).
+    # of the baseline whose index is refAnt (here the flagged autocorrelation (0, 0)).
     for mod in (oracle, lg):
         with pytest.raises(mod.InvalidArgument):
             mod.phase_matrix(a1, a2, fg, 0)
