@@ -151,12 +151,11 @@ __device__ __forceinline__ void issue_chunk(const ChunkCursor& k, const PipePara
 // shared-memory load and once swapped, vs = (im, re), shared by the DPW directions; the
 // phasor stays a natural (zr, zi) pair advanced by 4 scalar FMAs.  Then
 //     acc_a += v * z = (vr zr, vi zi),   acc_b += vs * z = (vi zr, vr zi),
-// and the fold takes re = acc_a.x - acc_a.y, im = acc_b.x + acc_b.y: 16 paired FMAs (32
+// and the fold takes re = acc_a.x - acc_a.y, im = acc_b.x + acc_b.y: 8 paired FMAs (16
 // FMA-pipe cycles) and 4 scalar ones per direction and channel, no per-direction moves.
 template <int DPW>
 __device__ __forceinline__ void mac_channel(const unsigned char* src, int h, float2 (&acc_a)[DPW][4],
-                                                   float2 (&acc_b)[DPW][4], float2 (&z)[DPW],
-                                                   const float2 (&w)[DPW]) {
+                                            float2 (&acc_b)[DPW][4], float2 (&z)[DPW], const float2 (&w)[DPW]) {
   const float4 x0 = *reinterpret_cast<const float4*>(src + 16 * h);
   const float4 x1 = *reinterpret_cast<const float4*>(src + 16 * (1 - h));
   const float2 v[4] = {make_float2(x0.x, x0.y), make_float2(x0.z, x0.w), make_float2(x1.x, x1.y),

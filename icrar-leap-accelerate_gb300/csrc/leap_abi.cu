@@ -440,7 +440,6 @@ int gridded_stage(leap_ctx* ctx, const std::vector<WorkItem>& items, const doubl
   return LEAP_OK;
 }
 
-// Rotate + average of every item into ctx->avg ([D][P][nbl]).
 // The gridded kernel runs when it is forced on, or by default when every item has enough
 // directions to amortise the grid product (the tensor-core rotation option, when forced, wins);
 // it needs the 4-pol complex<float> mixed form with TMA maps on every item.
@@ -455,6 +454,7 @@ bool uses_gridded(const leap_ctx* ctx, const std::vector<WorkItem>& items, int32
   return ctx->gridded == 1 || (ctx->mma_rotate != 2 && min_ndir >= kGridAutoDirs);
 }
 
+// Rotate + average of every item into ctx->avg ([D][P][nbl]).
 int rotate_stage(leap_ctx* ctx, const std::vector<WorkItem>& items, const double* d_dd, int32_t D, int32_t precision,
                  int P, cudaStream_t s, int& kernels) {
   Metadata& md = ctx->md;
