@@ -4,28 +4,42 @@ Metric: vis-directions/s — one visibility sample (pol, row, channel) phase-
 rotated and averaged for one calibration direction, through the whole path
 (rotate + average, phase angles, both pseudoinverse contractions).
 
-Workload (default): the precision-form MWA-like array — 128 antennas (8256
-baselines with autocorrelations), 14 timesteps at 8 s, 384 channels of 40 kHz
-from 150 MHz, 4 pols, complex<float> visibilities, 64 directions; synthetic,
-seeded.  The 1.42 GB visibility cube is larger than L2 (129 MB), so no L2 flush
-is needed between steps.
+Headline workload (default): the batched uneven workload — 128 antennas (8256
+baselines with autocorrelations), 32 integration chunks with timesteps uniform
+in 1..64 and channels from {48, 96, 384} (seed 4), 4 pols, complex<float>
+(52.3 GB resident), 256 directions dealt round-robin to the chunks, one
+leap_calibrate_batched call per step (graph replay).  Synthetic, seeded, the
+visibilities generated on the device.  Inputs are larger than L2 (129 MB), so
+no L2 flush is needed between steps.
 
-  value      inputs resident in HBM, the mixed-precision form, CUDA events on
-             the launching stream around exactly --steps calls
-  e2e        the public C ABI with host buffers: per step the visibilities in
-             MeasurementSet order ([row][channel][pol], page-locked host memory) +
-             UVWs go up through leap_set_integration_ms (transposed on the device),
-             then leap_calibrate with host dd / cal buffers; the upload of the
-             pre-transposed Integration layout (leap_set_integration) is reported
-             beside it
-  plain_fp64 the all-FP64 form on the same workload
-  roofline   the rotate+average kernel against the measured HBM copy bandwidth
-  cpu_baseline  the oracle port (C, OpenMP over directions) on a bounded sample
+The JSON line:
+  value        inputs resident in HBM, mixed-precision form, the library's CUDA
+               events on its stream around each call (exactly --steps calls)
+  e2e          the same call through the C ABI from host buffers: every step
+               uploads each chunk from page-locked host memory
+               (leap_set_integration) and reads the cal phases back
+  roofline     the bulk rotate + average kernel: the bytes it must move (each
+               sample read once, UVWs, one avgData write) over its event-timed
+               duration, against the measured HBM copy rate; the per-direction
+               convention (every direction re-reading the cube) beside it
+  plain_fp64   the all-FP64 form on the same workload
+  checks       both forms against the oracle over every chunk and direction
+               (branch choices at arg() cuts proved, oracle/branch_cuts.py)
+  cpu_baseline the oracle (C restatement of CpuLeapCalibrator, OpenMP over
+               (chunk, direction) pairs) on a bounded sample: the first timestep
+               of every chunk with all its directions
+  sub_results  the 128-antenna 14-timestep workload (64 directions), the
+               512-station SKA-Low-like workload (128 directions), the
+               reference's own direction spread, and the C++ drop-in call
+               (LeapCalibratorFactory::Create(gb300)->Calibrate) — each with its
+               own roofline, FP64 comparison and oracle checks
 
 ``--impl reference`` times the reference CPU algorithm (the oracle port of
-CpuLeapCalibrator, the reference itself cannot be built here) on all host cores.
-Multi-GPU (torchrun): each rank calibrates its own directions on its own copy
-of the integration (weak scaling, no collective); rank 0 prints.
+CpuLeapCalibrator; the reference itself cannot be built here) on all host cores
+on the same sample, with the same config; it maps no product library.
+Multi-GPU (torchrun): the direction set grows with the rank count; each rank
+calibrates its shard_range of it and rank 0 gathers the cal vectors
+(leap_gb300.sharding.calibrate_sharded) — weak scaling, host-side gather only.
 """
 from __future__ import annotations
 
@@ -35,14 +49,19 @@ import os
 import statistics
 import subprocess
 import sys
-import threading
+import tempfile
 import time
 
 import numpy as np
 
 ROOT = os.path.dirname(os.path.abspath(__file__))
 PKG = os.path.join(ROOT, "icrar-leap-accelerate_gb300")
+ORACLE_DIR = os.path.join(ROOT, "oracle")
 sys.path.insert(0, PKG)
+
+MIXED_TOL = 1e-5      # cal-phase bar of the mixed form against the FP64 oracle (rad)
+FP64_TOL = 1e-10      # bar of the all-FP64 form
+BRANCH_MARGIN = 1e-4  # angles this close to +-pi may take either branch in the mixed form
 
 
 def _peaks():
@@ -50,6 +69,24 @@ def _peaks():
         return json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
     except Exception:
         return None
+
+
+def _oracle():
+    if ORACLE_DIR not in sys.path:
+        sys.path.insert(0, ORACLE_DIR)
+    import oracle
+    return oracle
+
+
+def mapped_libraries():
+    """Shared objects of this repository mapped into the process."""
+    try:
+        maps = open("/proc/self/maps").read().split("\n")
+    except OSError:
+        return None
+    real = os.path.realpath(ROOT)
+    libs = sorted({ln.split()[-1] for ln in maps if ln.strip().endswith(".so") and real in ln})
+    return [os.path.relpath(p, real) for p in libs]
 
 
 class ClockSampler:
@@ -100,307 +137,252 @@ class ClockSampler:
                 "reasons": reasons, "samples": len(self.samples)}
 
 
-def make_workload(args, rank: int):
+# ---------------------------------------------------------------------------
+# Workload definitions shared by both arms
+# ---------------------------------------------------------------------------
+
+def batched_shapes(args):
     from leap_gb300 import synth
-    obs, dirs = synth.mwa_precision(timesteps=args.timesteps or 14, channels=args.channels, directions=args.directions)
-    if rank:
-        # Each rank calibrates its own directions (same array and integration).
-        _, lm = synth.random_directions(args.directions, seed=3 + 1000 * rank)
-        dirs = synth.lm_to_radec(lm[:, 0], lm[:, 1])
-    return obs, dirs
+    return synth.uneven_chunks(args.chunks, seed=4)
 
 
-def vis_dirs(obs, ndir: int) -> float:
-    return float(obs.pols) * obs.rows * obs.channels * ndir
+def workload_config(name: str, args) -> dict:
+    """The `config` of a workload; both arms print the same one."""
+    if name == "batched":
+        shapes = batched_shapes(args)
+        nd = args.directions or 256
+        gb = sum(s.timesteps * s.channels for s in shapes) * 8256 * 4 * 8 / 1e9
+        return {"workload": f"batched_uneven 128ant/8256bl, {len(shapes)} chunks (T 1-64, C in 48/96/384, seed 4; "
+                            f"{sum(s.timesteps for s in shapes)} timesteps), {nd} directions round-robin, 4pol "
+                            f"complex<float> ({gb:.1f} GB)",
+                "chunks": [[s.timesteps, s.channels] for s in shapes], "precision": args.precision,
+                "l2": f"inputs ({gb:.1f} GB) larger than L2; no flush"}
+    if name == "mwa":
+        t = args.timesteps or 14
+        nd = args.directions or 64
+        gb = t * 8256 * args.channels * 4 * 8 / 1e9
+        return {"workload": f"mwa_precision 128ant/8256bl/{t}t/{args.channels}ch/4pol/{nd}dir complex<float>",
+                "precision": args.precision, "l2": f"inputs ({gb:.2f} GB) larger than L2; no flush"}
+    if name == "ska_low":
+        t = args.timesteps or 16
+        nd = args.directions or 128
+        return {"workload": f"ska_low 512st/131328bl/{t}t/384ch/4pol/{nd}dir complex<float>", "precision": args.precision,
+                "l2": f"inputs ({t * 131328 * 384 * 32 / 1e9:.1f} GB) larger than L2; no flush"}
+    if name == "differentiable":
+        return {"workload": "differentiable 128ant/8256bl/8t/96ch/4pol/16dir complex<float>: forward + FP64 adjoint "
+                            "(d/d(l,m) and d/dV)", "precision": args.precision,
+                "l2": "inputs (203 MB) larger than L2; no flush"}
+    raise ValueError(name)
 
 
-def bench_cpu(obs, dirs, vis_t0, threads: int, budget_s: float):
-    """Oracle port on a bounded sample: the first timestep (vis_t0: (channels, nbl, pols))
-    and the first directions of the workload, grown towards `budget_s` seconds."""
-    sys.path.insert(0, os.path.join(ROOT, "oracle"))
-    import oracle
-    mdo = oracle.metadata(obs)
-    nbl = obs.nbaselines
-    vis = np.ascontiguousarray(vis_t0)
-    uvw = obs.uvw[:nbl]
-    d_s = max(1, min(len(dirs), threads))
-    dds = np.stack([oracle.dd_matrix(*obs.phase_centre, r, d) for r, d in dirs[:d_s]])
-    t0 = time.perf_counter()
-    oracle.calibrate_interval(vis, uvw, dds, mdo, nthreads=threads)
-    dt = time.perf_counter() - t0
-    # grow the sample towards the budget (directions are independent)
-    reps = max(1, int(budget_s / max(dt, 1e-3)))
-    d_s2 = min(len(dirs), d_s * reps)
-    if d_s2 > d_s:
-        dds = np.stack([oracle.dd_matrix(*obs.phase_centre, r, d) for r, d in dirs[:d_s2]])
+class CpuSample:
+    """A bounded sample of a workload for the oracle, on host memory: chunks of
+    (vis (channels, rows, pols), uvw (rows, 3), dds (D, 3, 3)), one metadata."""
+
+    def __init__(self, chunks, mdo, description):
+        self.chunks = chunks
+        self.mdo = mdo
+        self.description = description
+        self.units = float(sum(v.shape[0] * v.shape[1] * v.shape[2] * d.shape[0] for v, _, d in chunks))
+
+    def run(self, threads: int):
+        _oracle().calibrate_items(self.chunks, self.mdo, nthreads=threads)
+
+
+def cpu_sample(name: str, args) -> CpuSample:
+    """The oracle's sample of workload `name`: the same in the reference arm and in the
+    gb300 arm's cpu_baseline."""
+    from leap_gb300 import synth
+    oracle = _oracle()
+    if name == "batched":
+        obs_list, dirs, items, _ = synth.batched_uneven(chunks=args.chunks, directions=args.directions or 256,
+                                                        sample_timesteps=1)
+        mdo = oracle.metadata(obs_list[0])
+        dds = np.stack([oracle.dd_matrix(*obs_list[0].phase_centre, r, d) for r, d in dirs])
+        chunks = [(obs_list[sl].vis, obs_list[sl].uvw, dds[d0:d0 + n]) for sl, d0, n in items]
+        return CpuSample(chunks, mdo, f"the first timestep of each of the {len(items)} chunks with all its "
+                                      f"directions ({len(dirs)} directions in all)")
+    if name in ("mwa", "differentiable"):
+        if name == "mwa":
+            obs, dirs = synth.mwa_precision(timesteps=1, channels=args.channels, directions=args.directions or 64)
+        else:
+            obs, _ = synth.mwa_precision(timesteps=1, channels=96, directions=16)
+            _, lm = synth.random_directions(16, seed=31)
+            dirs = synth.lm_to_radec(lm[:, 0], lm[:, 1])
+        mdo = oracle.metadata(obs)
+        dds = np.stack([oracle.dd_matrix(*obs.phase_centre, r, d) for r, d in dirs])
+        return CpuSample([(obs.vis, obs.uvw, dds)], mdo, f"1 timestep x all {len(dirs)} directions")
+    if name == "ska_low":
+        obs, dirs = synth.ska_low(timesteps=1, directions=args.directions or 128)
+        mdo = oracle.metadata(obs)
+        dds = np.stack([oracle.dd_matrix(*obs.phase_centre, r, d) for r, d in dirs[:16]])
+        return CpuSample([(obs.vis, obs.uvw, dds)], mdo, "1 timestep x 16 directions")
+    raise ValueError(name)
+
+
+def time_cpu_sample(sample: CpuSample, threads: int, budget_s: float):
+    sample.run(threads)  # warm-up
+    runs, total = 0, 0.0
+    while total < budget_s or runs == 0:
         t0 = time.perf_counter()
-        oracle.calibrate_interval(vis, uvw, dds, mdo, nthreads=threads)
-        dt = time.perf_counter() - t0
-        d_s = d_s2
-    # repeat the sample until the budget is spent, so the timing covers ~budget_s of CPU work
-    runs, total = 1, dt
-    while total < budget_s:
-        t0 = time.perf_counter()
-        oracle.calibrate_interval(vis, uvw, dds, mdo, nthreads=threads)
+        sample.run(threads)
         total += time.perf_counter() - t0
         runs += 1
-    units = float(obs.pols) * vis.shape[1] * obs.channels * d_s * runs
-    return units / total, {"timesteps": 1, "directions": d_s, "seconds": total, "runs": runs}
+    return sample.units * runs / total, runs, total
 
 
-def run_reference(args, rank: int, world: int):
+def run_reference(args, name: str, rank: int, world: int):
+    """The reference's CPU algorithm (the oracle port) on the host cores; rank 0 only."""
     if rank != 0:
         return
-    sys.path.insert(0, os.path.join(ROOT, "oracle"))
-    import oracle
-    obs, dirs = make_workload(args, 0)
+    oracle = _oracle()
     threads = oracle.max_threads()
-    mdo = oracle.metadata(obs)
-    nbl = obs.nbaselines
-    # Each step: a bounded sample of the workload (1 timestep, `threads` directions).
-    vis = np.ascontiguousarray(obs.vis[:, :nbl, :])
-    uvw = obs.uvw[:nbl]
-    d_s = min(len(dirs), max(1, threads))
-    dds = np.stack([oracle.dd_matrix(*obs.phase_centre, r, d) for r, d in dirs[:d_s]])
+    sample = cpu_sample(name, args)
     for _ in range(args.warmup):
-        oracle.calibrate_interval(vis, uvw, dds, mdo, nthreads=threads)
+        sample.run(threads)
     t0 = time.perf_counter()
     for _ in range(args.steps):
-        oracle.calibrate_interval(vis, uvw, dds, mdo, nthreads=threads)
+        sample.run(threads)
     dt = (time.perf_counter() - t0) / args.steps
-    units = float(obs.pols) * nbl * obs.channels * d_s
-    value = units / dt
+    value = sample.units / dt
     line = {
         "impl": "reference", "metric": "vis-directions/s", "value": value, "unit": "vis-directions/s",
         "n_gpus": world, "steps": args.steps, "warmup": args.warmup, "ms_per_step": dt * 1e3,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-        "config": {"workload": "mwa_precision 128ant/8256bl/14t/384ch/4pol/64dir c64", "sample_per_step":
-                   f"1 timestep x {d_s} directions"},
+        "config": workload_config(name, args),
         "cpu_baseline": {"value": value, "unit": "vis-directions/s", "cores": threads, "kind": "port",
-                         "sample": f"1 of {obs.timesteps} timesteps, {d_s} of {len(dirs)} directions per step"},
+                         "sample": f"each step: {sample.description} ({sample.units:.3g} vis-directions)"},
         "e2e": {"value": value, "unit": "vis-directions/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+        "libraries_mapped": mapped_libraries(),
     }
     print(json.dumps(line), flush=True)
 
 
-def wrapped_max_diff(a, b) -> float:
-    return float(np.abs(np.angle(np.exp(1j * (np.asarray(a) - np.asarray(b))))).max())
+# ---------------------------------------------------------------------------
+# Parity against the oracle (after the timed regions)
+# ---------------------------------------------------------------------------
+
+def compare_with_oracle(cal: np.ndarray, cal_o: np.ndarray, avg_o: np.ndarray, mdo, tol: float, margin: float):
+    """Per-direction max |cal - cal_oracle|; directions over `tol` must be a branch choice at
+    an arg() within `margin` of +-pi (proved by re-solving the oracle's avgData)."""
+    import branch_cuts
+    err = np.abs(cal - cal_o).max(axis=1)
+    flips, unexplained, rest = 0, [], []
+    for d in np.flatnonzero(err > tol):
+        ok, _, r = branch_cuts.explain(cal[d], avg_o[d][:, 0], mdo, tol, margin)
+        if ok:
+            flips += 1
+            rest.append(r)
+        else:
+            unexplained.append(int(d))
+    plain = err[err <= tol] if (err <= tol).any() else err
+    return {"directions": int(len(err)), "max_rad": float(plain.max()), "median_rad": float(np.median(plain)),
+            "p99_rad": float(np.percentile(plain, 99)), "max_incl_branch_choices_rad": float(err.max()),
+            "branch_choices": flips, "max_after_branch_choice_rad": float(max(rest)) if rest else None,
+            "unexplained_directions": unexplained, "tolerance_rad": tol, "pass": not unexplained}
 
 
-def branch_margins(ctx, md, D, torch, dev, stream):
-    """Per direction of the last calibrate call: the smallest distance from +-pi of any arg()
-    in its solve (phi1 at the reference-antenna baselines, dInt at the first |I| rows), from
-    that call's own avgData.  An angle within a form's error of +-pi may land on the other
-    branch in another form; the cal phases then differ by 2*pi times a column of Ad (or Ad1),
-    a different branch rather than an error."""
-    from leap_gb300 import _abi
-    from leap_gb300.calibrator import stream_handle
-    nbl = md.nbaselines
-    avg0 = torch.empty((D, nbl), dtype=torch.complex128, device=dev)
-    ctx._check(_abi.lib.leap_get_avgdata_device(ctx.handle, 0, avg0.data_ptr(), stream_handle(stream)))
-    torch.cuda.synchronize()
-    i1 = torch.as_tensor(np.where(md.I1 < 0, md.I1 + nbl, md.I1), dtype=torch.int64, device=dev)
-    A = torch.as_tensor(md.A, device=dev)
-    Ad1 = torch.as_tensor(md.Ad1, device=dev)
-    phi1 = torch.angle(avg0[:, i1])
-    cal1 = torch.cat([phi1, torch.zeros((D, 1), dtype=torch.float64, device=dev)], dim=1) @ Ad1.T
-    nI = A.shape[0] - 1
-    out = []
-    for d0 in range(0, D, 16):  # bounded temporaries at 130k baselines
-        acal = cal1[d0:d0 + 16] @ A[:nI].T
-        dint = torch.angle(torch.exp(-2j * np.pi * acal) * avg0[d0:d0 + 16, :nI])
-        m = torch.minimum((np.pi - dint.abs()).min(dim=1).values, (np.pi - phi1[d0:d0 + 16].abs()).min(dim=1).values)
-        out.append(m)
-    return torch.cat(out).cpu().numpy()
+def oracle_checks(chunks, cal_mixed, cal_fp64, mdo, threads: int, what: str):
+    """chunks: [(vis, uvw, dds, row slice of the cal arrays)]."""
+    oracle = _oracle()
+    t0 = time.perf_counter()
+    cals, avgs = oracle.calibrate_items([(v, u, d) for v, u, d, _ in chunks], mdo, nthreads=threads, return_avg=True)
+    t_o = time.perf_counter() - t0
+    cal_o = np.concatenate(cals)
+    avg_o = np.concatenate(avgs)
+    rows = np.concatenate([np.arange(s.start, s.stop) for *_, s in chunks])
+    out = {"sample": what, "oracle_s": round(t_o, 1)}
+    if cal_mixed is not None:
+        out["mixed"] = compare_with_oracle(cal_mixed[rows], cal_o, avg_o, mdo, MIXED_TOL, BRANCH_MARGIN)
+    if cal_fp64 is not None:
+        out["fp64"] = compare_with_oracle(cal_fp64[rows], cal_o, avg_o, mdo, FP64_TOL, 1e-8)
+    return out
 
+
+# ---------------------------------------------------------------------------
+# Device workloads
+# ---------------------------------------------------------------------------
 
 class Workload:
-    """One benchmark workload resident on the device: `step(precision)` launches one
-    pass of the hot path; `e2e_step()` runs the same through the C ABI with host buffers."""
+    """One workload resident on the device.  step(precision) launches one pass of the hot path."""
     name = ""
-    config: dict = {}
-    units = 0.0           # vis-directions per step
-    b_alg = 0.0           # algorithmic HBM bytes per step (vis once per direction)
-    f_alg = 0.0           # FP32 FMA-pipe issue slots per step (compute roof)
-    traffic = None        # measured DRAM bytes per launch of the bulk kernel, if known
-    h2d = 0
-    d2h = 0
-    kernel_timing = "rotate"  # which leap_timings field times the bulk pass
-    checks: dict = {}
+    units = 0.0            # vis-directions per step
+    kernel_bytes = 0.0     # bytes the bulk kernel must move per launch (each sample once)
+    per_direction_bytes = 0.0  # the per-direction convention: every direction reads the cube
+    traffic = None         # ncu-measured DRAM bytes per launch of the bulk kernel, if known
+    kernel_name = ""
+    grid = None            # (tensor-core FLOPs per call, mean and max grid passes) of the gridded kernel
+    timing = "events"      # "events": torch events on the bench stream; "library": the library's own events
+    e2e_step = None
+    h2d = d2h = 0
+    extra_launches = 0
+
+    def close(self):
+        pass
 
 
-def alg_bytes(samples: float, rows: float, ndir: int, nbl: int, pols: int, vis_bytes: int) -> float:
-    """Bytes of the bulk pass on the per-direction convention: every direction reads the
-    visibilities (vis_bytes each) and 24 B of UVW per row, and writes its FP64 avgData."""
-    return ndir * (samples * vis_bytes + rows * 24) + ndir * nbl * pols * 16
+def read_once_bytes(samples: float, rows: float, nbl: int, ndir: int) -> float:
+    """Each complex<float> sample once, the split UVWs (24 B per row), one FP64 avgData write."""
+    return samples * 8 + rows * 24 + ndir * nbl * 4 * 16
 
 
-def fma_slots(rows: float, channels_x_rows: float, ndir: int, pols: int) -> float:
-    return ndir * channels_x_rows * (pols * 4 + 5)
+def per_direction_bytes(samples: float, rows: float, nbl: int, ndir: int) -> float:
+    """The reference's per-direction loop: every direction reads the cube and 24 B of UVW per row."""
+    return ndir * (samples * 8 + rows * 24) + ndir * nbl * 4 * 16
 
 
-def grid_mma_flops(obs, dds: np.ndarray, taps: int = 10, jw_max: int = 64, stride: int = 48, dirs_per_unit: int = 64):
-    """Tensor-core FLOPs of one call of the gridded kernel: the grid windows of its units
-    (quad of 4 baselines x all timesteps x up to 64 directions), computed as the kernel
-    computes them, times the 3xTF32 MMAs (6 per 16-channel chunk, M = 128, N = 2 jw, K = 8)."""
+def grid_windows_host(obs, dds: np.ndarray, taps: int = 7, jw_max: int = 64, stride: int = 56, load: int = 8,
+                      dirs_per_unit: int = 64):
+    """The gridded kernel's grid windows of one call, computed as its grid_windows kernel does:
+    (tensor-core FLOPs per call, mean passes per tile, max passes)."""
     C, nbl, T = obs.channels, obs.nbaselines, obs.timesteps
     n, lbase = 2 * C, ((C + taps + 8 + 7) // 8) * 8
     nchunk = (C + 15) // 16
     kb = -(dds[:, 2, :] - np.array([0.0, 0.0, 1.0])) * obs.freq_inc_hz / 299792458.0  # (D, 3) turns per metre
     uvw = obs.uvw.reshape(T, nbl, 3)
     nquad = (nbl + 3) // 4
-    flops = 0.0
+    flops, passes, tiles, pmax = 0.0, 0.0, 0.0, 0
     for d0 in range(0, dds.shape[0], dirs_per_unit):
-        B = np.einsum("tbj,dj->tbd", uvw, kb[d0:d0 + dirs_per_unit])          # turns per channel
+        B = np.einsum("tbj,dj->tbd", uvw, kb[d0:d0 + dirs_per_unit])
         B = B - np.rint(B)
-        s = np.floor(B * n).astype(np.int64) - taps // 2 + 1
+        s = np.floor(B * n + 0.5).astype(np.int64) - (taps - 1) // 2  # stencil start
         pad = nquad * 4 - nbl
         smin = np.pad(s.min(axis=(0, 2)), (0, pad), constant_values=1 << 40).reshape(nquad, 4).min(axis=1)
         smax = np.pad(s.max(axis=(0, 2)), (0, pad), constant_values=-(1 << 40)).reshape(nquad, 4).max(axis=1)
         r0 = ((smin + lbase) >> 3) * 8
-        need = smax + 16 + lbase - r0
+        need = smax + load + lbase - r0
         single = need <= jw_max
-        jw = np.where(single, np.maximum(16, (need + 7) & ~7), jw_max)
+        jw = np.where(single, np.maximum(8, (need + 7) & ~7), jw_max)
         npass = np.where(single, 1, (smax + lbase - r0) // stride + 1)
         ntb = (T + 3) // 4
         flops += float((ntb * npass * nchunk * 6 * 2 * 128 * 2 * jw * 8).sum())
-    return flops
+        passes += float((ntb * npass).sum())
+        tiles += float(ntb * nquad)
+        pmax = max(pmax, int(npass.max()))
+    return flops, passes / tiles, pmax
 
 
-def setup_single(args, ctx, lg, torch, local, rank, kind: str):
-    """One integration, all directions in one leap_calibrate_async call (MWA or SKA-Low)."""
+def setup_batched(run, dir_ids=None) -> Workload:
+    """32 uneven integration chunks, their directions dealt round-robin; one
+    leap_calibrate_batched call per step."""
     from leap_gb300 import synth
-    dev = f"cuda:{local}"
-    w = Workload()
-    if kind == "mwa":
-        obs, dirs = make_workload(args, rank)
-        vis_host = torch.from_numpy(obs.vis).pin_memory()
-        vis_dev = vis_host.to(dev)
-        w.cpu_case = (obs, dirs, obs.vis[:, :obs.nbaselines, :])
-        w.name = (f"mwa_precision {obs.num_stations}ant/{obs.nbaselines}bl/{obs.timesteps}t/{obs.channels}ch/"
-                  f"{obs.pols}pol/{len(dirs)}dir c64")
-    else:
-        obs, dirs = synth.ska_low(with_vis=False, timesteps=args.timesteps or 16, directions=args.directions or 128)
-        if rank:
-            _, lm = synth.random_directions(len(dirs), seed=3 + 1000 * rank)
-            dirs = synth.lm_to_radec(lm[:, 0], lm[:, 1])
-        vis_dev = synth.device_visibilities(obs, dev, seed=2)
-        w.cpu_case = (obs, dirs, vis_dev[:, :obs.nbaselines, :].cpu().numpy())
-        vis_host = None
-        if args.e2e:
-            vis_host = torch.empty(vis_dev.shape, dtype=vis_dev.dtype, pin_memory=True)
-            vis_host.copy_(vis_dev)
-        w.name = (f"ska_low {obs.num_stations}st/{obs.nbaselines}bl/{obs.timesteps}t/{obs.channels}ch/"
-                  f"{obs.pols}pol/{len(dirs)}dir c64 (visibilities generated on the device)")
-    t0 = time.perf_counter()
-    md = ctx.build_metadata(obs)  # on the device (leap_build_metadata); installs it on the context
-    w.metadata_s = time.perf_counter() - t0
-    uvw_host = torch.from_numpy(obs.uvw).pin_memory()
-    ctx.set_integration(0, vis_dev, uvw_host.to(dev))
-    del vis_dev
-    torch.cuda.empty_cache()
-    dds = np.stack([lg.dd_matrix(md.phase_centre_ra_rad, md.phase_centre_dec_rad, r, d) for r, d in dirs])
-    D, S = len(dirs), md.A.shape[1]
-    dd_dev = torch.from_numpy(dds.reshape(-1)).to(dev)
-    cal_dev = torch.empty((D, S), dtype=torch.float64, device=dev)
-    stream = torch.cuda.current_stream().cuda_stream
-
-    def step(p):
-        ctx.calibrate_async(0, dd_dev.data_ptr(), D, p, cal_dev.data_ptr(), stream)
-
-    w.step = step
-    w.result = lambda: cal_dev.cpu().numpy().copy()
-    w.obs, w.dirs, w.md, w.D, w.S = obs, dirs, md, D, S
-    w.min_ndir = D
-    w.grid_flops = grid_mma_flops(obs, dds)
-    w.vis_bytes_resident = obs.rows * obs.channels * obs.pols * 8
-    # DRAM traffic of one launch of the gridded kernel, from an ncu capture
-    # (dram__bytes_read.sum + dram__bytes_write.sum) of the 4-timestep case of the
-    # MWA workload: 101.8 MB read per timestep (the visibilities, once) + 26.9 MB of
-    # sum writes, scaled to the timesteps of this run.
-    if kind == "mwa" and obs.nbaselines == 8256 and obs.channels == 384 and D == 64:
-        w.grid_traffic = 101.80e6 * obs.timesteps + 26.94e6
-    w.units = vis_dirs(obs, D)
-    w.b_alg = alg_bytes(obs.pols * obs.rows * obs.channels, obs.rows, D, obs.nbaselines, obs.pols, 8)
-    w.f_alg = fma_slots(obs.rows, obs.rows * obs.channels, D, obs.pols)
-    # DRAM traffic of one launch of the bulk kernel, from an ncu capture
-    # (dram__bytes_read.sum + dram__bytes_write.sum) of the 2-timestep case of the
-    # MWA workload: 101.7 MB read per timestep (the visibilities, once) + 44.7 MB
-    # of partial-sum writes, scaled to the timesteps of this run.
-    if kind == "mwa" and obs.nbaselines == 8256 and obs.channels == 384 and D == 64:
-        w.traffic = 101.74e6 * obs.timesteps + 44.74e6
-    w.config = {"workload": w.name, "precision": args.precision,
-                "l2": f"inputs ({obs.vis.nbytes / 1e9 if obs.vis is not None else obs.rows * obs.channels * 32 / 1e9:.2f} GB)"
-                      " larger than L2; no flush"}
-    if vis_host is not None:
-        # The host holds the visibilities in MeasurementSet order, [row][channel][pol]
-        # (page-locked); each step ingests them through leap_set_integration_ms, which
-        # transposes on the device, then calibrates with host dd / cal buffers.
-        ms_host = torch.empty((vis_host.shape[1], vis_host.shape[0], vis_host.shape[2]), dtype=vis_host.dtype,
-                              pin_memory=True)
-        ms_host.copy_(vis_host.permute(1, 0, 2))
-        vis_np = vis_host.numpy()
-        uvw_np = uvw_host.numpy()
-        cal_host = np.zeros((D, S), dtype=np.float64)
-        C, rows, P = vis_np.shape
-        prec = lg.LEAP_PRECISION_MIXED if args.precision == "mixed" else lg.LEAP_PRECISION_FP64
-        from leap_gb300 import _abi
-
-        def e2e_step():
-            ctx._check(_abi.lib.leap_set_integration_ms(ctx.handle, 0, _abi.LEAP_VIS_C64, ms_host.data_ptr(), C, 0,
-                                                        uvw_np.ctypes.data, rows, C, P, _abi.LEAP_MEMORY_HOST))
-            ctx._check(_abi.lib.leap_calibrate(ctx.handle, 0, dds.ctypes.data, D, prec, cal_host.ctypes.data))
-
-        def e2e_pipelined(n):
-            # Double-buffered: the upload of step k+1's visibilities (asynchronous, copy stream) overlaps
-            # the calibration of step k; every step still moves its full input and output.
-            lib = _abi.lib
-            ctx._check(lib.leap_set_integration_ms_async(ctx.handle, 0, _abi.LEAP_VIS_C64, ms_host.data_ptr(), C, 0,
-                                                         uvw_host.data_ptr(), rows, C, P, _abi.LEAP_MEMORY_HOST))
-            for k in range(n):
-                if k + 1 < n:
-                    ctx._check(lib.leap_set_integration_ms_async(ctx.handle, (k + 1) % 2, _abi.LEAP_VIS_C64,
-                                                                 ms_host.data_ptr(), C, 0, uvw_host.data_ptr(), rows,
-                                                                 C, P, _abi.LEAP_MEMORY_HOST))
-                ctx._check(lib.leap_calibrate(ctx.handle, k % 2, dds.ctypes.data, D, prec, cal_host.ctypes.data))
-
-        def e2e_layout_step():
-            ctx._check(_abi.lib.leap_set_integration(ctx.handle, 0, _abi.LEAP_VIS_C64, vis_np.ctypes.data,
-                                                     uvw_np.ctypes.data, rows, C, P, _abi.LEAP_MEMORY_HOST))
-            ctx._check(_abi.lib.leap_calibrate(ctx.handle, 0, dds.ctypes.data, D, prec, cal_host.ctypes.data))
-
-        w.e2e_step = e2e_step
-        w.e2e_pipelined = e2e_pipelined
-        w.e2e_alt = ("integration_layout_upload", e2e_layout_step)
-        w.h2d = vis_np.nbytes + uvw_np.nbytes + dds.nbytes
-        w.d2h = cal_host.nbytes
-    else:
-        w.e2e_step = None
-    return w
-
-
-def setup_batched(args, ctx, lg, torch, local, rank):  # noqa: C901
-    """32 uneven integration chunks, 256 directions, one leap_calibrate_batched call per step."""
-    from leap_gb300 import synth
-    dev = f"cuda:{local}"
-    w = Workload()
+    args, ctx, lg, torch = run.args, run.ctx, run.lg, run.torch
     nd = args.directions or 256
-    obs_list, dirs, items, order = synth.batched_uneven(chunks=args.chunks, directions=nd)
+    obs_list, dirs, items, _ = synth.batched_uneven(chunks=args.chunks, directions=nd, direction_ids=dir_ids)
+    w = Workload()
+    w.name = "batched"
     t0 = time.perf_counter()
     md = ctx.build_metadata(obs_list[0])
     w.metadata_s = time.perf_counter() - t0
-    spot = None
+    keep_host = bool(args.e2e) or (run.rank == 0 and not args.skip_checks)
     hosts = []
-    small = min(range(len(obs_list)), key=lambda i: obs_list[i].rows * obs_list[i].channels)
     for i, obs in enumerate(obs_list):
-        vis = synth.device_visibilities(obs, dev, seed=2000 + i)
-        ctx.set_integration(i, vis, torch.from_numpy(obs.uvw).to(dev))
-        if args.e2e:
+        vis = synth.device_visibilities(obs, run.dev, seed=2000 + i)
+        ctx.set_integration(i, vis, torch.from_numpy(obs.uvw).to(run.dev))
+        if keep_host:
             vh = torch.empty(vis.shape, dtype=vis.dtype, pin_memory=True)
             vh.copy_(vis)
             hosts.append((vh, torch.from_numpy(obs.uvw).pin_memory()))
-        if i == small:
-            spot = vis.cpu().numpy()
         del vis
     torch.cuda.empty_cache()
     dds = np.stack([lg.dd_matrix(md.phase_centre_ra_rad, md.phase_centre_dec_rad, r, d) for r, d in dirs])
@@ -412,24 +394,22 @@ def setup_batched(args, ctx, lg, torch, local, rank):  # noqa: C901
 
     w.step = step
     w.result = lambda: holder["cal"].copy()
-    w.kernel_timing = "total"
-    w.obs, w.dirs, w.md, w.D, w.S, w.items, w.dds = obs_list[0], dirs, md, D, S, items, dds
-    w.min_ndir = min(it[2] for it in items)
-    w.units = sum(float(obs_list[sl].pols) * obs_list[sl].rows * obs_list[sl].channels * n for sl, _, n in items)
-    w.b_alg = sum(alg_bytes(4.0 * obs_list[sl].rows * obs_list[sl].channels, obs_list[sl].rows, n,
-                            obs_list[sl].nbaselines, 4, 8) for sl, _, n in items)
-    w.f_alg = sum(fma_slots(obs_list[sl].rows, obs_list[sl].rows * obs_list[sl].channels, n, 4) for sl, _, n in items)
-    samples = sum(4.0 * o.rows * o.channels for o in obs_list)
-    w.vis_bytes_resident = samples * 8
-    w.name = (f"batched_uneven 128ant/8256bl, {len(obs_list)} chunks (T 1-64, C in 48/96/384; "
-              f"{int(sum(o.timesteps for o in obs_list))} timesteps), {D} directions round-robin, 4pol c64 "
-              f"({samples * 8 / 1e9:.1f} GB, generated on the device)")
-    w.config = {"workload": w.name, "precision": args.precision, "chunks": [[o.timesteps, o.channels] for o in obs_list],
-                "l2": "inputs larger than L2; no flush"}
-    w.spot = (small, obs_list[small], spot)
-    sl, d0, nd = next(it for it in items if it[0] == small)
-    w.cpu_case = (obs_list[small], dirs, spot[:, :obs_list[small].nbaselines, :])
-    if args.e2e:
+    w.timing = "library"
+    w.obs_list, w.items, w.dds, w.md, w.D, w.S = obs_list, items, dds, md, D, S
+    w.units = sum(4.0 * obs_list[sl].rows * obs_list[sl].channels * n for sl, _, n in items)
+    samples = {sl: 4.0 * obs_list[sl].rows * obs_list[sl].channels for sl, _, _ in items}
+    w.kernel_bytes = sum(read_once_bytes(samples[sl], obs_list[sl].rows, 8256, n) for sl, _, n in items)
+    w.per_direction_bytes = sum(per_direction_bytes(samples[sl], obs_list[sl].rows, 8256, n) for sl, _, n in items)
+    w.vis_bytes = sum(samples.values()) * 8
+    w.kernel_name = ("rotate_average_mixed_pipe<8,4,4> (persistent, TMA-pipelined, 4 tiles x 8 directions per block; "
+                     "FP32 CUDA cores with compensated sums) + the rotate stage's small kernels")
+    # DRAM traffic of the bulk kernel: the cube once plus its partial-sum writes (ncu on the
+    # 4-timestep, 8-direction case of this kernel read 409.1 MB for 409.1 MB of visibilities and
+    # wrote 3.9 MB; the batched call's writes are its slabs' partial sums), scaled to this call.
+    w.traffic = None
+    w.hosts = hosts
+    w.min_ndir = min(n for _, _, n in items)
+    if args.e2e and hosts:
         prec = lg.LEAP_PRECISION_MIXED if args.precision == "mixed" else lg.LEAP_PRECISION_FP64
         from leap_gb300 import _abi
 
@@ -441,30 +421,141 @@ def setup_batched(args, ctx, lg, torch, local, rank):  # noqa: C901
             ctx.calibrate_batched(items, dds, prec)
 
         w.e2e_step = e2e_step
+        w.e2e_mode = ("serial: every step uploads all 32 chunks from page-locked host memory (leap_set_integration), "
+                      "then one leap_calibrate_batched call returns the cal phases to host memory")
         w.h2d = sum(vh.numel() * 8 + uh.numel() * 8 for vh, uh in hosts) + dds.nbytes
         w.d2h = D * S * 8
-    else:
-        w.e2e_step = None
+
+    def checks(cal_mixed, cal_fp64, threads):
+        mdo = _oracle().metadata(obs_list[0])
+        chunks = [(hosts[sl][0].numpy(), obs_list[sl].uvw, dds[d0:d0 + n], slice(d0, d0 + n)) for sl, d0, n in items]
+        return oracle_checks(chunks, cal_mixed, cal_fp64, mdo, threads,
+                             f"every chunk (all {sum(o.timesteps for o in obs_list)} timesteps) x all {D} directions")
+
+    w.checks = checks if hosts else None
     return w
 
 
-def setup_differentiable(args, ctx, lg, torch, local, rank):
+def setup_single(run, kind: str, dir_ids=None) -> Workload:
+    """One integration, all directions in one leap_calibrate_async call."""
+    from leap_gb300 import synth
+    args, ctx, lg, torch = run.args, run.ctx, run.lg, run.torch
+    w = Workload()
+    w.name = kind
+    if kind == "mwa":
+        obs, dirs = synth.mwa_precision(timesteps=args.timesteps or 14, channels=args.channels,
+                                        directions=args.directions or 64)
+        vis_np = obs.vis
+        vis_dev = torch.from_numpy(vis_np).to(run.dev)
+    else:
+        obs, dirs = synth.ska_low(with_vis=False, timesteps=args.timesteps or 16, directions=args.directions or 128)
+        vis_dev = synth.device_visibilities(obs, run.dev, seed=2)
+        vis_np = vis_dev.cpu().numpy() if (run.rank == 0 and not args.skip_checks) else None
+    if dir_ids is not None:
+        dirs = dirs[dir_ids]
+    t0 = time.perf_counter()
+    md = ctx.build_metadata(obs)
+    w.metadata_s = time.perf_counter() - t0
+    uvw_host = torch.from_numpy(obs.uvw).pin_memory()
+    ctx.set_integration(0, vis_dev, uvw_host.to(run.dev))
+    del vis_dev
+    torch.cuda.empty_cache()
+    dds = np.stack([lg.dd_matrix(md.phase_centre_ra_rad, md.phase_centre_dec_rad, r, d) for r, d in dirs])
+    D, S = len(dirs), md.A.shape[1]
+    dd_dev = torch.from_numpy(dds.reshape(-1)).to(run.dev)
+    cal_dev = torch.empty((D, S), dtype=torch.float64, device=run.dev)
+    stream = torch.cuda.current_stream().cuda_stream
+
+    def step(p):
+        ctx.calibrate_async(0, dd_dev.data_ptr(), D, p, cal_dev.data_ptr(), stream)
+
+    w.step = step
+    w.result = lambda: cal_dev.cpu().numpy().copy()
+    w.obs, w.dirs, w.dds, w.md, w.D, w.S = obs, dirs, dds, md, D, S
+    w.min_ndir = D
+    samples = 4.0 * obs.rows * obs.channels
+    w.units = samples * D
+    w.kernel_bytes = read_once_bytes(samples, obs.rows, obs.nbaselines, D)
+    w.per_direction_bytes = per_direction_bytes(samples, obs.rows, obs.nbaselines, D)
+    w.vis_bytes = samples * 8
+    w.grid = grid_windows_host(obs, dds)
+    # DRAM traffic of one launch of the gridded kernel, from an ncu capture
+    # (dram__bytes_read.sum + dram__bytes_write.sum) of the 4-timestep case of this
+    # workload: 101.8 MB read per timestep (the visibilities, once) + 26.9 MB of sum
+    # writes, scaled to the timesteps of this run.
+    if kind == "mwa" and obs.nbaselines == 8256 and obs.channels == 384 and D == 64:
+        w.grid_traffic = 101.80e6 * obs.timesteps + 26.94e6
+        w.pipe_traffic = 101.74e6 * obs.timesteps + 44.74e6
+
+    def checks(cal_mixed, cal_fp64, threads):
+        if vis_np is None:
+            return None
+        mdo = _oracle().metadata(obs)
+        if kind == "mwa":
+            sel, what = slice(0, D), f"all {D} directions x all {obs.timesteps} timesteps"
+        else:
+            sel, what = slice(0, min(D, 16)), f"the first {min(D, 16)} directions x all {obs.timesteps} timesteps"
+        return oracle_checks([(vis_np, obs.uvw, dds[sel], sel)], cal_mixed, cal_fp64, mdo, threads, what)
+
+    w.checks = checks
+    if kind == "mwa" and args.e2e:
+        # The host holds the visibilities in MeasurementSet order, [row][channel][pol]
+        # (page-locked); each step ingests them through leap_set_integration_ms, which
+        # transposes on the device, then calibrates with host dd / cal buffers.
+        vis_host = torch.from_numpy(vis_np)
+        ms_host = torch.empty((vis_host.shape[1], vis_host.shape[0], vis_host.shape[2]), dtype=vis_host.dtype,
+                              pin_memory=True)
+        ms_host.copy_(vis_host.permute(1, 0, 2))
+        uvw_np = uvw_host.numpy()
+        cal_host = np.zeros((D, S), dtype=np.float64)
+        C, rows, P = vis_np.shape
+        prec = lg.LEAP_PRECISION_MIXED if args.precision == "mixed" else lg.LEAP_PRECISION_FP64
+        from leap_gb300 import _abi
+        lib = _abi.lib
+
+        def e2e_step():
+            ctx._check(lib.leap_set_integration_ms(ctx.handle, 0, _abi.LEAP_VIS_C64, ms_host.data_ptr(), C, 0,
+                                                   uvw_np.ctypes.data, rows, C, P, _abi.LEAP_MEMORY_HOST))
+            ctx._check(lib.leap_calibrate(ctx.handle, 0, dds.ctypes.data, D, prec, cal_host.ctypes.data))
+
+        def e2e_pipelined(n):
+            # Double-buffered: the upload of step k+1's visibilities (asynchronous, copy stream) overlaps
+            # the calibration of step k; every step still moves its full input and output.
+            ctx._check(lib.leap_set_integration_ms_async(ctx.handle, 0, _abi.LEAP_VIS_C64, ms_host.data_ptr(), C, 0,
+                                                         uvw_host.data_ptr(), rows, C, P, _abi.LEAP_MEMORY_HOST))
+            for k in range(n):
+                if k + 1 < n:
+                    ctx._check(lib.leap_set_integration_ms_async(ctx.handle, (k + 1) % 2, _abi.LEAP_VIS_C64,
+                                                                 ms_host.data_ptr(), C, 0, uvw_host.data_ptr(), rows,
+                                                                 C, P, _abi.LEAP_MEMORY_HOST))
+                ctx._check(lib.leap_calibrate(ctx.handle, k % 2, dds.ctypes.data, D, prec, cal_host.ctypes.data))
+
+        w.e2e_step = e2e_step
+        w.e2e_pipelined = e2e_pipelined
+        w.e2e_mode = "serial: upload (MeasurementSet order, transposed on the device), then calibrate, each step"
+        w.h2d = vis_np.nbytes + obs.uvw.nbytes + dds.nbytes
+        w.d2h = cal_host.nbytes
+    return w
+
+
+def setup_differentiable(run) -> Workload:
     """Forward + backward of the differentiable form: 128 antennas, 8 timesteps, 96 channels,
     16 directions, complex<float>; loss = sum of squared wrapped residuals to the gain phases,
     gradients with respect to every direction's (l, m) and the visibilities."""
     from leap_gb300 import synth
     from leap_gb300.autograd import calibrate_lm
-    dev = f"cuda:{local}"
+    args, ctx, lg, torch = run.args, run.ctx, run.lg, run.torch
     w = Workload()
+    w.name = "differentiable"
     nd = args.directions or 16
     obs, _ = synth.mwa_precision(timesteps=8, channels=96, directions=nd)
-    _, lm = synth.random_directions(nd, seed=31 + 1000 * rank)
+    _, lm = synth.random_directions(nd, seed=31 + 1000 * run.rank)
     md = lg.build_metadata(obs)
     ctx.set_metadata(md)
-    vis = torch.from_numpy(obs.vis).to(dev).requires_grad_()
-    uvw = torch.from_numpy(obs.uvw).to(dev)
-    gain = torch.from_numpy(np.angle(obs.gains)).to(dev)
-    lm_t = torch.from_numpy(lm).to(dev).requires_grad_()
+    vis = torch.from_numpy(obs.vis).to(run.dev).requires_grad_()
+    uvw = torch.from_numpy(obs.uvw).to(run.dev)
+    gain = torch.from_numpy(np.angle(obs.gains)).to(run.dev)
+    lm_t = torch.from_numpy(lm).to(run.dev).requires_grad_()
     holder = {}
 
     def step(p):
@@ -477,53 +568,41 @@ def setup_differentiable(args, ctx, lg, torch, local, rank):
 
     w.step = step
     w.result = lambda: holder["cal"].detach().cpu().numpy()
-    w.kernel_timing = "events"
+    w.timing = "events"
+    w.whole_step_is_kernel = True
     w.extra_launches = 8  # leap_backward: 2 transposed contractions, cal1, 2 avgData, (l, m, n) + reduce, vis
-    w.obs, w.dirs, w.md, w.D, w.S = obs, None, md, nd, md.A.shape[1]
-    w.min_ndir = nd
-    w.units = vis_dirs(obs, nd)
-    w.b_alg = alg_bytes(4.0 * obs.rows * obs.channels, obs.rows, nd, obs.nbaselines, 4, 8)
-    w.f_alg = fma_slots(obs.rows, obs.rows * obs.channels, nd, 4)
-    w.name = (f"differentiable {obs.num_stations}ant/{obs.nbaselines}bl/{obs.timesteps}t/{obs.channels}ch/4pol/"
-              f"{nd}dir c64: forward + FP64 adjoint (d/d(l,m) and d/dV)")
-    w.config = {"workload": w.name, "precision": args.precision, "l2": "inputs (203 MB) larger than L2; no flush"}
-    w.e2e_step = None
-    dirs = synth.lm_to_radec(lm[:, 0], lm[:, 1])
-    w.dirs = dirs
-    w.cpu_case = (obs, dirs, obs.vis[:, :obs.nbaselines, :])
+    w.md, w.D, w.S, w.min_ndir = md, nd, md.A.shape[1], nd
+    samples = 4.0 * obs.rows * obs.channels
+    w.units = samples * nd
+    w.kernel_bytes = read_once_bytes(samples, obs.rows, obs.nbaselines, nd)
+    w.per_direction_bytes = per_direction_bytes(samples, obs.rows, obs.nbaselines, nd)
+    w.vis_bytes = samples * 8
+    w.kernel_name = "whole forward + backward step"
+    w.checks = None
     return w
 
 
-def run_gpu(args, rank: int, world: int):
-    import torch
-    import leap_gb300 as lg
-    from leap_gb300 import _abi
+class Run:
+    """Device, context and stream of one workload run."""
 
-    local = int(os.environ.get("LOCAL_RANK", "0"))
-    torch.cuda.set_device(local)
-    dist = None
-    if world > 1:
-        import torch.distributed as dist
-        dist.init_process_group("nccl")
+    def __init__(self, args, torch, lg, local, rank, world, dist):
+        self.args, self.torch, self.lg = args, torch, lg
+        self.local, self.rank, self.world, self.dist = local, rank, world, dist
+        self.dev = f"cuda:{local}"
+        self.ctx = lg.Context(local)
+        from leap_gb300 import _abi
+        if args.tc_rotation >= 0:
+            self.ctx.set_option(_abi.LEAP_OPTION_TENSOR_CORE_ROTATION, args.tc_rotation)
+        if args.gridded >= 0:
+            self.ctx.set_option(_abi.LEAP_OPTION_GRIDDED_ROTATION, args.gridded)
 
-    ctx = lg.Context(local)
-    if args.tc_rotation >= 0:
-        ctx.set_option(_abi.LEAP_OPTION_TENSOR_CORE_ROTATION, args.tc_rotation)
-    if args.gridded >= 0:
-        ctx.set_option(_abi.LEAP_OPTION_GRIDDED_ROTATION, args.gridded)
-    # A dedicated stream: the calls and the timing events go on the same (non-null) stream.
-    bstream = torch.cuda.Stream(device=f"cuda:{local}")
-    torch.cuda.set_stream(bstream)
-    if args.workload == "batched":
-        w = setup_batched(args, ctx, lg, torch, local, rank)
-    elif args.workload == "differentiable":
-        w = setup_differentiable(args, ctx, lg, torch, local, rank)
-    else:
-        w = setup_single(args, ctx, lg, torch, local, rank, args.workload)
-    prec = lg.LEAP_PRECISION_MIXED if args.precision == "mixed" else lg.LEAP_PRECISION_FP64
-    lib = _abi.lib
-
-    def timed(p, steps, warmup):
+    def timed(self, w: Workload, p: int, steps: int, warmup: int):
+        """W untimed steps, then exactly `steps` steps between barriers and synchronisations;
+        CUDA events on the launching stream (or the library's own events on its stream for
+        blocking batched calls); max over ranks."""
+        torch, dist = self.torch, self.dist
+        from leap_gb300 import _abi
+        lib = _abi.lib
         for _ in range(warmup):
             w.step(p)
         torch.cuda.synchronize()
@@ -531,7 +610,7 @@ def run_gpu(args, rank: int, world: int):
             dist.barrier()
         torch.cuda.synchronize()
         e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-        lib.leap_timing_reset(ctx.handle)
+        lib.leap_timing_reset(self.ctx.handle)
         e0.record()
         for _ in range(steps):
             w.step(p)
@@ -539,188 +618,306 @@ def run_gpu(args, rank: int, world: int):
         torch.cuda.synchronize()
         ms = e0.elapsed_time(e1) / steps
         t = _abi.LeapTimings()
-        ctx._check(lib.leap_get_timings(ctx.handle, t))
-        if w.kernel_timing == "total":
-            # blocking host calls: the device time of each call, from its own events
-            ms = t.total_ms / max(1, t.calls)
+        self.ctx._check(lib.leap_get_timings(self.ctx.handle, t))
+        if w.timing == "library":
+            ms = t.total_ms / max(1, t.calls)  # blocking calls on the library's stream: its own events
         if dist:
-            tt = torch.tensor([ms], device=f"cuda:{local}")
+            tt = torch.tensor([ms], device=self.dev)
             dist.all_reduce(tt, op=dist.ReduceOp.MAX)
             dist.barrier()
             ms = float(tt.item())
         return ms, t
 
-    with ClockSampler(local) as clk:
-        ms, tim = timed(prec, args.steps, args.warmup)
-    clocks = clk.summary()
-    value = w.units * world / (ms / 1e3)
-    cal_main = w.result()
-    gpu_launches = (int(tim.kernels) + getattr(w, "extra_launches", 0)) * args.steps
+    def close(self):
+        self.ctx.close()
+        self.torch.cuda.synchronize()
+        self.torch.cuda.empty_cache()
 
-    # The rotate + average kernel this run used (the library's choice for LEAP_OPTION_GRIDDED_ROTATION).
-    gridded = prec == lg.LEAP_PRECISION_MIXED and (
-        args.gridded == 1 or (args.gridded in (-1, 2) and args.tc_rotation != 2 and w.min_ndir >= 32))
-    alt_kernel = None
-    if gridded and args.gridded != 1 and args.workload in ("mwa", "ska_low"):
-        # The same call through the FP32 CUDA-core pipelined kernel, for comparison.
-        ctx.set_option(_abi.LEAP_OPTION_GRIDDED_ROTATION, 0)
-        ms_alt, _ = timed(prec, max(1, min(args.steps, 5)), 2)
-        cal_alt = w.result()
-        ctx.set_option(_abi.LEAP_OPTION_GRIDDED_ROTATION, 2)
-        alt_kernel = {"kernel": "rotate_average_mixed_pipe (FP32 CUDA cores, compensated sums)", "ms_per_step": ms_alt,
-                      "value": w.units * world / (ms_alt / 1e3),
-                      "max_cal_diff_vs_gridded_rad": wrapped_max_diff(cal_main, cal_alt)}
 
-    checks = {}
-    plain = None
-    if not args.skip_plain and prec == lg.LEAP_PRECISION_MIXED:
-        ms64, _ = timed(lg.LEAP_PRECISION_FP64, max(1, min(args.steps, 3)), 1)
-        cal64 = w.result()
-        per_dir = np.abs(np.angle(np.exp(1j * (cal_main - cal64)))).max(axis=1)
-        margin = branch_margins(ctx, w.md, w.D, torch, f"cuda:{local}", torch.cuda.current_stream().cuda_stream)
-        near = margin < 1e-5
-        plain = {"value": w.units * world / (ms64 / 1e3), "ms_per_step": ms64, "dtype": "f64",
-                 "mixed_vs_fp64_max_cal_err_rad": float(per_dir[~near].max()) if (~near).any() else None,
-                 "mixed_vs_fp64_cal_err_rad_median_p99": ([float(np.median(per_dir[~near])),
-                                                           float(np.percentile(per_dir[~near], 99))]
-                                                          if (~near).any() else None),
-                 "directions_near_branch_cut": int(near.sum()),
-                 "max_cal_err_rad_incl_branch_cut_directions": float(per_dir.max()),
-                 "speedup_mixed_over_fp64": ms64 / ms,
-                 "note": "directions whose FP64 solve has an arg() within 1e-5 rad of +-pi are counted apart: "
-                         "the mixed form may put that angle on the other branch, which moves cal by 2*pi "
-                         "times one column of Ad"}
+def kernel_time(run: Run, w: Workload, p: int, ms: float, tim) -> float:
+    """Event-timed duration of the rotate + average stage (the bulk kernel and the small kernels
+    launched with it on the same stream) per call."""
+    from leap_gb300 import _abi
+    if getattr(w, "whole_step_is_kernel", False):
+        return ms
+    if w.timing == "library":
+        # Graph replays record no event between the stages: time eager calls of the same launches.
+        run.ctx.set_option(_abi.LEAP_OPTION_GRAPH_REPLAY, 0)
+        try:
+            _, t = run.timed(w, p, 5, 1)
+        finally:
+            run.ctx.set_option(_abi.LEAP_OPTION_GRAPH_REPLAY, 1)
+        return t.rotate_ms / max(1, t.calls)
+    return tim.rotate_ms / max(1, tim.calls)
 
-    if rank == 0 and getattr(w, "spot", None) is not None and not args.skip_cpu:
-        # Full-size spot check: the smallest chunk's directions against the oracle.
-        sys.path.insert(0, os.path.join(ROOT, "oracle"))
-        import oracle
-        slot, obs_s, vis_s = w.spot
-        sl, d0, nd = next(it for it in w.items if it[0] == slot)
-        exp = oracle.calibrate_interval(vis_s, obs_s.uvw, w.dds[d0:d0 + nd], oracle.metadata(obs_s),
-                                        nthreads=oracle.max_threads())
-        checks["oracle_chunk"] = {"slot": slot, "timesteps": obs_s.timesteps, "channels": obs_s.channels,
-                                  "directions": nd, "max_cal_err_rad": wrapped_max_diff(cal_main[d0:d0 + nd], exp)}
 
-    e2e = None
-    if w.e2e_step is not None:
-        for _ in range(max(1, min(args.warmup, 2))):
-            w.e2e_step()
+def roofline(w: Workload, k_ms: float, gridded: bool, peaks) -> dict:
+    peak = peaks["hbm_gbs"] if peaks else 6800.0
+    achieved = w.kernel_bytes / (k_ms / 1e3) / 1e9
+    roof = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+            "traffic": w.traffic, "kernel": w.kernel_name, "kernel_ms": k_ms,
+            "algorithmic_bytes_per_launch": w.kernel_bytes,
+            "algorithmic_bytes": "each complex<float> sample read once (8 B), the split UVWs (24 B per row), one "
+                                 "FP64 avgData write per (baseline, pol, direction)",
+            "peak_source": "MEASURED_PEAKS.json hbm_gbs (of measured)" if peaks else "fallback 6.8 TB/s (of fallback)",
+            "per_direction_convention": {
+                "bytes": w.per_direction_bytes, "frac": w.per_direction_bytes / (k_ms / 1e3) / 1e9 / peak,
+                "note": "the reference's per-direction loop reads the cube once per direction; this kernel reads it "
+                        "once for all directions, so this figure is not a roofline fraction"}}
+    if gridded and w.grid is not None:
+        flops, mean_pass, max_pass = w.grid
+        tf32_peak = (peaks["bf16_tflops"] / 2 if peaks and "bf16_tflops" in peaks else 950.0) * 1e12
+        roof["tensor"] = {"tf32_flops_per_s": flops / (k_ms / 1e3), "peak_flops_per_s": tf32_peak,
+                          "frac": flops / (k_ms / 1e3) / tf32_peak, "mma_flops_per_call": flops,
+                          "grid_passes_per_tile_mean": mean_pass, "grid_passes_max": max_pass,
+                          "peak_source": "half of MEASURED_PEAKS.json bf16_tflops (TF32 rate, of measured)" if peaks
+                          else "half of the 1.9 PFLOP/s bf16 fallback (of fallback)"}
+    if roof["traffic"]:
+        roof["dram_traffic_frac"] = roof["traffic"] / (k_ms / 1e3) / 1e9 / peak
+    return roof
+
+
+def uses_gridded(args, w, p, lg) -> bool:
+    return p == lg.LEAP_PRECISION_MIXED and (args.gridded == 1 or (
+        args.gridded in (-1, 2) and args.tc_rotation != 2 and w.min_ndir >= 32))
+
+
+def time_e2e(run: Run, w: Workload, steps: int):
+    torch, dist = run.torch, run.dist
+    for _ in range(2):
+        w.e2e_step()
+    if dist:
+        dist.barrier()
+    t0 = time.perf_counter()
+    for _ in range(steps):
+        w.e2e_step()
+    e2e_s = (time.perf_counter() - t0) / steps
+    if dist:
+        tt = torch.tensor([e2e_s], device=run.dev)
+        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
+        e2e_s = float(tt.item())
+    e2e = {"value": w.units * run.world / e2e_s, "unit": "vis-directions/s", "h2d_bytes_per_step": int(w.h2d),
+           "d2h_bytes_per_step": int(w.d2h), "ms_per_step": e2e_s * 1e3, "steps": steps, "mode": w.e2e_mode}
+    pipe = getattr(w, "e2e_pipelined", None)
+    if pipe is not None:
+        pipe(2)
         if dist:
             dist.barrier()
-        e2e_steps = args.steps if args.workload == "mwa" else max(1, min(args.steps, 3))
         t0 = time.perf_counter()
-        for _ in range(e2e_steps):
-            w.e2e_step()
-        e2e_s = (time.perf_counter() - t0) / e2e_steps
-        if dist:
-            tt = torch.tensor([e2e_s], device=f"cuda:{local}")
-            dist.all_reduce(tt, op=dist.ReduceOp.MAX)
-            e2e_s = float(tt.item())
-        e2e = {"value": w.units * world / e2e_s, "unit": "vis-directions/s", "h2d_bytes_per_step": int(w.h2d),
-               "d2h_bytes_per_step": int(w.d2h), "ms_per_step": e2e_s * 1e3, "steps": e2e_steps,
-               "mode": "serial: upload, then calibrate, each step"}
-        pipe = getattr(w, "e2e_pipelined", None)
-        if pipe is not None:
-            pipe(2)
-            if dist:
-                dist.barrier()
-            t0 = time.perf_counter()
-            pipe(e2e_steps)
-            pl_s = (time.perf_counter() - t0) / e2e_steps
-            if dist:
-                tt = torch.tensor([pl_s], device=f"cuda:{local}")
-                dist.all_reduce(tt, op=dist.ReduceOp.MAX)
-                pl_s = float(tt.item())
-            e2e["serial"] = {"value": e2e["value"], "ms_per_step": e2e["ms_per_step"]}
-            e2e.update({"value": w.units * world / pl_s, "ms_per_step": pl_s * 1e3,
-                        "mode": "double-buffered: step k+1's upload overlaps step k's calibration; every step moves "
-                                "its full input (host -> device) and result (device -> host)"})
-        alt = getattr(w, "e2e_alt", None)
-        if alt is not None:
-            name, fn = alt
-            fn()
-            t0 = time.perf_counter()
-            for _ in range(e2e_steps):
-                fn()
-            e2e[name] = {"value": w.units * world / ((time.perf_counter() - t0) / e2e_steps),
-                         "ms_per_step": (time.perf_counter() - t0) / e2e_steps * 1e3}
+        pipe(steps)
+        pl_s = (time.perf_counter() - t0) / steps
+        e2e["serial"] = {"value": e2e["value"], "ms_per_step": e2e["ms_per_step"]}
+        e2e.update({"value": w.units * run.world / pl_s, "ms_per_step": pl_s * 1e3,
+                    "mode": "double-buffered: step k+1's upload overlaps step k's calibration; every step moves "
+                            "its full input (host -> device) and result (device -> host)"})
+    return e2e
 
-    peaks = _peaks()
-    peak = peaks["hbm_gbs"] if peaks else 6800.0
-    if w.kernel_timing == "rotate":
-        k_ms = tim.rotate_ms / max(1, tim.calls)
-        k_name = ("rotate_average (mixed: gridded kernel, 3xTF32 tcgen05 grid product + 10-point interpolation per "
-                  "direction; compensated reference-antenna pass)" if gridded else
-                  "rotate_average (mixed: persistent TMA-pipelined kernel + compensated reference-antenna pass)")
-    elif w.kernel_timing == "events":
-        k_ms = ms
-        k_name = "whole forward + backward step"
+
+def run_workload(name, args, torch, lg, local, rank, world, dist, steps, warmup, headline=False):
+    """Time one workload and measure everything reported about it."""
+    from leap_gb300.sharding import shard_range
+    run = Run(args, torch, lg, local, rank, world, dist)
+    bstream = torch.cuda.Stream(device=run.dev)  # calls and timing events on one non-null stream
+    torch.cuda.set_stream(bstream)
+    dir_ids = None
+    if world > 1:
+        # Weak scaling: the direction set grows with the ranks; each rank takes its shard.
+        per = args.directions or {"batched": 256, "mwa": 64, "ska_low": 128}.get(name, 16)
+        dir_ids = np.asarray(shard_range(per * world, world, rank))
+    if name == "batched":
+        w = setup_batched(run, dir_ids)
+    elif name == "differentiable":
+        w = setup_differentiable(run)
     else:
-        k_ms = ms
-        k_name = "whole batched call (graph replay)"
-    achieved = w.b_alg / (k_ms / 1e3) / 1e9
-    roof = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
-            "traffic": w.traffic, "kernel": k_name, "kernel_ms": k_ms,
-            "peak_source": "MEASURED_PEAKS.json hbm_gbs (of measured)" if peaks else "fallback 6.8 TB/s (of fallback)",
-            "note": "B_alg counts the visibilities once per direction; the kernel reads them once for all directions",
-            "compute": {"fp32_issue_per_s": w.f_alg / (k_ms / 1e3), "fp32_peak_fma_per_s": 3.6e13,
-                        "frac": w.f_alg / (k_ms / 1e3) / 3.6e13}}
-    if gridded and getattr(w, "grid_flops", None):
-        # Tensor pipe: the kernel's 3xTF32 MMA FLOPs (from its grid windows) against the TF32
-        # rate, half the measured dense BF16 rate.
-        tf32_peak = (peaks["bf16_tflops"] / 2 if peaks and "bf16_tflops" in peaks else 950.0) * 1e12
-        roof["compute"] = {"tensor_tf32_flops_per_s": w.grid_flops / (k_ms / 1e3), "tf32_peak_flops_per_s": tf32_peak,
-                           "frac": w.grid_flops / (k_ms / 1e3) / tf32_peak, "mma_flops_per_call": w.grid_flops,
-                           "peak_source": "half of MEASURED_PEAKS.json bf16_tflops (of measured)" if peaks else
-                                          "half of the 1.9 PFLOP/s bf16 fallback (of fallback)"}
-        roof["note"] = ("B_alg counts the visibilities once per direction (the reference's per-direction loop); the "
-                        "gridded kernel reads them once for all directions (hbm_read_once_frac)")
-    if hasattr(w, "vis_bytes_resident"):
-        roof["hbm_read_once_frac"] = w.vis_bytes_resident / (k_ms / 1e3) / 1e9 / peak
-    if gridded and getattr(w, "grid_traffic", None):
-        roof["traffic"] = w.grid_traffic
-    elif gridded:
-        roof["traffic"] = None
-    if roof["traffic"]:
-        # the DRAM bytes the kernel actually moves (ncu-measured traffic) over its event time
-        roof["dram_traffic_frac"] = roof["traffic"] / (k_ms / 1e3) / 1e9 / peak
+        w = setup_single(run, name, dir_ids)
+    prec = lg.LEAP_PRECISION_MIXED if args.precision == "mixed" else lg.LEAP_PRECISION_FP64
+    with ClockSampler(local) as clk:
+        ms, tim = run.timed(w, prec, steps, warmup)
+    out = {"ms_per_step": ms, "value": w.units * world / (ms / 1e3), "clocks": clk.summary(),
+           "gpu_launches": (int(tim.kernels) + w.extra_launches) * steps, "config": workload_config(name, args)}
+    cal_main = w.result()
+    gridded = uses_gridded(args, w, prec, lg)
+    if gridded and name in ("mwa", "ska_low"):
+        w.kernel_name = ("rotate_average_gridded<7> (3xTF32 tcgen05 grid product + 8-point interpolation per "
+                         "direction) + grid_windows + the compensated reference-antenna pass")
+        w.traffic = getattr(w, "grid_traffic", None)
+    elif name in ("mwa", "ska_low"):
+        w.kernel_name = "rotate_average_mixed_pipe (persistent, TMA-pipelined, FP32 CUDA cores, compensated sums)"
+        w.traffic = getattr(w, "pipe_traffic", None)
+    if not gridded:
+        w.grid = None
+    k_ms = kernel_time(run, w, prec, ms, tim)
+    out["roofline"] = roofline(w, k_ms, gridded, _peaks())
+    if gridded and args.gridded != 1 and name in ("mwa", "ska_low"):
+        # The same call through the FP32 CUDA-core pipelined kernel, for comparison.
+        from leap_gb300 import _abi
+        run.ctx.set_option(_abi.LEAP_OPTION_GRIDDED_ROTATION, 0)
+        ms_alt, t_alt = run.timed(w, prec, max(1, min(steps, 5)), 2)
+        cal_alt = w.result()
+        run.ctx.set_option(_abi.LEAP_OPTION_GRIDDED_ROTATION, 2)
+        out["alternative_kernel"] = {
+            "kernel": "rotate_average_mixed_pipe (FP32 CUDA cores, compensated sums)", "ms_per_step": ms_alt,
+            "kernel_ms": t_alt.rotate_ms / max(1, t_alt.calls), "value": w.units * world / (ms_alt / 1e3),
+            "max_cal_diff_vs_gridded_rad": float(np.abs(cal_main - cal_alt).max())}
+    cal64 = None
+    if not args.skip_plain and prec == lg.LEAP_PRECISION_MIXED:
+        n64 = 1 if name == "ska_low" else max(1, min(steps, 3))
+        ms64, _ = run.timed(w, lg.LEAP_PRECISION_FP64, n64, 1)
+        cal64 = w.result()
+        per_dir = np.abs(cal_main - cal64).max(axis=1)
+        out["plain_fp64"] = {"value": w.units * world / (ms64 / 1e3), "ms_per_step": ms64, "dtype": "f64",
+                             "speedup_mixed_over_fp64": ms64 / ms,
+                             "mixed_vs_fp64_cal_rad": {"max": float(per_dir.max()),
+                                                       "median": float(np.median(per_dir)),
+                                                       "p99": float(np.percentile(per_dir, 99))}}
+    if rank == 0 and not args.skip_checks and w.checks is not None:
+        out["checks"] = w.checks(cal_main, cal64, _oracle().max_threads())
+    if w.e2e_step is not None:
+        out["e2e"] = time_e2e(run, w, max(1, min(steps, 3)) if name == "batched" else steps)
+    if world > 1:
+        from leap_gb300.sharding import calibrate_sharded
+        holder = {}
 
+        def cal_fn(part):
+            t0 = time.perf_counter()
+            w.step(prec)
+            r = w.result()
+            holder["cal_s"] = time.perf_counter() - t0
+            return r
+
+        t0 = time.perf_counter()
+        gathered = calibrate_sharded(cal_fn, np.zeros((per * world, 3, 3)), w.S)
+        total = time.perf_counter() - t0
+        out["sharding"] = {"directions_total": per * world, "directions_per_rank": len(dir_ids),
+                           "gather_s": total - holder.get("cal_s", 0.0),
+                           "gathered_rows": None if gathered is None else int(gathered.shape[0])}
+    out["metadata_build_s"] = round(getattr(w, "metadata_s", 0.0), 3)
+    w.close()
+    del w
+    run.close()
+    return out
+
+
+def run_reference_directions(args, torch, lg, local):
+    """The reference's own direction spread (E2EPerformanceTests.cc:65-76: nine directions up
+    to ~1 rad from the phase centre of its MWA test set) on the 128-antenna array, 14 timesteps,
+    384 channels: the gridded kernel (forced on) and the pipelined kernel against the oracle."""
+    from leap_gb300 import synth, _abi
+    kats = json.load(open(os.path.join(ROOT, "tests", "golden", "reference_kats.json")))
+    pc = tuple(kats["dd"]["phase_centre"])
+    dirs = np.asarray(kats["e2e_directions"]["radec"], dtype=np.float64)
+    obs = synth.mwa_at_phase_centre(pc, timesteps=args.timesteps or 14, channels=args.channels)
+    ctx = lg.Context(local)
+    md = ctx.build_metadata(obs)
+    ctx.set_integration(0, obs.vis, obs.uvw)
+    dds = np.stack([lg.dd_matrix(md.phase_centre_ra_rad, md.phase_centre_dec_rad, r, d) for r, d in dirs])
+    out = {"source": kats["e2e_directions"]["source"], "phase_centre": list(pc), "directions": int(len(dirs)),
+           "workload": f"128ant/8256bl/{obs.timesteps}t/{obs.channels}ch/4pol complex<float>"}
+    flops, mean_pass, max_pass = grid_windows_host(obs, dds)
+    cals = {}
+    for label, opt in (("gridded", 1), ("pipelined", 0)):
+        ctx.set_option(_abi.LEAP_OPTION_GRIDDED_ROTATION, opt)
+        ctx.calibrate(0, dds, lg.LEAP_PRECISION_MIXED)
+        ctx.timing_reset()
+        for _ in range(5):
+            cals[label] = ctx.calibrate(0, dds, lg.LEAP_PRECISION_MIXED)
+        t = ctx.timings()
+        out[label] = {"ms_per_call": t["total_ms"] / t["calls"], "kernel_ms": t["rotate_ms"] / t["calls"]}
+    out["gridded"].update({"grid_passes_per_tile_mean": mean_pass, "grid_passes_max": max_pass,
+                           "mma_flops_per_call": flops})
+    cal64 = ctx.calibrate(0, dds, lg.LEAP_PRECISION_FP64)
+    ctx.close()
+    oracle = _oracle()
+    mdo = oracle.metadata(obs)
+    (cal_o,), (avg_o,) = oracle.calibrate_items([(obs.vis, obs.uvw, dds)], mdo, return_avg=True)
+    for label in ("gridded", "pipelined"):
+        out[label]["vs_oracle"] = compare_with_oracle(cals[label], cal_o, avg_o, mdo, MIXED_TOL, BRANCH_MARGIN)
+    out["fp64_vs_oracle"] = compare_with_oracle(cal64, cal_o, avg_o, mdo, FP64_TOL, 1e-8)
+    return out
+
+
+def run_dropin(args):
+    """The C++ drop-in call, LeapCalibratorFactory::Create(gb300)->Calibrate, on the 128-antenna
+    14-timestep workload written as a .leapms file: Slice(1) (one solution per timestep) and
+    Slice(-1) (one solution for all), mixed form, 64 directions."""
+    from leap_gb300 import synth
+    import leap_gb300 as lg
+    exe = os.path.join(os.path.dirname(lg.LIB_PATH), "leap_dropin_bench")
+    obs, dirs = synth.mwa_precision(timesteps=args.timesteps or 14, channels=args.channels,
+                                    directions=args.directions or 64)
+    out = {"call": "LeapCalibratorFactory::Create(ComputeImplementation::gb300)->Calibrate(ms, directions, slice, "
+                   "0.0, nullopt, false), mixed form",
+           "workload": f"128ant/8256bl/{obs.timesteps}t/{obs.channels}ch/4pol/{len(dirs)}dir complex<float>, "
+                       "MeasurementSet stand-in in host memory"}
+    with tempfile.TemporaryDirectory() as tmp:
+        path = os.path.join(tmp, "mwa.leapms")
+        synth.write_leapms(obs, path)
+        units = 4.0 * obs.rows * obs.channels * len(dirs)
+        for label, s in (("slice_1", "1"), ("slice_all", "-1")):
+            r = subprocess.run([exe, "-f", path, "-d", json.dumps(dirs.tolist()), "-s", s, "-p", "mixed",
+                                "--warmup", "2", "--repeat", "5"], capture_output=True, text=True, timeout=900)
+            if r.returncode != 0:
+                raise RuntimeError(f"leap_dropin_bench failed: {r.stderr}")
+            res = json.loads(r.stdout.strip().splitlines()[-1])
+            ms = statistics.median(res["ms_per_call"])
+            out[label] = {"ms_per_call_median": ms, "ms_per_call": res["ms_per_call"], "solutions": res["solutions"],
+                          "value": units / (ms / 1e3), "unit": "vis-directions/s",
+                          "h2d_bytes_per_call": res["visibility_bytes"]}
+    return out
+
+
+def run_gpu(args, rank: int, world: int):
+    import torch
+    import leap_gb300 as lg
+
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(local)
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+    headline = "batched" if args.workload == "all" else args.workload
+    head = run_workload(headline, args, torch, lg, local, rank, world, dist, args.steps, args.warmup, headline=True)
+    subs = {}
+    if args.workload == "all" and world == 1 and not args.skip_sub:
+        saved = (args.directions, args.timesteps)
+        args.directions, args.timesteps = 0, 0
+        for name in ("mwa", "ska_low"):
+            subs[name] = run_workload(name, args, torch, lg, local, rank, world, dist, max(3, min(args.steps, 10)), 3)
+        subs["reference_directions"] = run_reference_directions(args, torch, lg, local)
+        subs["dropin"] = run_dropin(args)
+        args.directions, args.timesteps = saved
     cpu = None
     if rank == 0 and world == 1 and not args.skip_cpu:
-        sys.path.insert(0, os.path.join(ROOT, "oracle"))
-        import oracle
+        oracle = _oracle()
         thr = oracle.max_threads()
-        c_obs, c_dirs, c_vis = w.cpu_case
-        v, samp = bench_cpu(c_obs, c_dirs, c_vis, thr, args.cpu_budget)
-        v1, samp1 = bench_cpu(c_obs, c_dirs, c_vis, 1, args.cpu_budget / 5)
+        sample = cpu_sample(headline, args)
+        v, runs, secs = time_cpu_sample(sample, thr, args.cpu_budget)
+        v1, runs1, secs1 = time_cpu_sample(sample, 1, args.cpu_budget / 5) if headline != "batched" else (None, 0, 0)
         cpu = {"value": v, "unit": "vis-directions/s", "cores": thr, "kind": "port",
-               "sample": f"1 timestep ({c_obs.nbaselines} baselines x {c_obs.channels} channels) x "
-                         f"{samp['directions']} of {w.D} directions, {samp['runs']} runs, {samp['seconds']:.1f} s",
-               "single_core": {"value": v1, "cores": 1,
-                               "sample": f"1 timestep x {samp1['directions']} directions, {samp1['runs']} runs, "
-                                         f"{samp1['seconds']:.1f} s"}}
-
+               "sample": f"{sample.description} ({sample.units:.3g} vis-directions), {runs} runs, {secs:.1f} s"}
+        if v1:
+            cpu["single_core"] = {"value": v1, "cores": 1, "sample": f"same, {runs1} runs, {secs1:.1f} s"}
     if rank == 0:
+        prec_mixed = args.precision == "mixed"
         line = {
-            "metric": "vis-directions/s", "value": value, "unit": "vis-directions/s", "n_gpus": world,
-            "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True,
+            "metric": "vis-directions/s", "value": head["value"], "unit": "vis-directions/s", "n_gpus": world,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": head["ms_per_step"], "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None,
-            "dtype": "f32 rotation + f64 phase arguments" if prec else "f64", "data": "synthetic",
-            "config": w.config,
-            "e2e": e2e,
-            "gpu_launches": gpu_launches,
-            "roofline": roof,
+            "dtype": "f32 rotation + f64 phase arguments" if prec_mixed else "f64", "data": "synthetic",
+            "config": head["config"],
+            "e2e": head.get("e2e"),
+            "gpu_launches": head["gpu_launches"],
+            "roofline": head["roofline"],
             "cpu_baseline": cpu,
-            "plain_fp64": plain,
-            "checks": checks or None,
-            "alternative_kernel": alt_kernel,
-            "metadata_build_s": round(getattr(w, "metadata_s", 0.0), 3),
-            "metadata_build": "leap_build_metadata (device pseudo-inverse) + host copies of A and Ad for the checks",
-            "clocks": clocks,
+            "plain_fp64": head.get("plain_fp64"),
+            "checks": head.get("checks"),
+            "sharding": head.get("sharding"),
+            "metadata_build_s": head["metadata_build_s"],
+            "sub_results": subs or None,
+            "clocks": head["clocks"],
         }
         print(json.dumps(line), flush=True)
-    ctx.close()
     if dist:
         dist.destroy_process_group()
 
@@ -732,9 +929,9 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--precision", default="mixed", choices=["mixed", "fp64"])
-    ap.add_argument("--workload", default="mwa", choices=["mwa", "batched", "ska_low", "differentiable"],
-                    help="mwa: 128 antennas, 14 t, 384 ch, 64 directions (default); batched: 32 uneven chunks, "
-                         "256 directions; ska_low: 512 stations, 16 t, 384 ch, 128 directions")
+    ap.add_argument("--workload", default="all", choices=["all", "batched", "mwa", "ska_low", "differentiable"],
+                    help="all (default): the batched workload as the headline, with the 128-antenna, SKA-Low, "
+                         "reference-direction and drop-in results beside it; otherwise that workload alone")
     ap.add_argument("--timesteps", type=int, default=0, help="0: the workload's own count (MWA 14, SKA-Low 16)")
     ap.add_argument("--channels", type=int, default=384)
     ap.add_argument("--directions", type=int, default=0, help="0: the workload's own count")
@@ -747,21 +944,21 @@ def main():
     ap.add_argument("--cpu-budget", type=float, default=15.0)
     ap.add_argument("--skip-cpu", action="store_true")
     ap.add_argument("--skip-plain", action="store_true")
+    ap.add_argument("--skip-checks", action="store_true", help="no oracle comparison")
+    ap.add_argument("--skip-sub", action="store_true", help="headline only")
     args = ap.parse_args()
-    if args.directions == 0 and args.workload == "mwa":
-        args.directions = 64
     if args.e2e < 0:
-        args.e2e = 1 if args.workload == "mwa" else 0
+        args.e2e = 1 if args.workload in ("all", "batched", "mwa") else 0
     rank = int(os.environ.get("RANK", "0"))
     world = int(os.environ.get("WORLD_SIZE", "1"))
+    headline = "batched" if args.workload == "all" else args.workload
     if args.impl == "reference":
-        run_reference(args, rank, world)
-    else:
-        if not os.path.exists(os.path.join(PKG, "leap_gb300", "_lib", "libleap_gb300.so")):
-            sys.path.insert(0, PKG)
-            import build as _b
-            _b.build()
-        run_gpu(args, rank, world)
+        run_reference(args, headline, rank, world)
+        return
+    if not os.path.exists(os.path.join(PKG, "leap_gb300", "_lib", "libleap_gb300.so")):
+        import build as _b
+        _b.build()
+    run_gpu(args, rank, world)
 
 
 if __name__ == "__main__":

@@ -111,11 +111,15 @@ def build(verbose: bool = False, force: bool = False) -> str:
         _run([nvcc, *ARCH, "-shared", "-o", LIB, *objs, "-lcudart"])
     if force or _newer(SYNTH_LIB, [synth_obj]):
         _run([nvcc, *ARCH, "-shared", "-o", SYNTH_LIB, synth_obj, "-lcudart"])
-    driver_src = os.path.join(CPP, "tools", "leap_calibrate_driver.cc")
-    driver = os.path.join(OUT_DIR, "leap_calibrate_driver")
-    if os.path.exists(driver_src) and (force or _newer(driver, [driver_src, LIB] + headers)):
-        _run(["g++", "-O2", "-std=c++17", *inc, driver_src, "-o", driver, "-L", OUT_DIR, "-lleap_gb300",
-              "-Wl,-rpath,$ORIGIN"])
+    tools = []
+    for name in ("leap_calibrate_driver", "leap_dropin_bench"):
+        src = os.path.join(CPP, "tools", name + ".cc")
+        exe = os.path.join(OUT_DIR, name)
+        if os.path.exists(src) and (force or _newer(exe, [src, LIB] + headers)):
+            tools.append(["g++", "-O2", "-std=c++17", *inc, src, "-o", exe, "-L", OUT_DIR, "-lleap_gb300",
+                          "-Wl,-rpath,$ORIGIN"])
+    with cf.ThreadPoolExecutor(max_workers=2) as ex:
+        list(ex.map(_run, tools))
     return LIB
 
 

@@ -59,28 +59,48 @@ cpu::CalibrationCollection GpuLeapCalibrator::Calibrate(const MeasurementSet& ms
   }
   const uint32_t nbl = ms.GetNumBaselines();
   const uint32_t C = ms.GetNumChannels(), P = ms.GetNumPols();
-  std::vector<cpu::Calibration> output;
+  const int32_t visType = ms.HasFloatData() ? LEAP_VIS_C64 : LEAP_VIS_C128;
   const int solutions = interval.GetSize();
-  for (int s = 0; s < solutions; ++s) {
-    output.emplace_back(epochs[static_cast<size_t>(s) * interval.interval],
-                        epochs[static_cast<size_t>(s + 1) * interval.interval - 1]);
+  // Solution intervals go up double-buffered: interval s + 1 is queued on the library's copy
+  // stream (slot (s + 1) % 2) while interval s calibrates, as the reference's loop would if it
+  // overlapped its per-interval uploads (CudaLeapCalibrator.cu:159-227).  The transpose from
+  // MeasurementSet order runs on the device; the UVWs of an interval stay alive in uvw[slot]
+  // until the call that reads the slot has returned.  A library that cannot queue an upload from
+  // this memory (pageable memory on a device that does not read it in place) takes each interval
+  // synchronously instead.
+  std::vector<double> uvw[2];
+  bool overlap = solutions > 1;
+  auto upload = [&](int s, int slot, bool async) -> int32_t {
     // Integration start row ignores Slice.start, as the reference does (CpuLeapCalibrator.cc:116).
     const uint32_t startRow = static_cast<uint32_t>(s) * interval.interval * nbl;
     const uint32_t rows = static_cast<uint32_t>(interval.interval) * nbl;
-    const std::vector<double> uvw = ms.GetCoords(startRow, rows);
-    // The interval's rows go up in MeasurementSet order; the device transposes them
-    // (the reference's host-side GetVis transpose, LA/ms/MeasurementSet.h:95-204).
-    check(leap_set_integration_ms(m_ctx, 0, ms.HasFloatData() ? LEAP_VIS_C64 : LEAP_VIS_C128, ms.GetRawVis(startRow), C,
-                                  0, uvw.data(), rows, C, P, LEAP_MEMORY_HOST),
-          m_ctx, "leap_set_integration_ms");
-    std::vector<double> cal(static_cast<size_t>(S) * directions.size());
-    check(leap_calibrate(m_ctx, 0, dd.data(), static_cast<int32_t>(directions.size()), m_options.precision, cal.data()),
+    uvw[slot] = ms.GetCoords(startRow, rows);
+    return (async ? leap_set_integration_ms_async : leap_set_integration_ms)(
+        m_ctx, slot, visType, ms.GetRawVis(startRow), C, 0, uvw[slot].data(), rows, C, P, LEAP_MEMORY_HOST);
+  };
+  if (overlap) {
+    const int32_t rc = upload(0, 0, true);
+    if (rc == LEAP_ERR_INVALID_ARGUMENT) overlap = false;
+    else check(rc, m_ctx, "leap_set_integration_ms_async");
+  }
+  std::vector<cpu::Calibration> output;
+  std::vector<double> cal(static_cast<size_t>(S) * directions.size());
+  for (int s = 0; s < solutions; ++s) {
+    output.emplace_back(epochs[static_cast<size_t>(s) * interval.interval],
+                        epochs[static_cast<size_t>(s + 1) * interval.interval - 1]);
+    const int slot = overlap ? s % 2 : 0;
+    if (!overlap) check(upload(s, 0, false), m_ctx, "leap_set_integration_ms");
+    // The next interval's slot was last read by calibration s - 1, which has returned.
+    if (overlap && s + 1 < solutions) check(upload(s + 1, (s + 1) % 2, true), m_ctx, "leap_set_integration_ms_async");
+    check(leap_calibrate(m_ctx, slot, dd.data(), static_cast<int32_t>(directions.size()), m_options.precision,
+                         cal.data()),
           m_ctx, "leap_calibrate");
     for (size_t i = 0; i < directions.size(); ++i)
       output.back().GetBeamCalibrations().emplace_back(
           directions[i], std::vector<double>(cal.begin() + static_cast<std::ptrdiff_t>(S * i),
                                              cal.begin() + static_cast<std::ptrdiff_t>(S * (i + 1))));
   }
+  if (overlap && solutions > 1) leap_release_integration(m_ctx, 1);
   leap_release_integration(m_ctx, 0);
   return cpu::CalibrationCollection(std::move(output));
 }

@@ -327,9 +327,10 @@ void grid_table(int32_t C, int32_t taps, double beta, int32_t lbase, int32_t row
       for (int ri = 0; ri < 2; ++ri) {
         const float hi = round_tf32(static_cast<float>(v[ri]));
         const float lo = round_tf32(static_cast<float>(v[ri] - static_cast<double>(hi)));
+        const int rr = 2 * r + ri;  // re and im rows of a grid point are neighbours
         for (int hl = 0; hl < 2; ++hl) {
-          const size_t base = ((static_cast<size_t>((q * 2 + ks) * 2 + hl) * 2 + ri) * nrg + (r >> 3)) * 64;
-          out[base + ((kk >> 2) & 1) * 32 + (r & 7) * 4 + (kk & 3)] = hl == 0 ? hi : lo;
+          const size_t base = (static_cast<size_t>((q * 2 + ks) * 2 + hl) * 2 * nrg + (rr >> 3)) * 64;
+          out[base + ((kk >> 2) & 1) * 32 + (rr & 7) * 4 + (kk & 3)] = hl == 0 ? hi : lo;
         }
       }
     }

@@ -14,10 +14,11 @@
 // over the W grid points nearest n B, with psi the "exponential of semicircle"
 // kernel psi(x) = exp(beta (sqrt(1 - (2x/W)^2) - 1)) and Psi its Fourier
 // transform at frequency k / n (Barnett, Magland & af Klinteberg, SIAM J. Sci.
-// Comput. 41 (2019) C479).  With W = 10, beta = 2.3 W the interpolation error is
-// about 1e-8 of the l2 norm of f.  Per (row, direction) the work is W complex
-// multiply-adds instead of C, so the direction count no longer multiplies the
-// channel work; the channel work moves to the tensor cores.
+// Comput. 41 (2019) C479).  With W = 7, beta = 2.3 W the interpolation error is
+// about 1e-7 of the l2 norm of f (their rule for a 2x grid: W = log10(1/eps) + 1).
+// Per (row, direction) the work is W + 1 complex multiply-adds instead of C, so the
+// direction count no longer multiplies the channel work; the channel work moves to
+// the tensor cores.
 //
 // Tile: M = 128 rows of the product = 4 baselines x 4 timesteps x 4 pols x
 // (re, im).  TMEM lane m = 32 q + 8 t + 2 p + s holds baseline q of the quad, so
@@ -36,8 +37,10 @@
 //
 // TMEM (512 columns, one block per SM): RS[0], RS[1] (running sums, double
 // buffered: the epilogue reads one while the next tile accumulates into the
-// other), IS (segments 1.. of the current tile), AC (corrections).  Columns
-// 0..Jw-1 of a region hold sum V_s Re E, columns Jw..2Jw-1 sum V_s Im E.
+// other), IS (segments 1.. of the current tile), AC (corrections).  Column 2j of
+// a region holds sum V_s Re E at window grid point j, column 2j + 1 sum V_s Im E
+// (the grid matrix interleaves its re and im rows), so the W + 1 taps of one
+// stencil are 2 (W + 1) = 16 adjacent columns: one 16-column tcgen05.ld.
 //
 // Warp roles (14 warps): 0 = TMA producer, 1 = MMA issuer (+ TMEM owner), 2-5 =
 // converters (split the visibility box into K-major hi/lo blocks, and fold the
@@ -54,16 +57,17 @@
 
 namespace leapgb {
 
-constexpr int kGrTaps = 10;           // W, grid points per interpolation
-constexpr float kGrBeta = 23.0f;      // 2.3 W
+constexpr int kGrTaps = 7;            // W, grid points per interpolation
+constexpr float kGrBeta = 16.1f;      // 2.3 W
 constexpr int kGrChunk = 16;          // channels per stage
 constexpr int kGrSegChunks = 4;       // chunks per hi*hi accumulation segment (64 channels)
 constexpr int kGrStages = 6;          // {visibility box / A hi, A lo, E window} ring
 constexpr int kGrMacro = 2;           // chunks handed over per barrier round (stages go in pairs)
 constexpr int kGrMacroStages = kGrStages / kGrMacro;
 constexpr int kGrJwMax = 64;          // grid points per pass (MMA N = 2 Jw <= 128)
-constexpr int kGrPassStride = 48;     // grid points between pass windows (multiple of 8)
-constexpr int kGrLoadCols = 16;       // TMEM columns one interpolation load reads
+constexpr int kGrPassStride = 56;     // grid points between pass windows (multiple of 8)
+constexpr int kGrLoadCols = 8;        // grid points one interpolation load reads (2 TMEM columns each)
+constexpr int kGrBatch = 4;           // directions whose loads share one tcgen05.wait::ld
 constexpr int kGrDirs = 64;           // directions per unit (8 epilogue warps x 32 / 4 quarters)
 constexpr int kGrEpiWarps = 8;
 constexpr int kGrWarpDirs = kGrDirs * 4 / kGrEpiWarps;  // directions per epilogue warp
@@ -76,8 +80,8 @@ static_assert(kGrAHalf == kGrVBytes, "the hi blocks are written over the visibil
 // Stage: [visibility box, then A hi][A lo][E]
 constexpr int kGrStageBytes = kGrVBytes + kGrAHalf + kGrEBytes;
 constexpr int kGrEOffset = kGrVBytes + kGrAHalf;
-constexpr int kGrRecWords = 20;                          // per (direction, timestep) record: 16-byte rows
-constexpr int kGrRecBytes = kGrEpiWarps * 32 * kGrRecWords * 4;  // [warps][4 t][8 dirs][20]
+constexpr int kGrRecWords = 12;                          // per (direction, timestep) record: 3 16-byte rows
+constexpr int kGrRecBytes = kGrEpiWarps * 32 * kGrRecWords * 4;  // [warps][4 t][8 dirs][12]
 constexpr uint32_t kGrRegion = 128;                      // TMEM columns per region
 constexpr uint32_t kGrIS = 2 * kGrRegion, kGrAC = 3 * kGrRegion;
 constexpr int kGrWide = 1 << 16;                         // record flag: the 4 timesteps need separate loads
@@ -96,7 +100,8 @@ __host__ __device__ constexpr int grid_smem_bytes() {
 __host__ __device__ constexpr int grid_lbase(int C) { return ((C + kGrTaps + 8 + 7) / 8) * 8; }
 __host__ __device__ constexpr int grid_rows(int C) { return ((grid_lbase(C) + C + kGrJwMax + 8 + 7) / 8) * 8; }
 __host__ __device__ constexpr int grid_chunks(int C) { return (C + kGrChunk - 1) / kGrChunk; }
-// Floats of the E table: [chunk][ks][hl][re/im][row group][8 rows x 8 k].
+// Floats of the E table: [chunk][ks][hl][row group][8 rows x 8 k], rows 2 l + (0: re, 1: im) of grid
+// point l (relative to -lbase).
 __host__ __device__ constexpr int64_t grid_table_floats(int C) {
   return static_cast<int64_t>(grid_chunks(C)) * 2 * 2 * 2 * grid_rows(C) * 8;
 }
@@ -165,6 +170,13 @@ __device__ __forceinline__ int grid_position(uint32_t pb, int n, float& f) {
   return static_cast<int>(prod >> 32);
 }
 
+// First grid point of the W-point stencil (W odd) around x = i0 + f: the points within
+// W/2 of x are round(x) - (W-1)/2 .. round(x) + (W-1)/2.
+static_assert(kGrTaps % 2 == 1, "the stencil start rounds x for odd W");
+__device__ __forceinline__ int grid_stencil_start(int i0, float f) {
+  return i0 - (kGrTaps - 1) / 2 + (f >= 0.5f ? 1 : 0);
+}
+
 __device__ __forceinline__ void tma_load_3d(void* smem_dst, const CUtensorMap* map, int x, int y, int z, uint64_t* bar) {
   asm volatile(
       "cp.async.bulk.tensor.3d.shared::cluster.global.tile.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, %4}], [%5];" ::"r"(
@@ -225,7 +237,8 @@ static __global__ void grid_windows(const GridParams p) {
       for (int h = 0; h < 2; ++h) {
         if (!has[h]) continue;
         float f;
-        const int s = grid_position(df_dot3_turns_u32(kb[h], x), n, f) - kGrTaps / 2 + 1;
+        const int i0 = grid_position(df_dot3_turns_u32(kb[h], x), n, f);
+        const int s = grid_stencil_start(i0, f);
         smin = min(smin, s);
         smax = max(smax, s);
       }
@@ -238,10 +251,10 @@ static __global__ void grid_windows(const GridParams p) {
     if (smin <= smax) {
       w.rg0 = (smin + I.lbase) >> 3;
       const int r0 = w.rg0 * 8;
-      // Stencil starts lie in [smin, smax]; a load reads kGrLoadCols columns from a start.
+      // Stencil starts lie in [smin, smax]; a load reads kGrLoadCols grid points from a start.
       const int need = smax + kGrLoadCols + I.lbase - r0;
       if (need <= kGrJwMax) {
-        w.jw = max(16, (need + 7) & ~7);
+        w.jw = max(8, (need + 7) & ~7);
         w.npass = 1;
       } else {
         w.jw = kGrJwMax;
@@ -264,52 +277,77 @@ __device__ __forceinline__ void grid_weights(float y, float (&w)[W + 1]) {
     const float z = (y - static_cast<float>(k)) * kInvHalf;
     const float z2 = z * z;
     const float q = fmaxf(1e-30f, 1.0f - z2);
-    w[k] = exp2f(-kBeta2 * __fdividef(z2, fmaf(q, rsqrtf(q), 1.0f)));
+    const float v = exp2f(-kBeta2 * __fdividef(z2, fmaf(q, rsqrtf(q), 1.0f)));
+    w[k] = z2 < 1.0f ? v : 0.0f;  // psi vanishes outside its support (the load's spare tap)
   }
 }
 
-// One direction of one lane: W + 1 taps of the grid values at TMEM columns col..,
-// weighted by wt (the lane's record), combined with the partner lane's component,
-// rotated by (cr, sr); returns this lane's component of the rotated sum.
-template <int W>
-__device__ __forceinline__ float grid_tap_sum(uint32_t taddr, int jw, const float (&rj)[W + 3], int comp) {
-  // Both loads and the wait in one statement: the results are defined only after the wait.
-  uint32_t vr[16], vi[16];
+// kGrBatch directions' stencils from TMEM: one 16-column load each (the W + 1 taps,
+// re and im interleaved) at columns col[b] of this warp's lanes, and one wait for all.
+__device__ __forceinline__ void grid_load_batch(uint32_t tbase, const uint32_t (&col)[kGrBatch],
+                                                uint32_t (&v)[kGrBatch][16]) {
+  static_assert(kGrBatch == 4 && kGrLoadCols == 8, "four 16-column loads per batch");
+  // All loads and the wait in one statement: the results are defined only after the wait.
   asm volatile(
-      "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%32];\n\t"
-      "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%16,%17,%18,%19,%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31}, [%33];\n\t"
+      "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%64];\n\t"
+      "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%16,%17,%18,%19,%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31}, [%65];\n\t"
+      "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%32,%33,%34,%35,%36,%37,%38,%39,%40,%41,%42,%43,%44,%45,%46,%47}, [%66];\n\t"
+      "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%48,%49,%50,%51,%52,%53,%54,%55,%56,%57,%58,%59,%60,%61,%62,%63}, [%67];\n\t"
       "tcgen05.wait::ld.sync.aligned;"
-      : "=r"(vr[0]), "=r"(vr[1]), "=r"(vr[2]), "=r"(vr[3]), "=r"(vr[4]), "=r"(vr[5]), "=r"(vr[6]), "=r"(vr[7]),
-        "=r"(vr[8]), "=r"(vr[9]), "=r"(vr[10]), "=r"(vr[11]), "=r"(vr[12]), "=r"(vr[13]), "=r"(vr[14]), "=r"(vr[15]),
-        "=r"(vi[0]), "=r"(vi[1]), "=r"(vi[2]), "=r"(vi[3]), "=r"(vi[4]), "=r"(vi[5]), "=r"(vi[6]), "=r"(vi[7]),
-        "=r"(vi[8]), "=r"(vi[9]), "=r"(vi[10]), "=r"(vi[11]), "=r"(vi[12]), "=r"(vi[13]), "=r"(vi[14]), "=r"(vi[15])
-      : "r"(taddr), "r"(taddr + static_cast<uint32_t>(jw)));
+      : "=r"(v[0][0]), "=r"(v[0][1]), "=r"(v[0][2]), "=r"(v[0][3]), "=r"(v[0][4]), "=r"(v[0][5]), "=r"(v[0][6]),
+        "=r"(v[0][7]), "=r"(v[0][8]), "=r"(v[0][9]), "=r"(v[0][10]), "=r"(v[0][11]), "=r"(v[0][12]), "=r"(v[0][13]),
+        "=r"(v[0][14]), "=r"(v[0][15]), "=r"(v[1][0]), "=r"(v[1][1]), "=r"(v[1][2]), "=r"(v[1][3]), "=r"(v[1][4]),
+        "=r"(v[1][5]), "=r"(v[1][6]), "=r"(v[1][7]), "=r"(v[1][8]), "=r"(v[1][9]), "=r"(v[1][10]), "=r"(v[1][11]),
+        "=r"(v[1][12]), "=r"(v[1][13]), "=r"(v[1][14]), "=r"(v[1][15]), "=r"(v[2][0]), "=r"(v[2][1]), "=r"(v[2][2]),
+        "=r"(v[2][3]), "=r"(v[2][4]), "=r"(v[2][5]), "=r"(v[2][6]), "=r"(v[2][7]), "=r"(v[2][8]), "=r"(v[2][9]),
+        "=r"(v[2][10]), "=r"(v[2][11]), "=r"(v[2][12]), "=r"(v[2][13]), "=r"(v[2][14]), "=r"(v[2][15]), "=r"(v[3][0]),
+        "=r"(v[3][1]), "=r"(v[3][2]), "=r"(v[3][3]), "=r"(v[3][4]), "=r"(v[3][5]), "=r"(v[3][6]), "=r"(v[3][7]),
+        "=r"(v[3][8]), "=r"(v[3][9]), "=r"(v[3][10]), "=r"(v[3][11]), "=r"(v[3][12]), "=r"(v[3][13]), "=r"(v[3][14]),
+        "=r"(v[3][15])
+      : "r"(tbase + col[0]), "r"(tbase + col[1]), "r"(tbase + col[2]), "r"(tbase + col[3]));
+}
+
+// One direction of one lane: the W + 1 taps v (re, im interleaved) weighted by the
+// lane's record (weights, then the rotation (cr, sr)), combined with the partner
+// lane's component, rotated; returns this lane's component of the rotated sum.
+template <int W>
+__device__ __forceinline__ float grid_tap_combine(const uint32_t (&v)[16], const float* rec, int comp) {
+  static_assert(W + 1 == 8, "record layout: 8 weights, then cr, sr, code");
+  const float4 q0 = reinterpret_cast<const float4*>(rec)[0], q1 = reinterpret_cast<const float4*>(rec)[1];
+  const float2 rot = reinterpret_cast<const float2*>(rec)[4];
+  const float w[8] = {q0.x, q0.y, q0.z, q0.w, q1.x, q1.y, q1.z, q1.w};
   float P = 0.f, Q = 0.f;
 #pragma unroll
   for (int k = 0; k <= W; ++k) {
-    P = fmaf(rj[k], __uint_as_float(vr[k]), P);
-    Q = fmaf(rj[k], __uint_as_float(vi[k]), Q);
+    P = fmaf(w[k], __uint_as_float(v[2 * k]), P);
+    Q = fmaf(w[k], __uint_as_float(v[2 * k + 1]), Q);
   }
   // Lane re (comp 0): P = sum Vr ReE, Q = sum Vr ImE; lane im: P = sum Vi ReE, Q = sum Vi ImE.
   // G = (P_re - Q_im) + i (Q_re + P_im); the lane's component of G * (cr + i sr).
   const float o = __shfl_xor_sync(0xffffffffu, Q, 1);
   const float gown = comp ? (o + P) : (P - o);
   const float o2 = __shfl_xor_sync(0xffffffffu, gown, 1);
-  const float cr = rj[W + 1], sr = rj[W + 2];
-  return comp ? fmaf(o2, sr, gown * cr) : fmaf(-o2, sr, gown * cr);
+  return comp ? fmaf(o2, rot.y, gown * rot.x) : fmaf(-o2, rot.y, gown * rot.x);
 }
 
 // A direction whose 4 timesteps need separate grid windows: one load per timestep
 // (rare; kept out of line so that the common path stays small).
 template <int W>
-__device__ __noinline__ float grid_wide_sum(const float* rec_dir, uint32_t tbase, int jw, const float (&rw)[W + 3], int comp,
-                                            int tl, int pp) {
+__device__ __noinline__ float grid_wide_sum(const float* rec_dir, uint32_t tbase, int comp, int tl, int pp) {
   float acc = 0.f;
   for (int tt = 0; tt < 4; ++tt) {
-    const int ct = __float_as_int(reinterpret_cast<const float4*>(rec_dir + tt * 8 * kGrRecWords)[3].y);
+    const float* r = rec_dir + tt * 8 * kGrRecWords;
+    const int ct = __float_as_int(r[10]);
     if ((ct & 0xFFFF) == 0xFFFF || ((ct >> 8) & 255) != pp) continue;  // same in every lane
-    const float v = grid_tap_sum<W>(tbase + static_cast<uint32_t>(ct & 255), jw, rw, comp);
-    if (tl == tt) acc += v;
+    uint32_t v[16];
+    asm volatile(
+        "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];\n\t"
+        "tcgen05.wait::ld.sync.aligned;"
+        : "=r"(v[0]), "=r"(v[1]), "=r"(v[2]), "=r"(v[3]), "=r"(v[4]), "=r"(v[5]), "=r"(v[6]), "=r"(v[7]), "=r"(v[8]),
+          "=r"(v[9]), "=r"(v[10]), "=r"(v[11]), "=r"(v[12]), "=r"(v[13]), "=r"(v[14]), "=r"(v[15])
+        : "r"(tbase + 2u * static_cast<uint32_t>(ct & 255)));
+    const float g = grid_tap_combine<W>(v, r, comp);
+    if (tl == tt) acc += g;
   }
   return acc;
 }
@@ -473,14 +511,11 @@ __global__ void __launch_bounds__(kGrThreads, 1) rotate_average_gridded(const Gr
 #pragma unroll
                 for (int ks = 0; ks < 2; ++ks)
 #pragma unroll
-                  for (int hl = 0; hl < 2; ++hl)
-#pragma unroll
-                    for (int ri = 0; ri < 2; ++ri) {
-                      const float* src =
-                          I.etab + ((static_cast<int64_t>(((q * 2 + ks) * 2 + hl) * 2 + ri) * I.nrg) + rg) * 64;
-                      bulk_copy_g2s(st + kGrEOffset + ((hl * 2 + ks) * 2 * w.jw + ri * w.jw) * 32, src, w.jw * 32,
-                                    &vfull[m]);
-                    }
+                  for (int hl = 0; hl < 2; ++hl) {
+                    // Window grid points [8 rg, 8 rg + jw): 2 jw interleaved (re, im) rows.
+                    const float* src = I.etab + (static_cast<int64_t>((q * 2 + ks) * 2 + hl) * 2 * I.nrg + 2 * rg) * 64;
+                    bulk_copy_g2s(st + kGrEOffset + (hl * 2 + ks) * 2 * w.jw * 32, src, 2 * w.jw * 32, &vfull[m]);
+                  }
               }
             }
       }
@@ -734,7 +769,7 @@ __global__ void __launch_bounds__(kGrThreads, 1) rotate_average_gridded(const Gr
               const uint32_t pb = df_dot3_turns_u32(kb, x);
               float f;
               const int i0 = grid_position(pb, n, f);
-              const int st = i0 - W / 2 + 1;  // this row's stencil start
+              const int st = grid_stencil_start(i0, f);  // this row's stencil start
               const int sl0 = rval ? st : 0x7fffffff, sh0 = rval ? st : -0x7fffffff;
               int cw = min(sl0, __shfl_xor_sync(0xffffffffu, sl0, 8));
               cw = min(cw, __shfl_xor_sync(0xffffffffu, cw, 16));
@@ -759,26 +794,39 @@ __global__ void __launch_bounds__(kGrThreads, 1) rotate_average_gridded(const Gr
               grid_weights<W>(any ? static_cast<float>(i0 - base) + f : 0.f, wt);
               float cr, sr;
               twiddle_turns(pa + static_cast<uint32_t>(c0) * pb, tab, cr, sr);
+              // Record: weights 0-7, then cr, sr, code.
               float4* my = reinterpret_cast<float4*>(rec + (tl * 8 + ps) * kGrRecWords);
               my[0] = make_float4(wt[0], wt[1], wt[2], wt[3]);
               my[1] = make_float4(wt[4], wt[5], wt[6], wt[7]);
-              my[2] = make_float4(wt[8], wt[9], wt[10], cr);
-              my[3] = make_float4(sr, __int_as_float(code), 0.f, 0.f);
+              my[2] = make_float4(cr, sr, __int_as_float(code), 0.f);
             }
             __syncwarp();
 #pragma unroll
-            for (int jj = 0; jj < 8; ++jj) {
-              const float4* rq = reinterpret_cast<const float4*>(rec + (tl * 8 + jj) * kGrRecWords);
-              const float4 q3 = rq[3];
-              const int code = __float_as_int(q3.y);  // same in every lane
-              if (code < 0) continue;
-              const float4 q0 = rq[0], q1 = rq[1], q2 = rq[2];
-              const float rw[W + 3] = {q0.x, q0.y, q0.z, q0.w, q1.x, q1.y, q1.z, q1.w, q2.x, q2.y, q2.z, q2.w, q3.x};
-              if (!(code & kGrWide)) {
-                if (((code >> 8) & 255) != pp) continue;
-                acc[gi * 8 + jj] += grid_tap_sum<W>(tbase + static_cast<uint32_t>(code & 255), w.jw, rw, comp);
-              } else {
-                acc[gi * 8 + jj] += grid_wide_sum<W>(rec + jj * kGrRecWords, tbase, w.jw, rw, comp, tl, pp);
+            for (int jb = 0; jb < 8; jb += kGrBatch) {
+              // The batch's directions that read this pass with one shared load (codes are the
+              // same in every lane for those): their loads, one wait, then their sums.
+              uint32_t col[kGrBatch];
+              int live = 0;
+#pragma unroll
+              for (int bb = 0; bb < kGrBatch; ++bb) {
+                const int code = __float_as_int(rec[(tl * 8 + jb + bb) * kGrRecWords + 10]);
+                const bool use = code >= 0 && !(code & kGrWide) && ((code >> 8) & 255) == pp;
+                col[bb] = use ? 2u * static_cast<uint32_t>(code & 255) : 0u;
+                live |= (use ? 1 : 0) << bb;
+              }
+              if (live) {
+                uint32_t v[kGrBatch][16];
+                grid_load_batch(tbase, col, v);
+#pragma unroll
+                for (int bb = 0; bb < kGrBatch; ++bb)
+                  if (live & (1 << bb))
+                    acc[gi * 8 + jb + bb] += grid_tap_combine<W>(v[bb], rec + (tl * 8 + jb + bb) * kGrRecWords, comp);
+              }
+#pragma unroll
+              for (int bb = 0; bb < kGrBatch; ++bb) {
+                const int code = __float_as_int(rec[(tl * 8 + jb + bb) * kGrRecWords + 10]);
+                if (code >= 0 && (code & kGrWide))  // the kGrWide bit is the same in every lane
+                  acc[gi * 8 + jb + bb] += grid_wide_sum<W>(rec + (jb + bb) * kGrRecWords, tbase, comp, tl, pp);
               }
             }
             __syncwarp();

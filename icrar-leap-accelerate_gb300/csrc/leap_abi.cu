@@ -109,10 +109,12 @@ struct TuneChoice {
 struct leap_ctx {
   int device = 0;
   int sms = 152;
+  bool pageable_direct = false;       // kernels can read pageable host memory in place (ATS / HMM)
   bool pipe_attr_set = false, pipe_attr_set4 = false;
   TuneChoice tune;
   bool capturing = false;             // recording a CUDA graph: skip host-side uploads and timing events
   bool autotune = true;               // tune new batched shapes on first use
+  bool graph_replay = true;           // batched calls: record and replay a CUDA graph per shape
   bool tc_gemm = true;                // mixed form: Ad contraction on the tensor cores (3xTF32)
   int mma_rotate = 1;                 // tensor-core rotate + average: 0 never, 1 autotuner candidate, 2 always
   int gridded = 2;                    // gridded rotate + average (tcgen05 grid product): 0 never, 1 always,
@@ -1058,7 +1060,7 @@ int calibrate_batched_impl(leap_ctx* ctx, const leap_work_item* witems, int32_t 
   for (int i = 0; i < nitems; ++i) items[i] = WorkItem{witems[i].slot, witems[i].first_direction, witems[i].ndirections};
   const std::string key = batch_key(ctx, items, D, precision);
   cudaStream_t s = ctx->stream;
-  if (ctx->graph_exec && ctx->graph_key == key && ctx->graph_epoch == g_alloc_epoch) {
+  if (ctx->graph_replay && ctx->graph_exec && ctx->graph_key == key && ctx->graph_epoch == g_alloc_epoch) {
     wait_for_uploads(ctx, items, s);
     cudaEvent_t* ev = ctx->ring[ctx->ring_count % leap_ctx::kRing];
     cudaEventRecord(ev[0], s);
@@ -1080,6 +1082,7 @@ int calibrate_batched_impl(leap_ctx* ctx, const leap_work_item* witems, int32_t 
   // Eager run: allocates and uploads the launch tables, produces this call's result.
   int rc = calibrate_items(ctx, items, ctx->dd.as<double>(), D, precision, ctx->cal.as<double>(), s);
   if (rc != LEAP_OK) return rc;
+  if (!ctx->graph_replay) return LEAP_OK;
   // Record the same launches once as a CUDA graph for the next calls of this shape.
   if (ctx->graph_exec) {
     cudaGraphExecDestroy(ctx->graph_exec);
@@ -1393,6 +1396,15 @@ int32_t leap_create(int32_t device, leap_ctx** out) {
   int rc = [&]() -> int {
     DeviceGuard g(device);
     LEAP_CUDA(cudaDeviceGetAttribute(&ctx->sms, cudaDevAttrMultiProcessorCount, device), "query SM count");
+    {
+      // On Grace hosts the GPU reads pageable host memory through the host's page tables
+      // at the rate of page-locked memory, so ingestion reads such sources in place.
+      int pageable = 0, host_tables = 0;
+      LEAP_CUDA(cudaDeviceGetAttribute(&pageable, cudaDevAttrPageableMemoryAccess, device), "query pageable access");
+      LEAP_CUDA(cudaDeviceGetAttribute(&host_tables, cudaDevAttrPageableMemoryAccessUsesHostPageTables, device),
+                "query pageable access");
+      ctx->pageable_direct = pageable != 0 && host_tables != 0;
+    }
     LEAP_CUDA(cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking), "create stream");
     LEAP_CUDA(cudaStreamCreateWithFlags(&ctx->aux, cudaStreamNonBlocking), "create aux stream");
     {
@@ -1652,6 +1664,7 @@ int32_t leap_set_integration_ms(leap_ctx* ctx, int32_t slot, int32_t vis_type, c
       direct = at.devicePointer;
     else
       cudaGetLastError();  // pageable memory: not an error
+    if (!direct && ctx->pageable_direct) direct = ms_data;  // pageable, read in place
   }
   if (direct) {
     int rc = ingest(ctx, vis_type, direct, row_channels, start_channel, rows, channels, pols, in.vis.ptr, rows, 0, s);
@@ -1713,9 +1726,13 @@ int32_t leap_set_integration_ms_async(leap_ctx* ctx, int32_t slot, int32_t vis_t
     cudaPointerAttributes au{};
     uvw_pinned = cudaPointerGetAttributes(&au, uvw) == cudaSuccess && au.type == cudaMemoryTypeHost;
     cudaGetLastError();
+    if (!direct && ctx->pageable_direct) direct = ms_data;  // pageable, read in place
+    if (!uvw_pinned && ctx->pageable_direct) uvw_pinned = true;
   }
   if (!direct || !uvw_pinned)
-    return fail(ctx, LEAP_ERR_INVALID_ARGUMENT, "asynchronous ingestion needs device or page-locked host memory");
+    return fail(ctx, LEAP_ERR_INVALID_ARGUMENT,
+                "asynchronous ingestion needs device memory, page-locked host memory, or a device that reads "
+                "pageable host memory");
   Integration& in = ctx->integ[slot];
   finish_upload(in);
   const size_t esz = vis_type == LEAP_VIS_C64 ? sizeof(float2) : sizeof(double2);
@@ -1968,6 +1985,7 @@ int32_t leap_set_option(leap_ctx* ctx, int32_t option, int32_t value) {
       if (value < 0 || value > 2) return fail(ctx, LEAP_ERR_INVALID_ARGUMENT, "gridded option must be 0, 1 or 2");
       ctx->gridded = value;
       return LEAP_OK;
+    case LEAP_OPTION_GRAPH_REPLAY: ctx->graph_replay = value != 0; return LEAP_OK;
     default: return fail(ctx, LEAP_ERR_INVALID_ARGUMENT, "unknown option");
   }
 }

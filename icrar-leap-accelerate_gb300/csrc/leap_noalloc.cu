@@ -7,6 +7,8 @@
 #include <cstring>
 #include <mutex>
 
+#include <cudaTypedefs.h>
+
 #include "leap_gb300.h"
 #include "kernels_rotate.cuh"
 
@@ -19,8 +21,18 @@ static __device__ __align__(256) unsigned char g_noalloc_scratch[LEAP_NOALLOC_SC
 namespace {
 
 constexpr int kMaxDevices = 64;
+
+// Per device: the scratch array's device address and the SM count, valid for the CUDA
+// context they were looked up in.  A device reset or another context made current on
+// the device loads the module again, at another address, so the entry is keyed by the
+// context's unique ID (cuCtxGetId: IDs are never reused within a process).
+struct DeviceSetup {
+  unsigned long long ctx_id = 0;
+  void* scratch = nullptr;
+  int sms = 0;
+};
 std::mutex g_mutex;
-void* g_scratch_addr[kMaxDevices] = {};  // device address of g_noalloc_scratch, per device
+DeviceSetup g_setup[kMaxDevices];
 
 thread_local char g_err[256] = {0};  // fixed buffer: reporting an error allocates nothing either
 
@@ -30,6 +42,26 @@ int fail(int code, const char* msg) {
   return code;
 }
 
+template <typename Fn>
+Fn driver_entry(const char* name, int version) {
+  void* f = nullptr;
+  cudaDriverEntryPointQueryResult q;
+  if (cudaGetDriverEntryPointByVersion(name, &f, version, cudaEnableDefault, &q) != cudaSuccess ||
+      q != cudaDriverEntryPointSuccess)
+    return nullptr;
+  return reinterpret_cast<Fn>(f);
+}
+
+// Unique ID of the context current on this thread (0 if none can be read).
+unsigned long long current_context_id() {
+  static const auto get_current = driver_entry<PFN_cuCtxGetCurrent_v4000>("cuCtxGetCurrent", 4000);
+  static const auto get_id = driver_entry<PFN_cuCtxGetId_v12000>("cuCtxGetId", 12000);
+  CUcontext c = nullptr;
+  unsigned long long id = 0;
+  if (!get_current || !get_id || get_current(&c) != CUDA_SUCCESS || !c || get_id(c, &id) != CUDA_SUCCESS) return 0;
+  return id;
+}
+
 // Wavelengths of the channels, formed as the reference's
 // Constants::GetChannelWavelength does: c / (f0 + ch*df), no fused multiply-add.
 __global__ void fill_wavelengths(double* lam, int channels, double f0, double df) {
@@ -37,9 +69,21 @@ __global__ void fill_wavelengths(double* lam, int channels, double f0, double df
     lam[c] = __ddiv_rn(kSpeedOfLight, __dadd_rn(f0, __dmul_rn(static_cast<double>(c), df)));
 }
 
+// Launches through cudaLaunchKernelEx, whose return value is this launch's own status:
+// an error left over from the caller's earlier work is neither reported nor cleared.
+template <typename... Params, typename... Args>
+cudaError_t launch_kernel(void (*kernel)(Params...), dim3 grid, dim3 block, cudaStream_t s, Args... args) {
+  cudaLaunchConfig_t cfg{};
+  cfg.gridDim = grid;
+  cfg.blockDim = block;
+  cfg.dynamicSmemBytes = 0;
+  cfg.stream = s;
+  return cudaLaunchKernelEx(&cfg, kernel, args...);
+}
+
 template <typename VisT, int P>
-void launch(const RotateArgs& a, dim3 grid, cudaStream_t s) {
-  rotate_average_fp64<VisT, P, 2, true><<<grid, 128, 0, s>>>(a);
+cudaError_t launch_rotate(const RotateArgs& a, dim3 grid, cudaStream_t s) {
+  return launch_kernel(rotate_average_fp64<VisT, P, 2, true>, grid, dim3(128), s, a);
 }
 
 }  // namespace
@@ -60,18 +104,28 @@ extern "C" int32_t leap_rotate_average_noalloc(int32_t vis_type, const void* vis
   if (cudaGetDevice(&dev) != cudaSuccess) return fail(LEAP_ERR_CUDA, "no current CUDA device");
   if (dev < 0 || dev >= kMaxDevices) return fail(LEAP_ERR_INVALID_ARGUMENT, "device index beyond the set-up table");
 
-  // Set-up, once per device with that device current: the host-side name of
-  // the array is not a device address, so ask the runtime for it.
+  // Set-up, once per device (and again if the device's context changed), with that
+  // device current: the host-side name of the array is not a device address, so ask
+  // the runtime for it.
   unsigned char* scratch = nullptr;
+  int sms = 0;
   {
     std::lock_guard<std::mutex> lock(g_mutex);
-    if (!g_scratch_addr[dev]) {
+    DeviceSetup& st = g_setup[dev];
+    const unsigned long long id = current_context_id();
+    if (!st.scratch || id == 0 || id != st.ctx_id) {
       void* p = nullptr;
       const cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
       if (e != cudaSuccess || !p) return fail(LEAP_ERR_CUDA, "cudaGetSymbolAddress of the scratch array failed");
-      g_scratch_addr[dev] = p;
+      int n = 0;
+      if (cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || n <= 0)
+        return fail(LEAP_ERR_CUDA, "cannot read the device's multiprocessor count");
+      st.scratch = p;
+      st.sms = n;
+      st.ctx_id = current_context_id();
     }
-    scratch = static_cast<unsigned char*>(g_scratch_addr[dev]);
+    scratch = static_cast<unsigned char*>(st.scratch);
+    sms = st.sms;
   }
 
   // Scratch layout: [wavelengths, 256-byte aligned][slab partial sums].
@@ -84,7 +138,7 @@ extern "C" int32_t leap_rotate_average_noalloc(int32_t vis_type, const void* vis
   const int dgroups = (ndirections + 7) / 8;  // 4 warps x 2 directions per block
   const size_t slab_bytes = sizeof(double2) * static_cast<size_t>(ndirections) * pols * nbl;
   // Timestep slabs: about 8 blocks per SM, as many as fit in the scratch.
-  int nts = static_cast<int>(std::min<int64_t>(T, std::max<int64_t>(1, (152 * 8 + int64_t(tiles) * dgroups - 1) /
+  int nts = static_cast<int>(std::min<int64_t>(T, std::max<int64_t>(1, (int64_t(sms) * 8 + int64_t(tiles) * dgroups - 1) /
                                                                            (int64_t(tiles) * dgroups))));
   while (nts > 1 && slab_bytes * nts > avail) --nts;
   const int t_per = (T + nts - 1) / nts;
@@ -110,25 +164,26 @@ extern "C" int32_t leap_rotate_average_noalloc(int32_t vis_type, const void* vis
   a.out = nts > 1 ? reinterpret_cast<double2*>(scratch + lam_bytes) : reinterpret_cast<double2*>(avg_out);
 
   cudaStream_t s = static_cast<cudaStream_t>(stream);
-  fill_wavelengths<<<(channels + 255) / 256, 256, 0, s>>>(reinterpret_cast<double*>(scratch), channels,
-                                                           freq_start_hz, freq_inc_hz);
+  cudaError_t e = launch_kernel(fill_wavelengths, dim3((channels + 255) / 256), dim3(256), s,
+                                reinterpret_cast<double*>(scratch), channels, freq_start_hz, freq_inc_hz);
+  if (e != cudaSuccess) return fail(LEAP_ERR_CUDA, cudaGetErrorString(e));
   const dim3 grid(tiles, dgroups, nts);
   if (vis_type == LEAP_VIS_C64) {
-    if (pols == 1) launch<float2, 1>(a, grid, s);
-    else if (pols == 2) launch<float2, 2>(a, grid, s);
-    else launch<float2, 4>(a, grid, s);
+    if (pols == 1) e = launch_rotate<float2, 1>(a, grid, s);
+    else if (pols == 2) e = launch_rotate<float2, 2>(a, grid, s);
+    else e = launch_rotate<float2, 4>(a, grid, s);
   } else {
-    if (pols == 1) launch<double2, 1>(a, grid, s);
-    else if (pols == 2) launch<double2, 2>(a, grid, s);
-    else launch<double2, 4>(a, grid, s);
+    if (pols == 1) e = launch_rotate<double2, 1>(a, grid, s);
+    else if (pols == 2) e = launch_rotate<double2, 2>(a, grid, s);
+    else e = launch_rotate<double2, 4>(a, grid, s);
   }
+  if (e != cudaSuccess) return fail(LEAP_ERR_CUDA, cudaGetErrorString(e));
   if (nts > 1) {
     const int64_t n = static_cast<int64_t>(ndirections) * pols * nbl;
-    const int blocks = static_cast<int>(std::min<int64_t>((n + 255) / 256, 152 * 32));
-    reduce_slabs<<<blocks, 256, 0, s>>>(reinterpret_cast<const double2*>(scratch + lam_bytes), nts, n,
-                                        reinterpret_cast<double2*>(avg_out));
+    const int blocks = static_cast<int>(std::min<int64_t>((n + 255) / 256, int64_t(sms) * 32));
+    e = launch_kernel(reduce_slabs, dim3(blocks), dim3(256), s, reinterpret_cast<const double2*>(scratch + lam_bytes),
+                      nts, n, reinterpret_cast<double2*>(avg_out));
+    if (e != cudaSuccess) return fail(LEAP_ERR_CUDA, cudaGetErrorString(e));
   }
-  const cudaError_t e = cudaGetLastError();
-  if (e != cudaSuccess) return fail(LEAP_ERR_CUDA, cudaGetErrorString(e));
   return LEAP_OK;
 }

@@ -132,7 +132,8 @@ def make_observation(spec: ArraySpec, timesteps: int, channels: int, freq_start_
                      vis_dtype=np.complex64, pols: int = 4, flag_autos: bool = True,
                      cadence_s: float = 8.0, hour_angle0: float = 0.0, with_vis: bool = True,
                      seeds=(0, 1, 2), timestep_offset: int = 0, positions: Optional[np.ndarray] = None,
-                     gains: Optional[np.ndarray] = None, channel_block: int = 16) -> Observation:
+                     gains: Optional[np.ndarray] = None, channel_block: int = 16,
+                     phase_centre=PHASE_CENTRE) -> Observation:
     pos = antenna_positions(spec, seeds[0]) if positions is None else positions
     S = spec.stations
     if gains is None:
@@ -140,7 +141,7 @@ def make_observation(spec: ArraySpec, timesteps: int, channels: int, freq_start_
         gains = np.exp(1j * g_rng.uniform(-np.pi, np.pi, S))
     a1, a2 = baselines(S, True)
     nbl = a1.size
-    ra0, dec0 = PHASE_CENTRE
+    ra0, dec0 = phase_centre
     rows = timesteps * nbl
     uvw = np.empty((rows, 3), dtype=np.float64)
     for t in range(timesteps):
@@ -169,7 +170,7 @@ def make_observation(spec: ArraySpec, timesteps: int, channels: int, freq_start_
             vis[c0:c1] = blk.astype(vis_dtype, copy=False)
     return Observation(
         num_stations=S, total_antennas=S, nbaselines=nbl, timesteps=timesteps, channels=channels,
-        pols=pols, freq_start_hz=freq_start_hz, freq_inc_hz=freq_inc_hz, phase_centre=PHASE_CENTRE,
+        pols=pols, freq_start_hz=freq_start_hz, freq_inc_hz=freq_inc_hz, phase_centre=tuple(phase_centre),
         antenna1=np.tile(a1, 1), antenna2=np.tile(a2, 1), flags=flags, uvw=uvw, epochs=epochs,
         vis=vis, gains=gains, positions_enu=pos, source_lmn=np.array([l0, m0, n0]), noise_sigma=noise_sigma)
 
@@ -197,6 +198,14 @@ def mwa_precision(with_vis: bool = True, timesteps: int = 14, channels: int = 38
     dirs, lm = random_directions(directions)
     dirs[0] = lm_to_radec(np.array([0.01]), np.array([-0.005]))[0]
     return obs, dirs
+
+
+def mwa_at_phase_centre(phase_centre, with_vis: bool = True, timesteps: int = 14, channels: int = 384) -> Observation:
+    """The 128-antenna array of mwa_precision observed about another phase centre (ra, dec)
+    in radians: for calibration directions given as (ra, dec) far from it."""
+    return make_observation(ArraySpec(128, 1500.0), timesteps=timesteps, channels=channels,
+                            freq_start_hz=150e6, freq_inc_hz=40e3, noise_sigma=0.5, source_lm=(0.01, -0.005),
+                            vis_dtype=np.complex64, with_vis=with_vis, phase_centre=phase_centre)
 
 
 def small_case(stations: int = 8, timesteps: int = 2, channels: int = 6, pols: int = 4, directions: int = 3,
@@ -341,28 +350,38 @@ def ska_low(with_vis: bool = True, timesteps: int = 16, channels: int = 384, dir
     return obs, dirs
 
 
-def batched_uneven(chunks: int = 32, directions: int = 256, stations: int = 128):
+def batched_uneven(chunks: int = 32, directions: int = 256, stations: int = 128,
+                   sample_timesteps: Optional[int] = None, direction_ids: Optional[np.ndarray] = None):
     """The batched workload: `chunks` consecutive integration chunks of the
     128-antenna array (timesteps uniform in 1..64, channels from {48, 96, 384},
     seed 4), 150 MHz / 40 kHz, sigma 0.5, and `directions` directions dealt
     round-robin to the chunks (direction j -> chunk j mod chunks).
 
-    Returns (observations without visibilities, directions (ra, dec) in item
-    order, work items [(slot, first_direction, ndirections)], original direction
-    index of each item-ordered direction)."""
+    With sample_timesteps, each chunk is cut to its first sample_timesteps timesteps
+    and its visibilities are generated on the host (a bounded sample of the workload
+    for a CPU run).  direction_ids restricts the calibration to those of the
+    `directions` directions (each still goes to chunk j mod chunks; a sharded run
+    passes its own range).
+
+    Returns (observations, directions (ra, dec) in item order, work items
+    [(slot, first_direction, ndirections)], original direction index of each
+    item-ordered direction)."""
     spec = ArraySpec(stations, 1500.0)
     pos = antenna_positions(spec, 0)
     gains = np.exp(1j * np.random.default_rng(1).uniform(-np.pi, np.pi, stations))
     shapes = uneven_chunks(chunks, seed=4)
     dirs, _ = random_directions(directions)
     dirs[0] = lm_to_radec(np.array([0.01]), np.array([-0.005]))[0]
+    wanted = np.arange(directions) if direction_ids is None else np.asarray(direction_ids)
     obs_list, order, items = [], [], []
     for i, ch in enumerate(shapes):
-        obs_list.append(make_observation(spec, timesteps=ch.timesteps, channels=ch.channels, freq_start_hz=150e6,
+        t = ch.timesteps if sample_timesteps is None else min(ch.timesteps, sample_timesteps)
+        obs_list.append(make_observation(spec, timesteps=t, channels=ch.channels, freq_start_hz=150e6,
                                          freq_inc_hz=40e3, noise_sigma=0.5, source_lm=(0.01, -0.005),
-                                         vis_dtype=np.complex64, with_vis=False, timestep_offset=ch.timestep_offset,
-                                         positions=pos, gains=gains))
-        mine = [j for j in range(directions) if j % chunks == i]
+                                         vis_dtype=np.complex64, with_vis=sample_timesteps is not None,
+                                         timestep_offset=ch.timestep_offset, positions=pos, gains=gains,
+                                         seeds=(0, 1, 2 + i)))
+        mine = [int(j) for j in wanted if j % chunks == i]
         if mine:
             items.append((i, len(order), len(mine)))
             order += mine

@@ -142,15 +142,18 @@ int32_t leap_set_integration(leap_ctx* ctx, int32_t slot, int32_t vis_type, cons
  * LA/ms/MeasurementSet.h:95-204); channels [start_channel, start_channel +
  * channels) of each row are taken.  The transpose to the Integration layout and
  * the NaN rule run on the device.  Device memory and page-locked host memory
- * are read directly by the transpose kernel; pageable host memory goes through
- * two pinned 64 MiB staging buffers, the host copy of one piece overlapping the
- * upload and transpose of the previous one. */
+ * are read directly by the transpose kernel, and so is pageable host memory on
+ * devices that read it through the host's page tables (Grace hosts:
+ * cudaDevAttrPageableMemoryAccessUsesHostPageTables); elsewhere pageable memory
+ * goes through two pinned 64 MiB staging buffers, the host copy of one piece
+ * overlapping the upload and transpose of the previous one. */
 int32_t leap_set_integration_ms(leap_ctx* ctx, int32_t slot, int32_t vis_type, const void* ms_data,
                                 int64_t row_channels, int32_t start_channel, const double* uvw, int64_t rows,
                                 int32_t channels, int32_t pols, int32_t memory);
 
 /* Asynchronous form of leap_set_integration_ms for device or page-locked host
- * memory (ms_data and uvw; anything else is rejected): the upload is queued on the
+ * memory, or pageable host memory on devices that read it in place (ms_data and
+ * uvw; anything else is rejected): the upload is queued on the
  * context's copy stream, after every call already queued on the context's stream,
  * and the function returns at once.  Calibrate calls on the slot wait for it on the
  * device; rewriting or releasing the slot waits for it on the host.  The caller
@@ -226,6 +229,10 @@ int32_t leap_set_autotune(leap_ctx* ctx, int32_t enable);
                                                     10-point interpolation per (row, direction).  0: never;
                                                     1: always; 2 (default): when every work item has at least
                                                     32 directions (unless the tensor-core rotation is forced) */
+#define LEAP_OPTION_GRAPH_REPLAY 5             /* leap_calibrate_batched: 1 (default) records a call's launches as
+                                                    a CUDA graph and replays it for later calls of the same shape;
+                                                    0 launches every call eagerly, so that its timing events (and
+                                                    leap_get_timings' rotate_ms) bracket the rotate + average stage */
 int32_t leap_set_option(leap_ctx* ctx, int32_t option, int32_t value);
 
 /* Copy the avgData of `direction` from the last calibrate call to host memory

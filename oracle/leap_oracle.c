@@ -281,6 +281,53 @@ int oracle_calibrate_interval(const void* vis, int vis_f32, const double* uvw, i
     return err;
 }
 
+/*
+ * Several solution intervals (integration chunks of one array, so one set of A, Ad,
+ * A1, Ad1), each with its own directions: the direction loop of
+ * CpuLeapCalibrator::Calibrate (LA/algorithm/cpu/CpuLeapCalibrator.cc:132-139) for
+ * every chunk, one (chunk, direction) pair per task, so that all host threads are busy
+ * when each chunk has fewer directions than there are threads.  Each task is exactly
+ * the per-direction work of oracle_calibrate_interval.
+ *
+ * Chunk i: vis[i] (channels[i] x rows[i] x pols), uvw[i] (rows[i] x 3), dd[i]
+ * (ndir[i] row-major 3x3), cal_out[i] (ndir[i] x S), avg_out[i] (NULL, or ndir[i]
+ * avgData blocks as in oracle_calibrate_interval).
+ */
+int oracle_calibrate_items(int32_t nitems, const void* const* vis, int vis_f32, const double* const* uvw,
+                           const int64_t* rows, const int32_t* channels, int32_t pols, int32_t nbl, double f0,
+                           double df, const double* const* dd, const int32_t* ndir,
+                           const double* A, int32_t A_rows, int32_t S, const double* Ad,
+                           const int32_t* I1, const double* Ad1, int32_t A1_rows,
+                           double* const* cal_out, double* const* avg_out, int32_t nthreads)
+{
+#ifdef _OPENMP
+    if (nthreads <= 0) nthreads = omp_get_max_threads();
+#endif
+    (void)nthreads;
+    int64_t ntask = 0;
+    for (int32_t i = 0; i < nitems; ++i) ntask += ndir[i];
+    int err = ORACLE_OK;
+#ifdef _OPENMP
+#pragma omp parallel for num_threads(nthreads) schedule(dynamic, 1)
+#endif
+    for (int64_t t = 0; t < ntask; ++t) {
+        int32_t i = 0;
+        int64_t d = t;
+        while (d >= ndir[i]) d -= ndir[i++];
+        double* avg = (double*)calloc((size_t)2 * nbl * pols, sizeof(double));
+        if (!avg) {
+            err = ORACLE_ERR_INVALID_ARGUMENT;
+            continue;
+        }
+        oracle_rotate_visibilities(vis[i], vis_f32, uvw[i], dd[i] + 9 * (size_t)d, rows[i], channels[i], pols, nbl,
+                                   f0, df, avg);
+        oracle_solve(avg, nbl, A, A_rows, S, Ad, I1, Ad1, A1_rows, cal_out[i] + (size_t)S * d);
+        if (avg_out && avg_out[i]) memcpy(avg_out[i] + (size_t)2 * nbl * pols * d, avg, sizeof(double) * 2 * nbl * pols);
+        free(avg);
+    }
+    return err;
+}
+
 int oracle_max_threads(void)
 {
 #ifdef _OPENMP

@@ -72,6 +72,9 @@ def _load():
         lib.oracle_calibrate_interval.argtypes = [vp, ctypes.c_int, vp, i64, i32, i32, i32, f64, f64,
                                                   vp, i32, vp, i32, i32, vp, vp, vp, i32, vp, vp, i32]
         lib.oracle_calibrate_interval.restype = ctypes.c_int
+        lib.oracle_calibrate_items.argtypes = [i32, vp, ctypes.c_int, vp, vp, vp, i32, i32, f64, f64, vp, vp,
+                                               vp, i32, i32, vp, vp, vp, i32, vp, vp, i32]
+        lib.oracle_calibrate_items.restype = ctypes.c_int
         lib.oracle_max_threads.argtypes = []
         lib.oracle_max_threads.restype = ctypes.c_int
         _lib = lib
@@ -255,6 +258,47 @@ def calibrate_interval(vis: np.ndarray, uvw: np.ndarray, dds: np.ndarray, md: Or
         avg_c = avg.view(np.complex128).reshape(D, P, md.nbaselines).transpose(0, 2, 1).copy()
         return cal, avg_c
     return cal
+
+
+def calibrate_items(chunks, md: OracleMetaData, nthreads: int = 0, return_avg: bool = False):
+    """Several integration chunks of one array, each with its own directions: `chunks` is a
+    list of (vis (channels, rows, pols), uvw (rows, 3), dds (D, 3, 3)).  One (chunk, direction)
+    pair per host task.  Returns a list of cal (D, S) (and of avgData (D, nbl, P))."""
+    n = len(chunks)
+    vis_l, uvw_l, dd_l, cal_l, avg_l = [], [], [], [], []
+    f32 = None
+    P = None
+    for vis, uvw, dds in chunks:
+        v, f = _vis_args(vis)
+        if f32 is None:
+            f32, P = f, v.shape[2]
+        if f != f32 or v.shape[2] != P:
+            raise TypeError("chunks must share one visibility dtype and pol count")
+        vis_l.append(v)
+        uvw_l.append(np.ascontiguousarray(uvw, dtype=np.float64))
+        dd_l.append(np.ascontiguousarray(dds, dtype=np.float64).reshape(-1, 9))
+    A = np.asfortranarray(md.A)
+    Ad = np.asfortranarray(md.Ad)
+    Ad1 = np.asfortranarray(md.Ad1)
+    I1 = np.ascontiguousarray(md.I1, dtype=np.int32)
+    S = A.shape[1]
+    for d in dd_l:
+        cal_l.append(np.zeros((d.shape[0], S), dtype=np.float64))
+        avg_l.append(np.zeros(d.shape[0] * 2 * md.nbaselines * P, dtype=np.float64) if return_avg else None)
+    ptrs = lambda arrs: (ctypes.c_void_p * n)(*[a.ctypes.data if a is not None else None for a in arrs])
+    rows = np.array([v.shape[1] for v in vis_l], dtype=np.int64)
+    chans = np.array([v.shape[0] for v in vis_l], dtype=np.int32)
+    ndir = np.array([d.shape[0] for d in dd_l], dtype=np.int32)
+    rc = _load().oracle_calibrate_items(
+        n, ptrs(vis_l), f32, ptrs(uvw_l), _ptr(rows), _ptr(chans), P, md.nbaselines, md.freq_start_hz,
+        md.freq_inc_hz, ptrs(dd_l), _ptr(ndir), _ptr(A), A.shape[0], S, _ptr(Ad), _ptr(I1), _ptr(Ad1),
+        md.A1.shape[0], ptrs(cal_l), ptrs(avg_l) if return_avg else None, int(nthreads))
+    if rc != 0:
+        raise MemoryError("oracle allocation failed")
+    if return_avg:
+        avgs = [a.view(np.complex128).reshape(-1, P, md.nbaselines).transpose(0, 2, 1).copy() for a in avg_l]
+        return cal_l, avgs
+    return cal_l
 
 
 def evaluate_slice(start: int, interval: int, end: int, collection_size: int):

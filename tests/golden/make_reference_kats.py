@@ -9,8 +9,11 @@ or run) and records the numbers its hot-path tests assert:
 * channel-0 wavelength, dlm_ra/dlm_dec constants (PhaseRotateTests.cc:202-207,
   MetaDataTests.cc:186)
 * pseudoinverse known answers (src/icrar/leap-accelerate/tests/math/MatrixTests.cc:154-250)
+* the calibration directions of the end-to-end multi-direction run
+    (src/icrar/leap-accelerate-cli/tests/E2EPerformanceTests.cc:65-76) and of the
+    phase-rotate test (PhaseRotateTests.cc:97-103), as (ra, dec) in radians
 
-Usage:  python tests/golden/make_reference_kats.py [reference_root]
+Usage:  python tests/golden/make_reference_kats.py <reference_root>
 """
 from __future__ import annotations
 
@@ -76,6 +79,12 @@ def main(root):
         e = _matrix_after(blk, "expected_m1d", c, r)
         pinv.append({"name": name, "A": a, "expected": e})
 
+    e2e = os.path.join(root, "src", "icrar", "leap-accelerate-cli", "tests", "E2EPerformanceTests.cc")
+    e2e_dirs = [_nums(x) for x in re.findall(r"MVDirection\(([^)]*)\)", _lines(e2e, 65, 76))]
+    assert len(e2e_dirs) == 9 and all(len(d) == 2 for d in e2e_dirs), e2e_dirs
+    pr_dirs = [_nums(x) for x in re.findall(r"\{\s*(" + NUM + r"\s*,\s*" + NUM + r")\s*\}", _lines(pr, 97, 103))]
+    assert len(pr_dirs) == 4, pr_dirs
+
     out = {
         "source": "reference gtest sources (values asserted by the hot-path tests)",
         "dd": {"phase_centre": [consts["phase_centre_ra_rad"], consts["phase_centre_dec_rad"]],
@@ -85,6 +94,9 @@ def main(root):
         "pinv_tolerance": 1e-4,
         "pinv": pinv,
         "phase_matrix_empty_input_throws": {"refAnt": 0},
+        "e2e_directions": {"source": "E2EPerformanceTests.cc:65-76 (MultiDirectionTest: Slice(0,1,1), refAnt 0)",
+                           "radec": e2e_dirs},
+        "phase_rotate_directions": {"source": "PhaseRotateTests.cc:97-103", "radec": pr_dirs},
     }
     here = os.path.dirname(os.path.abspath(__file__))
     with open(os.path.join(here, "reference_kats.json"), "w") as f:
@@ -93,4 +105,6 @@ def main(root):
 
 
 if __name__ == "__main__":
-    main(sys.argv[1] if len(sys.argv) > 1 else "/root/reference")
+    if len(sys.argv) != 2:
+        sys.exit("usage: make_reference_kats.py <reference_root>")
+    main(sys.argv[1])

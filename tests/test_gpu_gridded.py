@@ -4,8 +4,9 @@ the grid values as one 3xTF32 tcgen05 product per tile.
 
 Bars, as for the other mixed-form kernels: avgData within 2e-6 of the oracle's
 FP64 sums relative to the sum of |terms| of each (baseline, pol); per-antenna cal
-phase within 1e-5 rad of the oracle (directions whose solve passes an arg() within
-1e-4 rad of +-pi excluded, as in the other parity tests).
+phase within 1e-5 rad of the oracle, or of the oracle's solve with angles within
+1e-4 rad of +-pi on the other branch (proved per direction, as in the other parity
+tests).
 """
 import numpy as np
 import pytest
@@ -49,7 +50,7 @@ def _check(ctx, obs, dirs, avg_tol=AVG_TOL):
     err = np.abs(avg - avg_o) / np.maximum(_scale(obs), 1e-30)[None]
     assert np.isfinite(cal).all()
     assert err.max() < avg_tol, err.max()
-    assert_cal_close(cal, cal_o, avg_o, mdo, MIXED_CAL_TOL, 1e-4)
+    assert_cal_close(cal, cal_o, avg_o, mdo, MIXED_CAL_TOL)
     ctx.release_integration(0)
     return cal, cal_o
 
@@ -101,7 +102,7 @@ def test_gridded_nan_samples_are_skipped(ctx):
     cal = _gridded(ctx, lambda: ctx.calibrate(0, dds, lg.LEAP_PRECISION_MIXED))
     cal_o, avg_o = oracle.calibrate_interval(obs.vis, obs.uvw, dds, mdo, return_avg=True)
     assert np.isfinite(cal).all()
-    assert_cal_close(cal, cal_o, avg_o, mdo, MIXED_CAL_TOL, 1e-4)
+    assert_cal_close(cal, cal_o, avg_o, mdo, MIXED_CAL_TOL)
     ctx.release_integration(0)
 
 
@@ -141,7 +142,7 @@ def test_gridded_batched_graph(ctx):
         ctx.set_option(LEAP_OPTION_GRIDDED_ROTATION, 2)
     for slot, (obs, dirs, d0) in enumerate(chunks):
         exp, avg_o = oracle.calibrate_interval(obs.vis, obs.uvw, dds[d0:d0 + len(dirs)], mdo, return_avg=True)
-        assert_cal_close(cal[d0:d0 + len(dirs)], exp, avg_o, mdo, MIXED_CAL_TOL, 1e-4)
+        assert_cal_close(cal[d0:d0 + len(dirs)], exp, avg_o, mdo, MIXED_CAL_TOL)
     np.testing.assert_array_equal(cal, again)
     for slot in range(len(chunks)):
         ctx.release_integration(slot)
@@ -165,5 +166,5 @@ def test_gridded_auto_selection(ctx):
     cal_o, avg_o = oracle.calibrate_interval(obs.vis, obs.uvw, dds, mdo, return_avg=True)
     for nd in (40, 8):
         cal = ctx.calibrate(0, dds[:nd], lg.LEAP_PRECISION_MIXED)
-        assert_cal_close(cal, cal_o[:nd], avg_o[:nd], mdo, MIXED_CAL_TOL, 1e-4)
+        assert_cal_close(cal, cal_o[:nd], avg_o[:nd], mdo, MIXED_CAL_TOL)
     ctx.release_integration(0)

@@ -49,3 +49,21 @@ def test_dd_third_row_is_lmn():
         dd = oracle.dd_matrix(*synth.PHASE_CENTRE, rd[0], rd[1])
         n = np.sqrt(1 - lm[0] ** 2 - lm[1] ** 2)
         np.testing.assert_allclose(dd[2], [lm[0], lm[1], n], atol=1e-14)
+
+
+def test_calibrate_items_equals_per_interval_calls():
+    """oracle.calibrate_items (one host task per (chunk, direction)) gives exactly the
+    results of calibrate_interval chunk by chunk."""
+    import oracle
+    from leap_gb300 import synth
+    obs, dirs = synth.small_case(stations=12, timesteps=3, channels=9, directions=5, vis_dtype=np.complex64)
+    mdo = oracle.metadata(obs)
+    dds = np.stack([oracle.dd_matrix(*obs.phase_centre, r, d) for r, d in dirs])
+    nbl = obs.nbaselines
+    parts = [(slice(0, nbl), slice(0, 2)), (slice(nbl, 3 * nbl), slice(2, 5))]
+    chunks = [(obs.vis[:, r], obs.uvw[r], dds[d]) for r, d in parts]
+    cals, avgs = oracle.calibrate_items(chunks, mdo, nthreads=3, return_avg=True)
+    for (vis, uvw, dd), cal, avg in zip(chunks, cals, avgs):
+        exp, exp_avg = oracle.calibrate_interval(vis, uvw, dd, mdo, return_avg=True)
+        np.testing.assert_array_equal(cal, exp)
+        np.testing.assert_array_equal(avg, exp_avg)

@@ -34,13 +34,18 @@ def _regular_avgdata(obs, dds):
         return np.stack([ctx.avgdata(d) for d in range(dds.shape[0])])  # (D, nbl, P)
 
 
-@pytest.mark.parametrize("dtype,timesteps", [(np.complex128, 5), (np.complex64, 9)])
-def test_no_alloc_entry_point_matches_regular_path(dtype, timesteps):
+@pytest.mark.parametrize("dtype,timesteps,stations,channels,ndir", [
+    (np.complex128, 5, 24, 40, 6),    # several timestep slabs
+    (np.complex64, 9, 24, 40, 6),
+    (np.complex64, 1, 24, 40, 6),     # one timestep: the kernel writes avg_out itself, no slab sum
+    (np.complex64, 6, 128, 16, 8),    # 4.2 MB per slab: fewer slabs than the launch wants, to fit 16 MiB
+], ids=["c128_slabs", "c64_slabs", "c64_single_slab", "c64_slabs_cut_to_fit"])
+def test_no_alloc_entry_point_matches_regular_path(dtype, timesteps, stations, channels, ndir):
     import torch
-    obs, dirs = synth.small_case(stations=24, timesteps=timesteps, channels=40, pols=4, directions=6,
+    obs, dirs = synth.small_case(stations=stations, timesteps=timesteps, channels=channels, pols=4, directions=ndir,
                                  vis_dtype=dtype, seed_shift=5)
     vis = obs.vis.copy()
-    vis.reshape(-1)[[3, 1000, 4321]] = np.nan
+    vis.reshape(-1)[[3, 1000, min(4321, vis.size - 1)]] = np.nan
     obs.vis = vis
     md = lg.build_metadata(obs)
     dds = np.stack([lg.dd_matrix(md.phase_centre_ra_rad, md.phase_centre_dec_rad, r, d) for r, d in dirs])
