@@ -331,10 +331,10 @@ def per_direction_bytes(samples: float, rows: float, nbl: int, ndir: int) -> flo
     return ndir * (samples * 8 + rows * 24) + ndir * nbl * 4 * 16
 
 
-def grid_windows_host(obs, dds: np.ndarray, taps: int = 7, jw_max: int = 64, stride: int = 56, load: int = 8,
-                      dirs_per_unit: int = 64):
-    """The gridded kernel's grid windows of one call, computed as its grid_windows kernel does:
-    (tensor-core FLOPs per call, mean passes per tile, max passes)."""
+def grid_windows_host(obs, dds: np.ndarray, taps: int = 8, jw_max: int = 64, stride: int = 56, load: int = 9):
+    """The gridded kernel's grid windows of one call, computed as its grid_windows kernel does
+    (one window per quad of baselines over all directions): (tensor-core FLOPs per call, mean
+    passes per tile, max passes)."""
     C, nbl, T = obs.channels, obs.nbaselines, obs.timesteps
     n, lbase = 2 * C, ((C + taps + 8 + 7) // 8) * 8
     nchunk = (C + 15) // 16
@@ -342,10 +342,10 @@ def grid_windows_host(obs, dds: np.ndarray, taps: int = 7, jw_max: int = 64, str
     uvw = obs.uvw.reshape(T, nbl, 3)
     nquad = (nbl + 3) // 4
     flops, passes, tiles, pmax = 0.0, 0.0, 0.0, 0
-    for d0 in range(0, dds.shape[0], dirs_per_unit):
-        B = np.einsum("tbj,dj->tbd", uvw, kb[d0:d0 + dirs_per_unit])
+    for d0 in range(0, 1):
+        B = np.einsum("tbj,dj->tbd", uvw, kb)
         B = B - np.rint(B)
-        s = np.floor(B * n + 0.5).astype(np.int64) - (taps - 1) // 2  # stencil start
+        s = np.floor(B * n).astype(np.int64) - taps // 2 + 1  # stencil start
         pad = nquad * 4 - nbl
         smin = np.pad(s.min(axis=(0, 2)), (0, pad), constant_values=1 << 40).reshape(nquad, 4).min(axis=1)
         smax = np.pad(s.max(axis=(0, 2)), (0, pad), constant_values=-(1 << 40)).reshape(nquad, 4).max(axis=1)
@@ -738,7 +738,7 @@ def run_workload(name, args, torch, lg, local, rank, world, dist, steps, warmup,
     cal_main = w.result()
     gridded = uses_gridded(args, w, prec, lg)
     if gridded and name in ("mwa", "ska_low"):
-        w.kernel_name = ("rotate_average_gridded<7> (3xTF32 tcgen05 grid product + 8-point interpolation per "
+        w.kernel_name = ("rotate_average_gridded<8> (3xTF32 tcgen05 grid product + 8-point interpolation per "
                          "direction) + grid_windows + the compensated reference-antenna pass")
         w.traffic = getattr(w, "grid_traffic", None)
     elif name in ("mwa", "ska_low"):

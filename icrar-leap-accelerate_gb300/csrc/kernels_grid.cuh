@@ -14,8 +14,9 @@
 // over the W grid points nearest n B, with psi the "exponential of semicircle"
 // kernel psi(x) = exp(beta (sqrt(1 - (2x/W)^2) - 1)) and Psi its Fourier
 // transform at frequency k / n (Barnett, Magland & af Klinteberg, SIAM J. Sci.
-// Comput. 41 (2019) C479).  With W = 7, beta = 2.3 W the interpolation error is
-// about 1e-7 of the l2 norm of f (their rule for a 2x grid: W = log10(1/eps) + 1).
+// Comput. 41 (2019) C479).  With W = 8, beta = 2.3 W the interpolation error is
+// about 1e-7 of the l2 norm of f (their rule for a 2x grid: W = log10(1/eps) + 1;
+// W = 7 was measured too coarse for 16-station arrays, whose solve averages little).
 // Per (row, direction) the work is W + 1 complex multiply-adds instead of C, so the
 // direction count no longer multiplies the channel work; the channel work moves to
 // the tensor cores.
@@ -40,7 +41,7 @@
 // other), IS (segments 1.. of the current tile), AC (corrections).  Column 2j of
 // a region holds sum V_s Re E at window grid point j, column 2j + 1 sum V_s Im E
 // (the grid matrix interleaves its re and im rows), so the W + 1 taps of one
-// stencil are 2 (W + 1) = 16 adjacent columns: one 16-column tcgen05.ld.
+// stencil are 2 (W + 1) = 18 adjacent columns: a 16- and a 2-column tcgen05.ld.
 //
 // Warp roles (14 warps): 0 = TMA producer, 1 = MMA issuer (+ TMEM owner), 2-5 =
 // converters (split the visibility box into K-major hi/lo blocks, and fold the
@@ -57,8 +58,8 @@
 
 namespace leapgb {
 
-constexpr int kGrTaps = 7;            // W, grid points per interpolation
-constexpr float kGrBeta = 16.1f;      // 2.3 W
+constexpr int kGrTaps = 8;            // W, grid points per interpolation
+constexpr float kGrBeta = 18.4f;      // 2.3 W
 constexpr int kGrChunk = 16;          // channels per stage
 constexpr int kGrSegChunks = 4;       // chunks per hi*hi accumulation segment (64 channels)
 constexpr int kGrStages = 6;          // {visibility box / A hi, A lo, E window} ring
@@ -66,7 +67,7 @@ constexpr int kGrMacro = 2;           // chunks handed over per barrier round (s
 constexpr int kGrMacroStages = kGrStages / kGrMacro;
 constexpr int kGrJwMax = 64;          // grid points per pass (MMA N = 2 Jw <= 128)
 constexpr int kGrPassStride = 56;     // grid points between pass windows (multiple of 8)
-constexpr int kGrLoadCols = 8;        // grid points one interpolation load reads (2 TMEM columns each)
+constexpr int kGrLoadCols = 9;        // grid points one interpolation load reads (2 TMEM columns each)
 constexpr int kGrBatch = 4;           // directions whose loads share one tcgen05.wait::ld
 constexpr int kGrDirs = 64;           // directions per unit (8 epilogue warps x 32 / 4 quarters)
 constexpr int kGrEpiWarps = 8;
@@ -133,8 +134,10 @@ struct GridParams {
   int32_t nslots, nitems, units, nbl;
 };
 
+// A unit: one quad of baselines over one timestep slab, for every direction of its item
+// (the grid product of a tile serves all of them).
 struct GridUnit {
-  int item, quad, dg, slab, t_lo, t_hi, ntb;
+  int item, quad, slab, t_lo, t_hi, ntb;
 };
 
 __device__ __forceinline__ int grid_find_item(const GridItem* items, int nitems, int u) {
@@ -152,8 +155,7 @@ __device__ __forceinline__ GridUnit grid_unit(const GridParams& p, int u) {
   g.item = grid_find_item(p.items, p.nitems, u);
   const GridItem& I = p.items[g.item];
   const int l = u - I.unit_begin;
-  g.quad = l / (I.dgroups * I.nslab);
-  g.dg = (l / I.nslab) % I.dgroups;
+  g.quad = l / I.nslab;
   g.slab = l % I.nslab;
   g.t_lo = g.slab * I.tb_per_slab * 4;
   g.t_hi = min(I.T, g.t_lo + I.tb_per_slab * 4);
@@ -170,12 +172,11 @@ __device__ __forceinline__ int grid_position(uint32_t pb, int n, float& f) {
   return static_cast<int>(prod >> 32);
 }
 
-// First grid point of the W-point stencil (W odd) around x = i0 + f: the points within
-// W/2 of x are round(x) - (W-1)/2 .. round(x) + (W-1)/2.
-static_assert(kGrTaps % 2 == 1, "the stencil start rounds x for odd W");
-__device__ __forceinline__ int grid_stencil_start(int i0, float f) {
-  return i0 - (kGrTaps - 1) / 2 + (f >= 0.5f ? 1 : 0);
-}
+// First grid point of the W-point stencil (W even) around x = i0 + f: the points within
+// W/2 of x are i0 - W/2 + 1 .. i0 + W/2.  A load reads W + 1 points from the earliest
+// start of a quarter's 4 timesteps, which covers starts that differ by one.
+static_assert(kGrTaps % 2 == 0, "the stencil start is floor(x) - W/2 + 1 for even W");
+__device__ __forceinline__ int grid_stencil_start(int i0, float) { return i0 - kGrTaps / 2 + 1; }
 
 __device__ __forceinline__ void tma_load_3d(void* smem_dst, const CUtensorMap* map, int x, int y, int z, uint64_t* bar) {
   asm volatile(
@@ -209,38 +210,40 @@ static __global__ void grid_windows(const GridParams p) {
   const GridUnit g = grid_unit(p, u);
   const GridItem& I = p.items[g.item];
   const int n = 2 * I.C;
-  const int nd = min(kGrDirs, I.ndir - g.dg * kGrDirs);
-  // Lanes hold the slopes of directions lane and lane + 32 and walk the unit's rows;
-  // a row's UVWs are one broadcast load for the warp.
-  static_assert(kGrDirs == 64, "two directions per lane");
-  float kb[2][6];
-  bool has[2];
-#pragma unroll
-  for (int h = 0; h < 2; ++h) {
-    const int dj = lane + 32 * h;
-    has[h] = dj < nd;
-    const int d = I.dir0 + g.dg * kGrDirs + min(dj, nd - 1);
-#pragma unroll
-    for (int i = 0; i < 6; ++i) kb[h][i] = __ldg(p.dirk + 12 * d + 6 + i);
-  }
   int smin = 0x7fffffff, smax = -0x7fffffff;
-  for (int t = g.t_lo; t < g.t_hi; ++t) {
+  // Every direction group of the item: lanes hold the slopes of directions lane and
+  // lane + 32 of the group and walk the unit's rows; a row's UVWs are one broadcast load.
+  static_assert(kGrDirs == 64, "two directions per lane");
+  for (int dg = 0; dg < I.dgroups; ++dg) {
+    const int nd = min(kGrDirs, I.ndir - dg * kGrDirs);
+    float kb[2][6];
+    bool has[2];
 #pragma unroll
-    for (int q = 0; q < 4; ++q) {
-      const int b = g.quad * 4 + q;
-      if (b >= p.nbl) continue;
-      const int64_t r = static_cast<int64_t>(t) * p.nbl + b;
-      float x[6];
+    for (int h = 0; h < 2; ++h) {
+      const int dj = lane + 32 * h;
+      has[h] = dj < nd;
+      const int d = I.dir0 + dg * kGrDirs + min(dj, nd - 1);
 #pragma unroll
-      for (int i = 0; i < 6; ++i) x[i] = __ldg(I.uvw_f + 6 * r + i);
+      for (int i = 0; i < 6; ++i) kb[h][i] = __ldg(p.dirk + 12 * d + 6 + i);
+    }
+    for (int t = g.t_lo; t < g.t_hi; ++t) {
 #pragma unroll
-      for (int h = 0; h < 2; ++h) {
-        if (!has[h]) continue;
-        float f;
-        const int i0 = grid_position(df_dot3_turns_u32(kb[h], x), n, f);
-        const int s = grid_stencil_start(i0, f);
-        smin = min(smin, s);
-        smax = max(smax, s);
+      for (int q = 0; q < 4; ++q) {
+        const int b = g.quad * 4 + q;
+        if (b >= p.nbl) continue;
+        const int64_t r = static_cast<int64_t>(t) * p.nbl + b;
+        float x[6];
+#pragma unroll
+        for (int i = 0; i < 6; ++i) x[i] = __ldg(I.uvw_f + 6 * r + i);
+#pragma unroll
+        for (int h = 0; h < 2; ++h) {
+          if (!has[h]) continue;
+          float f;
+          const int i0 = grid_position(df_dot3_turns_u32(kb[h], x), n, f);
+          const int s = grid_stencil_start(i0, f);
+          smin = min(smin, s);
+          smax = max(smax, s);
+        }
       }
     }
   }
@@ -282,40 +285,48 @@ __device__ __forceinline__ void grid_weights(float y, float (&w)[W + 1]) {
   }
 }
 
-// kGrBatch directions' stencils from TMEM: one 16-column load each (the W + 1 taps,
-// re and im interleaved) at columns col[b] of this warp's lanes, and one wait for all.
+// kGrBatch directions' stencils from TMEM: a 16- and a 2-column load each (the W + 1
+// taps, re and im interleaved) at columns col[b] of this warp's lanes, and one wait for all.
 __device__ __forceinline__ void grid_load_batch(uint32_t tbase, const uint32_t (&col)[kGrBatch],
-                                                uint32_t (&v)[kGrBatch][16]) {
-  static_assert(kGrBatch == 4 && kGrLoadCols == 8, "four 16-column loads per batch");
+                                                uint32_t (&v)[kGrBatch][18]) {
+  static_assert(kGrBatch == 4 && kGrLoadCols == 9, "four 18-column loads per batch");
   // All loads and the wait in one statement: the results are defined only after the wait.
   asm volatile(
-      "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%64];\n\t"
-      "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%16,%17,%18,%19,%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31}, [%65];\n\t"
-      "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%32,%33,%34,%35,%36,%37,%38,%39,%40,%41,%42,%43,%44,%45,%46,%47}, [%66];\n\t"
-      "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%48,%49,%50,%51,%52,%53,%54,%55,%56,%57,%58,%59,%60,%61,%62,%63}, [%67];\n\t"
+      "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%72];\n\t"
+      "tcgen05.ld.sync.aligned.32x32b.x2.b32 {%16,%17}, [%73];\n\t"
+      "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%18,%19,%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31,%32,%33}, [%74];\n\t"
+      "tcgen05.ld.sync.aligned.32x32b.x2.b32 {%34,%35}, [%75];\n\t"
+      "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%36,%37,%38,%39,%40,%41,%42,%43,%44,%45,%46,%47,%48,%49,%50,%51}, [%76];\n\t"
+      "tcgen05.ld.sync.aligned.32x32b.x2.b32 {%52,%53}, [%77];\n\t"
+      "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%54,%55,%56,%57,%58,%59,%60,%61,%62,%63,%64,%65,%66,%67,%68,%69}, [%78];\n\t"
+      "tcgen05.ld.sync.aligned.32x32b.x2.b32 {%70,%71}, [%79];\n\t"
       "tcgen05.wait::ld.sync.aligned;"
       : "=r"(v[0][0]), "=r"(v[0][1]), "=r"(v[0][2]), "=r"(v[0][3]), "=r"(v[0][4]), "=r"(v[0][5]), "=r"(v[0][6]),
         "=r"(v[0][7]), "=r"(v[0][8]), "=r"(v[0][9]), "=r"(v[0][10]), "=r"(v[0][11]), "=r"(v[0][12]), "=r"(v[0][13]),
-        "=r"(v[0][14]), "=r"(v[0][15]), "=r"(v[1][0]), "=r"(v[1][1]), "=r"(v[1][2]), "=r"(v[1][3]), "=r"(v[1][4]),
-        "=r"(v[1][5]), "=r"(v[1][6]), "=r"(v[1][7]), "=r"(v[1][8]), "=r"(v[1][9]), "=r"(v[1][10]), "=r"(v[1][11]),
-        "=r"(v[1][12]), "=r"(v[1][13]), "=r"(v[1][14]), "=r"(v[1][15]), "=r"(v[2][0]), "=r"(v[2][1]), "=r"(v[2][2]),
-        "=r"(v[2][3]), "=r"(v[2][4]), "=r"(v[2][5]), "=r"(v[2][6]), "=r"(v[2][7]), "=r"(v[2][8]), "=r"(v[2][9]),
-        "=r"(v[2][10]), "=r"(v[2][11]), "=r"(v[2][12]), "=r"(v[2][13]), "=r"(v[2][14]), "=r"(v[2][15]), "=r"(v[3][0]),
-        "=r"(v[3][1]), "=r"(v[3][2]), "=r"(v[3][3]), "=r"(v[3][4]), "=r"(v[3][5]), "=r"(v[3][6]), "=r"(v[3][7]),
-        "=r"(v[3][8]), "=r"(v[3][9]), "=r"(v[3][10]), "=r"(v[3][11]), "=r"(v[3][12]), "=r"(v[3][13]), "=r"(v[3][14]),
-        "=r"(v[3][15])
-      : "r"(tbase + col[0]), "r"(tbase + col[1]), "r"(tbase + col[2]), "r"(tbase + col[3]));
+        "=r"(v[0][14]), "=r"(v[0][15]), "=r"(v[0][16]), "=r"(v[0][17]),
+        "=r"(v[1][0]), "=r"(v[1][1]), "=r"(v[1][2]), "=r"(v[1][3]), "=r"(v[1][4]), "=r"(v[1][5]), "=r"(v[1][6]),
+        "=r"(v[1][7]), "=r"(v[1][8]), "=r"(v[1][9]), "=r"(v[1][10]), "=r"(v[1][11]), "=r"(v[1][12]), "=r"(v[1][13]),
+        "=r"(v[1][14]), "=r"(v[1][15]), "=r"(v[1][16]), "=r"(v[1][17]),
+        "=r"(v[2][0]), "=r"(v[2][1]), "=r"(v[2][2]), "=r"(v[2][3]), "=r"(v[2][4]), "=r"(v[2][5]), "=r"(v[2][6]),
+        "=r"(v[2][7]), "=r"(v[2][8]), "=r"(v[2][9]), "=r"(v[2][10]), "=r"(v[2][11]), "=r"(v[2][12]), "=r"(v[2][13]),
+        "=r"(v[2][14]), "=r"(v[2][15]), "=r"(v[2][16]), "=r"(v[2][17]),
+        "=r"(v[3][0]), "=r"(v[3][1]), "=r"(v[3][2]), "=r"(v[3][3]), "=r"(v[3][4]), "=r"(v[3][5]), "=r"(v[3][6]),
+        "=r"(v[3][7]), "=r"(v[3][8]), "=r"(v[3][9]), "=r"(v[3][10]), "=r"(v[3][11]), "=r"(v[3][12]), "=r"(v[3][13]),
+        "=r"(v[3][14]), "=r"(v[3][15]), "=r"(v[3][16]), "=r"(v[3][17])
+      : "r"(tbase + col[0]), "r"(tbase + col[0] + 16u), "r"(tbase + col[1]), "r"(tbase + col[1] + 16u),
+        "r"(tbase + col[2]), "r"(tbase + col[2] + 16u), "r"(tbase + col[3]), "r"(tbase + col[3] + 16u));
 }
 
 // One direction of one lane: the W + 1 taps v (re, im interleaved) weighted by the
 // lane's record (weights, then the rotation (cr, sr)), combined with the partner
 // lane's component, rotated; returns this lane's component of the rotated sum.
 template <int W>
-__device__ __forceinline__ float grid_tap_combine(const uint32_t (&v)[16], const float* rec, int comp) {
-  static_assert(W + 1 == 8, "record layout: 8 weights, then cr, sr, code");
+__device__ __forceinline__ float grid_tap_combine(const uint32_t (&v)[18], const float* rec, int comp) {
+  static_assert(W + 1 == 9, "record layout: 9 weights, then cr, sr, code");
   const float4 q0 = reinterpret_cast<const float4*>(rec)[0], q1 = reinterpret_cast<const float4*>(rec)[1];
-  const float2 rot = reinterpret_cast<const float2*>(rec)[4];
-  const float w[8] = {q0.x, q0.y, q0.z, q0.w, q1.x, q1.y, q1.z, q1.w};
+  const float4 q2 = reinterpret_cast<const float4*>(rec)[2];
+  const float2 rot = make_float2(q2.y, q2.z);
+  const float w[9] = {q0.x, q0.y, q0.z, q0.w, q1.x, q1.y, q1.z, q1.w, q2.x};
   float P = 0.f, Q = 0.f;
 #pragma unroll
   for (int k = 0; k <= W; ++k) {
@@ -337,15 +348,18 @@ __device__ __noinline__ float grid_wide_sum(const float* rec_dir, uint32_t tbase
   float acc = 0.f;
   for (int tt = 0; tt < 4; ++tt) {
     const float* r = rec_dir + tt * 8 * kGrRecWords;
-    const int ct = __float_as_int(r[10]);
+    const int ct = __float_as_int(r[11]);
     if ((ct & 0xFFFF) == 0xFFFF || ((ct >> 8) & 255) != pp) continue;  // same in every lane
-    uint32_t v[16];
+    uint32_t v[18];
+    const uint32_t a0 = tbase + 2u * static_cast<uint32_t>(ct & 255);
     asm volatile(
-        "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];\n\t"
+        "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%18];\n\t"
+        "tcgen05.ld.sync.aligned.32x32b.x2.b32 {%16,%17}, [%19];\n\t"
         "tcgen05.wait::ld.sync.aligned;"
         : "=r"(v[0]), "=r"(v[1]), "=r"(v[2]), "=r"(v[3]), "=r"(v[4]), "=r"(v[5]), "=r"(v[6]), "=r"(v[7]), "=r"(v[8]),
-          "=r"(v[9]), "=r"(v[10]), "=r"(v[11]), "=r"(v[12]), "=r"(v[13]), "=r"(v[14]), "=r"(v[15])
-        : "r"(tbase + 2u * static_cast<uint32_t>(ct & 255)));
+          "=r"(v[9]), "=r"(v[10]), "=r"(v[11]), "=r"(v[12]), "=r"(v[13]), "=r"(v[14]), "=r"(v[15]), "=r"(v[16]),
+          "=r"(v[17])
+        : "r"(a0), "r"(a0 + 16u));
     const float g = grid_tap_combine<W>(v, r, comp);
     if (tl == tt) acc += g;
   }
@@ -428,6 +442,22 @@ __device__ __forceinline__ void grid_mma_hihi(uint32_t d, uint64_t ah, uint64_t 
 __device__ __forceinline__ void tc_commit(uint64_t* bar) {
   asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(smem_u32(bar))
                : "memory");
+}
+
+// Sum a warp's per-lane sums over the 4 timesteps of its quad lanes and store them
+// (first) or add them to the unit's output: directions dbase .. dbase + nd of the item,
+// out[direction][pol][nbl] complex doubles.  Each output element has one writer lane.
+__device__ __forceinline__ void grid_flush(const float (&acc)[kGrWarpDirs], double2* out, int dbase, int nd, int b,
+                                           bool bval, int tl, int ps, int comp, int nbl, bool first) {
+#pragma unroll
+  for (int j = 0; j < kGrWarpDirs; ++j) {
+    float v = acc[j] + __shfl_xor_sync(0xffffffffu, acc[j], 8);
+    v += __shfl_xor_sync(0xffffffffu, v, 16);
+    if (tl == 0 && bval && j < nd) {
+      double* o = reinterpret_cast<double*>(out + (static_cast<int64_t>(dbase + j) * 4 + (ps >> 1)) * nbl + b);
+      o[comp] = first ? static_cast<double>(v) : o[comp] + static_cast<double>(v);
+    }
+  }
 }
 
 template <int W>
@@ -728,10 +758,13 @@ __global__ void __launch_bounds__(kGrThreads, 1) rotate_average_gridded(const Gr
       if (w.npass == 0) continue;
       const int n = 2 * I.C, c0 = I.C / 2;
       const int r0 = w.rg0 * 8;
-      const int dbase = g.dg * kGrDirs + half * kGrWarpDirs;  // item-relative first direction of this warp
-      const int nd = max(0, min(kGrWarpDirs, I.ndir - dbase));
       const int b = g.quad * 4 + quarter;
       const bool bval = b < p.nbl;
+      double2* out = I.out + static_cast<int64_t>(I.nslab > 1 ? g.slab : 0) * I.ndir * 4 * p.nbl;
+      // With one direction group the warp's sums stay in registers over the unit's tiles and
+      // passes; with several, each (tile, pass, group) adds its sums to the unit's output in
+      // order (the first stores), since every group's sums do not fit in registers.
+      const bool keep = I.dgroups == 1;
       float acc[kGrWarpDirs];
 #pragma unroll
       for (int j = 0; j < kGrWarpDirs; ++j) acc[j] = 0.f;
@@ -751,6 +784,13 @@ __global__ void __launch_bounds__(kGrThreads, 1) rotate_average_gridded(const Gr
           }
           asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
           const uint32_t tbase = tmem + (static_cast<uint32_t>(quarter * 32) << 16) + rb * kGrRegion;
+          for (int dg = 0; dg < I.dgroups; ++dg) {
+          const int dbase = dg * kGrDirs + half * kGrWarpDirs;  // item-relative first direction of this warp
+          const int nd = max(0, min(kGrWarpDirs, I.ndir - dbase));
+          if (!keep) {
+#pragma unroll
+            for (int j = 0; j < kGrWarpDirs; ++j) acc[j] = 0.f;
+          }
 #pragma unroll
           for (int gi = 0; gi < kGrWarpDirs / 8; ++gi) {
             if (gi * 8 >= nd) break;
@@ -794,11 +834,11 @@ __global__ void __launch_bounds__(kGrThreads, 1) rotate_average_gridded(const Gr
               grid_weights<W>(any ? static_cast<float>(i0 - base) + f : 0.f, wt);
               float cr, sr;
               twiddle_turns(pa + static_cast<uint32_t>(c0) * pb, tab, cr, sr);
-              // Record: weights 0-7, then cr, sr, code.
+              // Record: weights 0-8, then cr, sr, code.
               float4* my = reinterpret_cast<float4*>(rec + (tl * 8 + ps) * kGrRecWords);
               my[0] = make_float4(wt[0], wt[1], wt[2], wt[3]);
               my[1] = make_float4(wt[4], wt[5], wt[6], wt[7]);
-              my[2] = make_float4(cr, sr, __int_as_float(code), 0.f);
+              my[2] = make_float4(wt[8], cr, sr, __int_as_float(code));
             }
             __syncwarp();
 #pragma unroll
@@ -809,13 +849,13 @@ __global__ void __launch_bounds__(kGrThreads, 1) rotate_average_gridded(const Gr
               int live = 0;
 #pragma unroll
               for (int bb = 0; bb < kGrBatch; ++bb) {
-                const int code = __float_as_int(rec[(tl * 8 + jb + bb) * kGrRecWords + 10]);
+                const int code = __float_as_int(rec[(tl * 8 + jb + bb) * kGrRecWords + 11]);
                 const bool use = code >= 0 && !(code & kGrWide) && ((code >> 8) & 255) == pp;
                 col[bb] = use ? 2u * static_cast<uint32_t>(code & 255) : 0u;
                 live |= (use ? 1 : 0) << bb;
               }
               if (live) {
-                uint32_t v[kGrBatch][16];
+                uint32_t v[kGrBatch][18];
                 grid_load_batch(tbase, col, v);
 #pragma unroll
                 for (int bb = 0; bb < kGrBatch; ++bb)
@@ -824,12 +864,14 @@ __global__ void __launch_bounds__(kGrThreads, 1) rotate_average_gridded(const Gr
               }
 #pragma unroll
               for (int bb = 0; bb < kGrBatch; ++bb) {
-                const int code = __float_as_int(rec[(tl * 8 + jb + bb) * kGrRecWords + 10]);
+                const int code = __float_as_int(rec[(tl * 8 + jb + bb) * kGrRecWords + 11]);
                 if (code >= 0 && (code & kGrWide))  // the kGrWide bit is the same in every lane
                   acc[gi * 8 + jb + bb] += grid_wide_sum<W>(rec + (jb + bb) * kGrRecWords, tbase, comp, tl, pp);
               }
             }
             __syncwarp();
+          }
+          if (!keep) grid_flush(acc, out, dbase, nd, b, bval, tl, ps, comp, p.nbl, tb == 0 && pp == 0);
           }
           asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
           __syncwarp();
@@ -837,17 +879,8 @@ __global__ void __launch_bounds__(kGrThreads, 1) rotate_average_gridded(const Gr
         }
       }
       if (!ok) break;
-      // Sum the 4 timesteps of the quad's lanes and write this unit's sums.
-      double2* out = I.out + static_cast<int64_t>(I.nslab > 1 ? g.slab : 0) * I.ndir * 4 * p.nbl;
-#pragma unroll
-      for (int j = 0; j < kGrWarpDirs; ++j) {
-        float v = acc[j] + __shfl_xor_sync(0xffffffffu, acc[j], 8);
-        v += __shfl_xor_sync(0xffffffffu, v, 16);
-        if (tl == 0 && bval && j < nd) {
-          double* o = reinterpret_cast<double*>(out + (static_cast<int64_t>(dbase + j) * 4 + (ps >> 1)) * p.nbl + b);
-          o[comp] = static_cast<double>(v);
-        }
-      }
+      if (keep) grid_flush(acc, out, half * kGrWarpDirs, max(0, min(kGrWarpDirs, I.ndir - half * kGrWarpDirs)), b,
+                           bval, tl, ps, comp, p.nbl, true);
     }
   }
   asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");

@@ -28,6 +28,7 @@ struct RotateArgs {
   const double* uvw;        // [rows][3]
   const double* dd;         // [ndir][9] row-major direction matrices
   const double* lambda;     // [channels] c / (f0 + ch*df), as the reference computes it
+  const double* inv_lambda; // [channels] 1 / lambda, rounded (all-FP64 form)
   const float2* twiddle;    // [kTwiddleSize] (cos, sin) table for the mixed form
   const float* uvw_f;       // [rows][6] (u, v, w) as (hi, lo) float pairs
   const float* dirk;        // [ndir][12] phase constants as (hi, lo) pairs: -(l, m, n-1)*f0/c, -(l, m, n-1)*df/c
@@ -60,12 +61,24 @@ __device__ __forceinline__ void load_sample_f(const VisT* __restrict__ p, float&
 // ---------------------------------------------------------------------------
 // All-FP64 form.  Lanes own baselines, a warp owns DPW directions, a block's
 // warps share one baseline tile (so the visibility loads of one warp hit L1
-// for the others).  The reference phase is shiftRad(c) = shiftFactor / lambda_c
-// = shiftFactor * (f0 + c*df) / c_light, linear in the channel index, so
-// exp(i*shiftRad) is advanced channel to channel by one complex multiply with
-// exp(i*shiftFactor*df/c_light) and re-seeded with an exact FP64 sincos every
-// kSeed channels (drift below 1e-14 rad).  FP64 sincos runs at about 1/25 of
-// the DFMA rate on GB300, so this removes it from the inner loop.
+// for the others).  The reference phase is shiftRad(c) = fl(shiftFactor /
+// lambda_c) (CpuLeapCalibrator.cc:190-198), nearly linear in the channel index,
+// so exp(i*shiftRad) is advanced channel to channel by one complex multiply with
+// exp(i*shiftFactor*df/c_light) and re-seeded with an FP64 sincos every kSeed
+// channels.  FP64 sincos runs at about 1/25 of the DFMA rate on GB300, so this
+// removes it from the inner loop.
+//
+// The reference's own rounding matters here.  Its argument reaches thousands of
+// radians for directions ~1 rad from the phase centre, where one unit in the last
+// place is ~1e-12 rad, and lambda_c's rounding is the same for every row; the
+// solve then moves the cal phases by ~5e-11 rad between two equally valid FP64
+// roundings of the argument (shiftFactor * (1 / lambda_c) against shiftFactor /
+// lambda_c).  So each channel's twiddle is corrected to the reference's own
+// argument: fl(shiftFactor / lambda_c) from the rounded reciprocal and one
+// FMA-exact remainder step (the correctly rounded quotient), minus the
+// recurrence's phase seed + k * step, applied to first order (the difference is
+// below 1e-11 rad, so its square is far below rounding).  shiftFactor itself is
+// formed without fused operations, as the reference's expression is.
 // ---------------------------------------------------------------------------
 // kCheckNan: skip (row, channel) groups with a NaN in any pol inside the kernel
 // (for callers whose visibilities did not go through the ingestion sanitiser).
@@ -104,19 +117,26 @@ __global__ void __launch_bounds__(128) rotate_average_fp64(RotateArgs a) {
     for (int t = t_lo; t < t_hi; ++t) {
       const int64_t r = static_cast<int64_t>(t) * a.nbl + b;
       const double u = __ldg(a.uvw + 3 * r), v = __ldg(a.uvw + 3 * r + 1), w = __ldg(a.uvw + 3 * r + 2);
-      double sf[DPW], wr[DPW], wi[DPW];
+      double sf[DPW], st[DPW], wr[DPW], wi[DPW];
 #pragma unroll
       for (int j = 0; j < DPW; ++j) {
-        const double wrot = dd2[j][0] * u + dd2[j][1] * v + dd2[j][2] * w;
-        sf[j] = -kTwoPi * (wrot - w);
-        sincos(sf[j] * (a.df * inv_c), &wi[j], &wr[j]);
+        const double wrot =
+            __dadd_rn(__dadd_rn(__dmul_rn(dd2[j][0], u), __dmul_rn(dd2[j][1], v)), __dmul_rn(dd2[j][2], w));
+        sf[j] = __dmul_rn(-kTwoPi, __dadd_rn(wrot, -w));
+        st[j] = sf[j] * (a.df * inv_c);
+        sincos(st[j], &wi[j], &wr[j]);
       }
       for (int cb = c_lo; cb < c_hi; cb += kSeed) {
         const int ce = min(c_hi, cb + kSeed);
-        double zr[DPW], zi[DPW];
+        double zr[DPW], zi[DPW], seed[DPW];
 #pragma unroll
-        for (int j = 0; j < DPW; ++j) sincos(sf[j] / __ldg(a.lambda + cb), &zi[j], &zr[j]);
+        for (int j = 0; j < DPW; ++j) {
+          seed[j] = sf[j] / __ldg(a.lambda + cb);
+          sincos(seed[j], &zi[j], &zr[j]);
+        }
         for (int c = cb; c < ce; ++c) {
+          const double lam = __ldg(a.lambda + c), rlam = __ldg(a.inv_lambda + c);
+          const double k = static_cast<double>(c - cb);
           const VisT* src = vis + (static_cast<int64_t>(c) * a.rows + r) * P;
           double vr[P], vi[P];
 #pragma unroll
@@ -132,10 +152,15 @@ __global__ void __launch_bounds__(128) rotate_average_fp64(RotateArgs a) {
           }
 #pragma unroll
           for (int j = 0; j < DPW; ++j) {
+            // The reference's argument fl(sf / lambda_c), and its difference from seed + k * step.
+            const double q = sf[j] * rlam;
+            const double arg = fma(fma(-q, lam, sf[j]), rlam, q);
+            const double dlt = fma(-k, st[j], arg - seed[j]);
+            const double tr = fma(-dlt, zi[j], zr[j]), ti = fma(dlt, zr[j], zi[j]);
 #pragma unroll
             for (int p = 0; p < P; ++p) {
-              accr[j][p] += vr[p] * zr[j] - vi[p] * zi[j];
-              acci[j][p] += vr[p] * zi[j] + vi[p] * zr[j];
+              accr[j][p] += vr[p] * tr - vi[p] * ti;
+              acci[j][p] += vr[p] * ti + vi[p] * tr;
             }
             const double nr = zr[j] * wr[j] - zi[j] * wi[j];
             zi[j] = zr[j] * wi[j] + zi[j] * wr[j];

@@ -301,8 +301,9 @@ int gridded_stage(leap_ctx* ctx, const std::vector<WorkItem>& items, const doubl
   std::vector<ReduceItem>& red = ctx->reduce_items_host;
   git.assign(items.size(), GridItem{});
   red.clear();
+  // A unit is a quad of baselines over a timestep slab, for all of its item's directions.
   int64_t base_units = 0;
-  for (const auto& w : items) base_units += static_cast<int64_t>(nquad) * ((w.ndir + kGrDirs - 1) / kGrDirs);
+  for (size_t i = 0; i < items.size(); ++i) base_units += nquad;
   // Timestep slabs only when the (quad, direction group) units alone would leave blocks idle.
   const int64_t want_slabs = std::max<int64_t>(1, (4 * static_cast<int64_t>(ctx->sms) + base_units - 1) / base_units);
   int units = 0;
@@ -334,17 +335,20 @@ int gridded_stage(leap_ctx* ctx, const std::vector<WorkItem>& items, const doubl
     it.C = C;
     it.nchunk = grid_chunks(C);
     const int ntb = (T + 3) / 4;
-    const int nslab_want = static_cast<int>(std::min<int64_t>(ntb, want_slabs));
+    it.dgroups = (w.ndir + kGrDirs - 1) / kGrDirs;
+    // With several direction groups the epilogue cannot hold every group's sums across a
+    // unit's tiles, so a unit is one tile (a slab per timestep block) and its sums are
+    // stored once; the fixed-order slab reduction adds the tiles.
+    const int nslab_want = it.dgroups > 1 ? ntb : static_cast<int>(std::min<int64_t>(ntb, want_slabs));
     it.tb_per_slab = (ntb + nslab_want - 1) / nslab_want;
     it.nslab = (ntb + it.tb_per_slab - 1) / it.tb_per_slab;
     it.nquad = nquad;
-    it.dgroups = (w.ndir + kGrDirs - 1) / kGrDirs;
     it.dir0 = w.dir0;
     it.ndir = w.ndir;
     it.unit_begin = units;
     it.nrg = grid_rows(C) / 8;
     it.lbase = grid_lbase(C);
-    units += it.nquad * it.dgroups * it.nslab;
+    units += it.nquad * it.nslab;
     if (it.nslab > 1) {
       partial_off[i] = partial_elems;
       partial_elems += static_cast<int64_t>(it.nslab) * w.ndir * 4 * nbl;
@@ -367,11 +371,12 @@ int gridded_stage(leap_ctx* ctx, const std::vector<WorkItem>& items, const doubl
     std::vector<std::pair<int64_t, int>> cost;
     cost.reserve(units);
     for (const GridItem& it : git) {
-      const int per_item = it.nquad * it.dgroups * it.nslab;
+      const int per_item = it.nquad * it.nslab;
       for (int l = 0; l < per_item; ++l) {
         const int slab = l % it.nslab;
         const int t_lo = slab * it.tb_per_slab * 4, t_hi = std::min(it.T, t_lo + it.tb_per_slab * 4);
-        cost.emplace_back(-static_cast<int64_t>((t_hi - t_lo + 3) / 4) * (it.nchunk + 2), it.unit_begin + l);
+        cost.emplace_back(-static_cast<int64_t>((t_hi - t_lo + 3) / 4) * (it.nchunk + 2 * it.dgroups),
+                          it.unit_begin + l);
       }
     }
     std::stable_sort(cost.begin(), cost.end());
@@ -473,14 +478,22 @@ int rotate_stage(leap_ctx* ctx, const std::vector<WorkItem>& items, const double
   }
   // Channel wavelengths, computed exactly as Constants::GetChannelWavelength does;
   // uploaded only when the channel count or the spectral window changes.
-  LEAP_CUDA(ctx->lambda.ensure(sizeof(double) * maxC), "alloc wavelengths");
-  if (ctx->lambda_host.size() != static_cast<size_t>(maxC) || ctx->lambda_f0 != md.k.freq_start_hz ||
+  LEAP_CUDA(ctx->lambda.ensure(sizeof(double) * 2 * maxC), "alloc wavelengths");
+  if (ctx->lambda_host.size() != static_cast<size_t>(2 * maxC) || ctx->lambda_f0 != md.k.freq_start_hz ||
       ctx->lambda_df != md.k.freq_inc_hz) {
-    ctx->lambda_host.resize(maxC);
-    for (int c = 0; c < maxC; ++c) ctx->lambda_host[c] = kSpeedOfLight / (md.k.freq_start_hz + c * md.k.freq_inc_hz);
+    // [wavelengths][their reciprocals]: c / (f0 + ch*df) with each operation rounded on its own,
+    // as the reference's Constants::GetChannelWavelength (no fused multiply-add).
+    ctx->lambda_host.resize(2 * maxC);
+    for (int c = 0; c < maxC; ++c) {
+      volatile double prod = static_cast<double>(c) * md.k.freq_inc_hz;
+      const double lam = kSpeedOfLight / (md.k.freq_start_hz + prod);
+      ctx->lambda_host[c] = lam;
+      ctx->lambda_host[maxC + c] = 1.0 / lam;
+    }
     ctx->lambda_f0 = md.k.freq_start_hz;
     ctx->lambda_df = md.k.freq_inc_hz;
-    LEAP_CUDA(cudaMemcpyAsync(ctx->lambda.ptr, ctx->lambda_host.data(), sizeof(double) * maxC, cudaMemcpyHostToDevice, s),
+    LEAP_CUDA(cudaMemcpyAsync(ctx->lambda.ptr, ctx->lambda_host.data(), sizeof(double) * 2 * maxC,
+                              cudaMemcpyHostToDevice, s),
               "upload wavelengths");
   }
 
@@ -669,6 +682,7 @@ int rotate_stage(leap_ctx* ctx, const std::vector<WorkItem>& items, const double
     ra.uvw = in.uvw.as<double>();
     ra.dd = d_dd + 9 * static_cast<int64_t>(w.dir0);
     ra.lambda = ctx->lambda.as<double>();
+    ra.inv_lambda = ctx->lambda.as<double>() + ctx->lambda_host.size() / 2;
     ra.twiddle = ctx->twiddle.as<float2>();
     ra.rows = in.rows;
     ra.channels = C;
@@ -742,6 +756,7 @@ int refant_stage(leap_ctx* ctx, const std::vector<WorkItem>& items, const double
       rr.uvw = in.uvw.as<double>();
       rr.dd = d_dd + 9 * static_cast<int64_t>(w.dir0);
       rr.lambda = ctx->lambda.as<double>();
+      rr.inv_lambda = ctx->lambda.as<double>() + ctx->lambda_host.size() / 2;
       rr.rows = in.rows;
       rr.channels = in.channels;
       rr.pols = in.pols;

@@ -63,10 +63,14 @@ unsigned long long current_context_id() {
 }
 
 // Wavelengths of the channels, formed as the reference's
-// Constants::GetChannelWavelength does: c / (f0 + ch*df), no fused multiply-add.
+// Constants::GetChannelWavelength does: c / (f0 + ch*df), no fused multiply-add;
+// then their rounded reciprocals (lam[channels + c]).
 __global__ void fill_wavelengths(double* lam, int channels, double f0, double df) {
-  for (int c = blockIdx.x * blockDim.x + threadIdx.x; c < channels; c += gridDim.x * blockDim.x)
-    lam[c] = __ddiv_rn(kSpeedOfLight, __dadd_rn(f0, __dmul_rn(static_cast<double>(c), df)));
+  for (int c = blockIdx.x * blockDim.x + threadIdx.x; c < channels; c += gridDim.x * blockDim.x) {
+    const double l = __ddiv_rn(kSpeedOfLight, __dadd_rn(f0, __dmul_rn(static_cast<double>(c), df)));
+    lam[c] = l;
+    lam[channels + c] = __drcp_rn(l);
+  }
 }
 
 // Launches through cudaLaunchKernelEx, whose return value is this launch's own status:
@@ -128,8 +132,8 @@ extern "C" int32_t leap_rotate_average_noalloc(int32_t vis_type, const void* vis
     sms = st.sms;
   }
 
-  // Scratch layout: [wavelengths, 256-byte aligned][slab partial sums].
-  const size_t lam_bytes = ((sizeof(double) * static_cast<size_t>(channels) + 255) / 256) * 256;
+  // Scratch layout: [wavelengths, reciprocals, 256-byte aligned][slab partial sums].
+  const size_t lam_bytes = ((2 * sizeof(double) * static_cast<size_t>(channels) + 255) / 256) * 256;
   if (lam_bytes > LEAP_NOALLOC_SCRATCH_BYTES)
     return fail(LEAP_ERR_INVALID_ARGUMENT, "channel count exceeds the no-allocation scratch limit");
   const size_t avail = LEAP_NOALLOC_SCRATCH_BYTES - lam_bytes;
@@ -149,6 +153,7 @@ extern "C" int32_t leap_rotate_average_noalloc(int32_t vis_type, const void* vis
   a.uvw = uvw;
   a.dd = dd;
   a.lambda = reinterpret_cast<const double*>(scratch);
+  a.inv_lambda = reinterpret_cast<const double*>(scratch) + channels;
   a.rows = rows;
   a.channels = channels;
   a.pols = pols;

@@ -307,7 +307,7 @@ int32_t leap_synchronize(leap_ctx* ctx);
  *
  * Its scratch (wavelength table and partial sums) is one array of
  * LEAP_NOALLOC_SCRATCH_BYTES per device; sizes that cannot fit (more than
- * about two million channels) are rejected with LEAP_ERR_INVALID_ARGUMENT, and
+ * about one million channels) are rejected with LEAP_ERR_INVALID_ARGUMENT, and
  * large workloads use fewer partial-sum slabs.  All calls on a device share the
  * array, so calls that overlap on the GPU (different streams, or several host
  * threads) race and must be serialised by the caller.  The first call on each

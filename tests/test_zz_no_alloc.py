@@ -78,7 +78,7 @@ def test_no_alloc_rejects_oversized_channel_count():
     import torch
     dev = torch.device("cuda:0")
     x = torch.zeros(16, dtype=torch.float64, device=dev)
-    too_many = _abi.LEAP_NOALLOC_SCRATCH_BYTES // 8 + 1
+    too_many = _abi.LEAP_NOALLOC_SCRATCH_BYTES // 16 + 1  # wavelengths and reciprocals, 16 B a channel
     rc = _abi.lib.leap_rotate_average_noalloc(_abi.LEAP_VIS_C64, x.data_ptr(), x.data_ptr(), 1, too_many, 1, 1,
                                               1e8, 1e3, x.data_ptr(), 1, x.data_ptr(), None)
     assert rc == _abi.LEAP_ERR_INVALID_ARGUMENT
