@@ -403,10 +403,11 @@ def setup_batched(run, dir_ids=None) -> Workload:
     w.vis_bytes = sum(samples.values()) * 8
     w.kernel_name = ("rotate_average_mixed_pipe<8,4,4> (persistent, TMA-pipelined, 4 tiles x 8 directions per block; "
                      "FP32 CUDA cores with compensated sums) + the rotate stage's small kernels")
-    # DRAM traffic of the bulk kernel: the cube once plus its partial-sum writes (ncu on the
-    # 4-timestep, 8-direction case of this kernel read 409.1 MB for 409.1 MB of visibilities and
-    # wrote 3.9 MB; the batched call's writes are its slabs' partial sums), scaled to this call.
-    w.traffic = None
+    # DRAM traffic of the bulk kernel, from an ncu capture (dram__bytes_read.sum +
+    # dram__bytes_write.sum) of the same kernel on 4 timesteps of the 128-antenna array with 8
+    # directions: 408.99 MB read for 405.80 MB of visibilities (the rest is the split UVWs), a few
+    # MB of partial-sum writes.  Reads scale with the visibilities; writes taken as one avgData.
+    w.traffic = w.vis_bytes * (408.99 / 405.80) + sum(n * 8256 * 4 * 16 for _, _, n in items)
     w.hosts = hosts
     w.min_ndir = min(n for _, _, n in items)
     if args.e2e and hosts:
@@ -595,6 +596,8 @@ class Run:
             self.ctx.set_option(_abi.LEAP_OPTION_TENSOR_CORE_ROTATION, args.tc_rotation)
         if args.gridded >= 0:
             self.ctx.set_option(_abi.LEAP_OPTION_GRIDDED_ROTATION, args.gridded)
+        if args.grid_shared >= 0:
+            self.ctx.set_option(_abi.LEAP_OPTION_GRID_SHARED_GROUPS, args.grid_shared)
 
     def timed(self, w: Workload, p: int, steps: int, warmup: int):
         """W untimed steps, then exactly `steps` steps between barriers and synchronisations;
@@ -759,6 +762,16 @@ def run_workload(name, args, torch, lg, local, rank, world, dist, steps, warmup,
             "kernel": "rotate_average_mixed_pipe (FP32 CUDA cores, compensated sums)", "ms_per_step": ms_alt,
             "kernel_ms": t_alt.rotate_ms / max(1, t_alt.calls), "value": w.units * world / (ms_alt / 1e3),
             "max_cal_diff_vs_gridded_rad": float(np.abs(cal_main - cal_alt).max())}
+    if gridded and name == "ska_low" and args.grid_shared < 0 and w.D > 64:
+        # The other arrangement of the direction groups (one grid product per tile for all groups).
+        from leap_gb300 import _abi
+        run.ctx.set_option(_abi.LEAP_OPTION_GRID_SHARED_GROUPS, 1)
+        ms_sh, t_sh = run.timed(w, prec, max(1, min(steps, 5)), 2)
+        run.ctx.set_option(_abi.LEAP_OPTION_GRID_SHARED_GROUPS, 0)
+        out["alternative_grouping"] = {
+            "grouping": "one grid product per tile for both groups of 64 directions (one-tile units)",
+            "ms_per_step": ms_sh, "kernel_ms": t_sh.rotate_ms / max(1, t_sh.calls),
+            "max_cal_diff_rad": float(np.abs(w.result() - cal_main).max())}
     cal64 = None
     if not args.skip_plain and prec == lg.LEAP_PRECISION_MIXED:
         n64 = 1 if name == "ska_low" else max(1, min(steps, 3))
@@ -913,6 +926,8 @@ def run_gpu(args, rank: int, world: int):
             "plain_fp64": head.get("plain_fp64"),
             "checks": head.get("checks"),
             "sharding": head.get("sharding"),
+            "alternative_kernel": head.get("alternative_kernel"),
+            "alternative_grouping": head.get("alternative_grouping"),
             "metadata_build_s": head["metadata_build_s"],
             "sub_results": subs or None,
             "clocks": head["clocks"],
@@ -941,6 +956,9 @@ def main():
                     help="tensor-core rotate + average: 0 never, 1 autotuned (library default), 2 always")
     ap.add_argument("--gridded", type=int, default=-1,
                     help="gridded rotate + average (tcgen05 grid product): 0 off, 1 on, -1 library default")
+    ap.add_argument("--grid-shared", type=int, default=-1,
+                    help="gridded kernel, > 64 directions: 1 one grid product per tile for all direction groups, "
+                         "0 one per group, -1 library default")
     ap.add_argument("--cpu-budget", type=float, default=15.0)
     ap.add_argument("--skip-cpu", action="store_true")
     ap.add_argument("--skip-plain", action="store_true")

@@ -43,14 +43,19 @@
 // (the grid matrix interleaves its re and im rows), so the W + 1 taps of one
 // stencil are 2 (W + 1) = 18 adjacent columns: a 16- and a 2-column tcgen05.ld.
 //
-// Warp roles (14 warps): 0 = TMA producer, 1 = MMA issuer (+ TMEM owner), 2-5 =
-// converters (split the visibility box into K-major hi/lo blocks, and fold the
-// accumulators), 6-13 = epilogue (warp w reads TMEM lanes 32 (w % 4) ..; two
-// warps per quarter take 32 directions each).  One ring of kGrStages stages of
-// {visibility box (overwritten by A hi), A lo, E window}, handed over in pairs and
-// released by one MMA commit per pair.  Every wait is bounded; a timeout sets the
-// error word, stops every role, and the block still waits (bounded) for its copies
-// and MMAs and frees its TMEM.
+// Operands.  The tile's visibilities reach shared memory already split into TF32 hi
+// and lo parts in the MMA's canonical K-major layout: grid_split_operand builds that
+// copy of an integration once (16 KB per tile and 16-channel chunk, twice the bytes of
+// the visibilities), and each chunk is then one bulk copy, so no warp converts
+// operands between the copy and the MMAs.
+//
+// Warp roles (14 warps): 0 = producer (bulk copies of the split operand and of the E
+// window), 1 = MMA issuer (+ TMEM owner), 2-5 = fold warps (add the finished hi*hi
+// segments and the corrections into the running sums), 6-13 = epilogue (warp w reads
+// TMEM lanes 32 (w % 4) ..; two warps per quarter take 32 directions each).  One ring of
+// kGrStages stages of {A hi, A lo, E window}, handed over in pairs and released by one
+// MMA commit per pair.  Every wait is bounded; a timeout sets the error word, stops every
+// role, and the block still waits (bounded) for its copies and MMAs and frees its TMEM.
 #pragma once
 
 #include "leap_common.cuh"
@@ -74,11 +79,11 @@ constexpr int kGrEpiWarps = 8;
 constexpr int kGrWarpDirs = kGrDirs * 4 / kGrEpiWarps;  // directions per epilogue warp
 constexpr int kGrWarps = 6 + kGrEpiWarps;
 constexpr int kGrThreads = kGrWarps * 32;
-constexpr int kGrVBytes = 32 * 4 * kGrChunk * 4;         // [16 ch][4 t][32 floats]
+constexpr int kGrVBytes = 32 * 4 * kGrChunk * 4;         // one chunk of a tile: 16 ch x 4 t x 32 floats
 constexpr int kGrEBytes = 2 * 2 * 2 * kGrJwMax * 32;     // [hl][ks][2 Jw rows x 32 B]
 constexpr int kGrAHalf = 2 * 128 * 32;                   // one split of A: [ks][128 rows x 32 B]
-static_assert(kGrAHalf == kGrVBytes, "the hi blocks are written over the visibility box");
-// Stage: [visibility box, then A hi][A lo][E]
+static_assert(kGrAHalf == kGrVBytes, "one split of A holds one chunk of a tile");
+// Stage: [A hi][A lo][E]
 constexpr int kGrStageBytes = kGrVBytes + kGrAHalf + kGrEBytes;
 constexpr int kGrEOffset = kGrVBytes + kGrAHalf;
 constexpr int kGrRecWords = 12;                          // per (direction, timestep) record: 3 16-byte rows
@@ -86,7 +91,7 @@ constexpr int kGrRecBytes = kGrEpiWarps * 32 * kGrRecWords * 4;  // [warps][4 t]
 constexpr uint32_t kGrRegion = 128;                      // TMEM columns per region
 constexpr uint32_t kGrIS = 2 * kGrRegion, kGrAC = 3 * kGrRegion;
 constexpr int kGrWide = 1 << 16;                         // record flag: the 4 timesteps need separate loads
-constexpr int kGrNumBars = 4 * kGrMacroStages + 8;
+constexpr int kGrNumBars = 2 * kGrMacroStages + 8;
 
 // A pass window must hold every stencil whose start falls in its stride, plus the
 // columns one load reads past the stencil.
@@ -107,15 +112,65 @@ __host__ __device__ constexpr int64_t grid_table_floats(int C) {
   return static_cast<int64_t>(grid_chunks(C)) * 2 * 2 * 2 * grid_rows(C) * 8;
 }
 
-// One item of a gridded launch (device memory; the tensor map needs 128-byte alignment).
-struct alignas(128) GridItem {
-  CUtensorMap map;       // [channel][timestep][nbl*8 floats], box 32 x 4 x kGrChunk
+// Split grid operand of an integration: per (quad, timestep block, 16-channel chunk) the
+// tile's visibilities as TF32 hi and lo parts in the MMA's canonical K-major layout,
+// [hi: 2 k-steps x 16 row groups x 2 k-halves x 8 rows x 16 B][lo: the same], 16 KB,
+// exactly what the shared-memory stage holds before the MMAs of a chunk.
+constexpr int kGrOpBytes = 2 * 2 * 128 * 32;  // hi + lo blocks of one chunk of one tile
+__host__ __device__ constexpr int64_t grid_operand_bytes(int nbl, int T, int C) {
+  return static_cast<int64_t>((nbl + 3) / 4) * ((T + 3) / 4) * ((C + 15) / 16) * kGrOpBytes;
+}
+
+// Builds the split grid operand of a 4-pol complex<float> integration [C][rows][8 floats]:
+// one 128-thread block per (chunk, timestep block, quad); warp w takes timestep w of the
+// block and lane = 8 q + 2 p + s, the baseline q of the quad, pol p, (re, im) s.  Rows and
+// channels past the integration are zero, as a tensor-map load fills them.  hi is the
+// visibility rounded to TF32, lo the remainder rounded to TF32.
+static __global__ void __launch_bounds__(128) grid_split_operand(const float* __restrict__ vis, int64_t rows, int nbl,
+                                                                 int T, int C, int ntb, float* __restrict__ out) {
+  const int q = blockIdx.x, tb = blockIdx.y, chunk = blockIdx.z;
+  const int lane = threadIdx.x & 31, tl = threadIdx.x >> 5;
+  const int t = tb * 4 + tl, b = q * 4 + (lane >> 3);
+  const bool rv = t < T && b < nbl;
+  const int64_t row = static_cast<int64_t>(t) * nbl + b;
+  unsigned char* dst = reinterpret_cast<unsigned char*>(out) +
+                       ((static_cast<int64_t>(q) * ntb + tb) * gridDim.z + chunk) * kGrOpBytes;
+  const int mrow = (lane >> 3) * 32 + tl * 8 + (lane & 7);  // TMEM lane: baseline, timestep, pol, re/im
+#pragma unroll
+  for (int cg = 0; cg < 4; ++cg) {
+    float x[4];
+#pragma unroll
+    for (int j = 0; j < 4; ++j) {
+      const int c = chunk * kGrChunk + cg * 4 + j;
+      x[j] = (rv && c < C) ? __ldg(vis + (static_cast<int64_t>(c) * rows + row) * 8 + (lane & 7)) : 0.f;
+    }
+    float4 hi, lo;
+    hi.x = to_tf32(x[0]);
+    hi.y = to_tf32(x[1]);
+    hi.z = to_tf32(x[2]);
+    hi.w = to_tf32(x[3]);
+    lo.x = to_tf32(x[0] - hi.x);
+    lo.y = to_tf32(x[1] - hi.y);
+    lo.z = to_tf32(x[2] - hi.z);
+    lo.w = to_tf32(x[3] - hi.w);
+    const int k = cg * 4;
+    const int off = (k >> 3) * 4096 + (((mrow >> 3) << 1) + ((k >> 2) & 1)) * 128 + (mrow & 7) * 16;
+    *reinterpret_cast<float4*>(dst + off) = hi;
+    *reinterpret_cast<float4*>(dst + kGrAHalf + off) = lo;
+  }
+}
+
+// One item of a gridded launch (device memory).
+struct alignas(16) GridItem {
+  const float* op;       // split grid operand: [quad][timestep block][chunk][kGrOpBytes]
   const float* uvw_f;    // [rows][6] split UVWs
   const float* etab;     // E table of this channel count
   double2* out;          // nslab == 1: avg + dir0*4*nbl; else this item's [nslab][ndir][4][nbl] partials
   int32_t T, C, nchunk, tb_per_slab;
   int32_t nslab, nquad, dgroups, dir0;
   int32_t ndir, unit_begin, nrg, lbase;
+  int32_t udg, uparts;   // direction groups per unit, units per (quad, slab): ceil(dgroups / udg)
+  int32_t ntb, pad_;     // timestep blocks of the integration (the operand's second dimension)
 };
 
 // Grid window of one unit, written by grid_windows: table rows [8 rg0, 8 rg0 + jw)
@@ -134,10 +189,10 @@ struct GridParams {
   int32_t nslots, nitems, units, nbl;
 };
 
-// A unit: one quad of baselines over one timestep slab, for every direction of its item
-// (the grid product of a tile serves all of them).
+// A unit: one quad of baselines over one timestep slab, for direction groups [dg_lo, dg_hi)
+// of its item (the grid product of a tile serves all of them).
 struct GridUnit {
-  int item, quad, slab, t_lo, t_hi, ntb;
+  int item, quad, slab, t_lo, t_hi, ntb, dg_lo, dg_hi;
 };
 
 __device__ __forceinline__ int grid_find_item(const GridItem* items, int nitems, int u) {
@@ -155,8 +210,11 @@ __device__ __forceinline__ GridUnit grid_unit(const GridParams& p, int u) {
   g.item = grid_find_item(p.items, p.nitems, u);
   const GridItem& I = p.items[g.item];
   const int l = u - I.unit_begin;
-  g.quad = l / I.nslab;
+  g.quad = l / (I.uparts * I.nslab);
+  const int part = (l / I.nslab) % I.uparts;
   g.slab = l % I.nslab;
+  g.dg_lo = part * I.udg;
+  g.dg_hi = min(I.dgroups, g.dg_lo + I.udg);
   g.t_lo = g.slab * I.tb_per_slab * 4;
   g.t_hi = min(I.T, g.t_lo + I.tb_per_slab * 4);
   g.ntb = (g.t_hi - g.t_lo + 3) / 4;
@@ -214,7 +272,7 @@ static __global__ void grid_windows(const GridParams p) {
   // Every direction group of the item: lanes hold the slopes of directions lane and
   // lane + 32 of the group and walk the unit's rows; a row's UVWs are one broadcast load.
   static_assert(kGrDirs == 64, "two directions per lane");
-  for (int dg = 0; dg < I.dgroups; ++dg) {
+  for (int dg = g.dg_lo; dg < g.dg_hi; ++dg) {
     const int nd = min(kGrDirs, I.ndir - dg * kGrDirs);
     float kb[2][6];
     bool has[2];
@@ -468,11 +526,9 @@ __global__ void __launch_bounds__(kGrThreads, 1) rotate_average_gridded(const Gr
   float2* tab = reinterpret_cast<float2*>(smem + kGrStages * kGrStageBytes);
   float* rec_all = reinterpret_cast<float*>(tab + kTwiddleSize);
   uint64_t* bars = reinterpret_cast<uint64_t*>(rec_all + kGrRecBytes / 4);
-  uint64_t* vfull = bars;                      // [kGrMacroStages] TMA bytes of a stage pair landed
-  uint64_t* afull = vfull + kGrMacroStages;    // [kGrMacroStages] converters wrote its A blocks
-  uint64_t* sdone = afull + kGrMacroStages;    // [kGrMacroStages] MMAs that read it completed
-  uint64_t* vread = sdone + kGrMacroStages;    // [kGrMacroStages] every converter warp read the boxes
-  uint64_t* is_full = vread + kGrMacroStages;  // a middle segment is complete in IS
+  uint64_t* vfull = bars;                      // [kGrMacroStages] bytes of a stage pair landed
+  uint64_t* sdone = vfull + kGrMacroStages;    // [kGrMacroStages] MMAs that read it completed
+  uint64_t* is_full = sdone + kGrMacroStages;  // a middle segment is complete in IS
   uint64_t* is_empty = is_full + 1;            // ... and was folded into RS
   uint64_t* blk_full = is_empty + 1;           // every MMA of a tile completed
   uint64_t* ac_free = blk_full + 1;            // final fold of a tile done: IS and AC reusable
@@ -491,10 +547,8 @@ __global__ void __launch_bounds__(kGrThreads, 1) rotate_average_gridded(const Gr
   if (threadIdx.x == 0) {
     for (int i = 0; i < kGrMacroStages; ++i) {
       mbar_init(&vfull[i], 1);
-      mbar_init(&afull[i], 4);
       mbar_init(&sdone[i], 1);
     }
-    for (int i = 0; i < kGrMacroStages; ++i) mbar_init(&vread[i], 4);
     mbar_init(is_full, 1);
     mbar_init(is_empty, 4);
     mbar_init(blk_full, 1);
@@ -532,12 +586,16 @@ __global__ void __launch_bounds__(kGrThreads, 1) rotate_average_gridded(const Gr
                 ok = false;
                 break;
               }
-              mbar_arrive_expect_tx(&vfull[m], nq * (kGrVBytes + 8 * w.jw * 32));
+              mbar_arrive_expect_tx(&vfull[m], nq * (kGrOpBytes + 8 * w.jw * 32));
               const int rg = w.rg0 + ps * (kGrPassStride / 8);
+              const int tbi = g.t_lo / 4 + tb;  // the tile's timestep block in the integration
               for (int i = 0; i < nq; ++i) {
                 const int q = q0 + i;
                 unsigned char* st = ve + (m * kGrMacro + i) * kGrStageBytes;
-                tma_load_3d(st, &I.map, g.quad * 32, g.t_lo + tb * 4, q * kGrChunk, &vfull[m]);
+                // The chunk's A operand, hi and lo, already in the MMA layout.
+                bulk_copy_g2s(st, reinterpret_cast<const unsigned char*>(I.op) +
+                                      ((static_cast<int64_t>(g.quad) * I.ntb + tbi) * I.nchunk + q) * kGrOpBytes,
+                              kGrOpBytes, &vfull[m]);
 #pragma unroll
                 for (int ks = 0; ks < 2; ++ks)
 #pragma unroll
@@ -581,7 +639,7 @@ __global__ void __launch_bounds__(kGrThreads, 1) rotate_average_gridded(const Gr
             for (int q0 = 0; q0 < I.nchunk && ok; q0 += kGrMacro, ++ctr) {
               const int m = ctr % kGrMacroStages;
               const int nq = min(kGrMacro, I.nchunk - q0);
-              if (!grid_wait(&afull[m], (ctr / kGrMacroStages) & 1, abort_flag)) {
+              if (!grid_wait(&vfull[m], (ctr / kGrMacroStages) & 1, abort_flag)) {
                 grid_fail(p, abort_flag);
                 ok = false;
                 break;
@@ -623,10 +681,9 @@ __global__ void __launch_bounds__(kGrThreads, 1) rotate_average_gridded(const Gr
       }
     }
   } else if (warp < 6) {
-    // ---------------- converters: visibility box -> K-major hi/lo A blocks; folds ----------------
-    const int cw = warp - 2;
+    // ---------------- fold warps: segments and corrections into the running sums ----------------
     const uint32_t lanes = static_cast<uint32_t>((warp & 3) * 32) << 16;
-    uint32_t ctr = 0, blk = 0, mids = 0;
+    uint32_t blk = 0, mids = 0;
     bool ok = true;
     for (int sl = blockIdx.x; ok; sl += gridDim.x) {
       const int u = sl < p.nslots ? __ldg(p.order + sl) : -1;
@@ -638,89 +695,20 @@ __global__ void __launch_bounds__(kGrThreads, 1) rotate_average_gridded(const Gr
       for (int tb = 0; tb < g.ntb && ok; ++tb)
         for (int ps = 0; ps < w.npass && ok; ++ps, ++blk) {
           const uint32_t b = blk & 1;
-          for (int q0 = 0; q0 < I.nchunk; q0 += kGrMacro, ++ctr) {
-            // The stages' previous MMAs completed before the producer refilled them, so a full
-            // stage pair's A blocks are free to overwrite.
-            const int m = ctr % kGrMacroStages;
-            const int nq = min(kGrMacro, I.nchunk - q0);
-            if (!grid_wait(&vfull[m], (ctr / kGrMacroStages) & 1, abort_flag)) {
+          // Middle segments 1 .. nseg - 2 complete in IS one after another: each is added to RS
+          // as soon as its MMAs have completed, so that the next segment can restart IS.
+          for (int sg = 1; sg <= nseg - 2; ++sg) {
+            if (!grid_wait(is_full, mids & 1, abort_flag)) {
               grid_fail(p, abort_flag);
               ok = false;
               break;
             }
-            // Read both boxes of the round; the hi blocks overwrite them, so every converter
-            // warp must have read them before any warp writes.
-            float x[kGrMacro][4][4];
-#pragma unroll
-            for (int i = 0; i < kGrMacro; ++i) {
-              if (i < nq) {
-                const float* vb = reinterpret_cast<const float*>(ve + (m * kGrMacro + i) * kGrStageBytes);
-#pragma unroll
-                for (int bi = 0; bi < 4; ++bi) {
-                  const int blk4 = cw + 4 * bi;  // 16 blocks of (4 channels, 1 timestep)
-                  const int cg = blk4 >> 2, tl = blk4 & 3;
-#pragma unroll
-                  for (int j = 0; j < 4; ++j) x[i][bi][j] = vb[(cg * 4 + j) * 128 + tl * 32 + lane];
-                }
-              }
-            }
+            asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+            grid_fold(lanes, tmem + b * kGrRegion, tmem + kGrIS, 0, true, false, 2 * w.jw);
+            asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
             __syncwarp();
-            if (lane == 0) mbar_arrive(&vread[m]);
-            if (!grid_wait(&vread[m], (ctr / kGrMacroStages) & 1, abort_flag)) {
-              grid_fail(p, abort_flag);
-              ok = false;
-              break;
-            }
-#pragma unroll
-            for (int i = 0; i < kGrMacro; ++i) {
-              if (i < nq) {
-                unsigned char* sb = ve + (m * kGrMacro + i) * kGrStageBytes;
-#pragma unroll
-                for (int bi = 0; bi < 4; ++bi) {
-                  const int blk4 = cw + 4 * bi;
-                  const int cg = blk4 >> 2, tl = blk4 & 3;
-                  float4 hi, lo;
-                  hi.x = to_tf32(x[i][bi][0]);
-                  hi.y = to_tf32(x[i][bi][1]);
-                  hi.z = to_tf32(x[i][bi][2]);
-                  hi.w = to_tf32(x[i][bi][3]);
-                  lo.x = to_tf32(x[i][bi][0] - hi.x);
-                  lo.y = to_tf32(x[i][bi][1] - hi.y);
-                  lo.z = to_tf32(x[i][bi][2] - hi.z);
-                  lo.w = to_tf32(x[i][bi][3] - hi.w);
-                  const int mrow = (lane >> 3) * 32 + tl * 8 + (lane & 7);  // TMEM lane: baseline, timestep, pol, re/im
-                  const int k = cg * 4;                                     // 0..15 within the chunk
-                  const int off = (k >> 3) * 4096 + (((mrow >> 3) << 1) + ((k >> 2) & 1)) * 128 + (mrow & 7) * 16;
-                  *reinterpret_cast<float4*>(sb + off) = hi;
-                  *reinterpret_cast<float4*>(sb + kGrAHalf + off) = lo;
-                }
-              }
-            }
-            asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-            __syncwarp();
-            if (lane == 0) mbar_arrive(&afull[m]);
-            // Fold middle segment sg (1 <= sg <= nseg - 2) into RS once the next segment's
-            // second chunk is converted (its first if it has only one).
-            for (int i = 0; i < nq && ok; ++i) {
-              const int q = q0 + i;
-              const int seg = q / kGrSegChunks, qs = q % kGrSegChunks;
-              const int nxt = min(kGrSegChunks, I.nchunk - seg * kGrSegChunks);
-              const int sg = seg - 1;
-              if (sg >= 1 && sg <= nseg - 2 && qs == min(1, nxt - 1)) {
-                if (!grid_wait(is_full, mids & 1, abort_flag)) {
-                  grid_fail(p, abort_flag);
-                  ok = false;
-                  break;
-                }
-                asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-                grid_fold(lanes, tmem + b * kGrRegion, tmem + kGrIS, 0, true, false, 2 * w.jw);
-                asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
-                __syncwarp();
-                if (lane == 0) mbar_arrive(is_empty);
-                ++mids;
-              }
-            }
-            if (!ok) break;
+            if (lane == 0) mbar_arrive(is_empty);
+            ++mids;
           }
           if (!ok) break;
           // Final fold: RS += last segment (if any beyond the first) + corrections.
@@ -764,7 +752,7 @@ __global__ void __launch_bounds__(kGrThreads, 1) rotate_average_gridded(const Gr
       // With one direction group the warp's sums stay in registers over the unit's tiles and
       // passes; with several, each (tile, pass, group) adds its sums to the unit's output in
       // order (the first stores), since every group's sums do not fit in registers.
-      const bool keep = I.dgroups == 1;
+      const bool keep = g.dg_hi - g.dg_lo == 1;
       float acc[kGrWarpDirs];
 #pragma unroll
       for (int j = 0; j < kGrWarpDirs; ++j) acc[j] = 0.f;
@@ -784,7 +772,7 @@ __global__ void __launch_bounds__(kGrThreads, 1) rotate_average_gridded(const Gr
           }
           asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
           const uint32_t tbase = tmem + (static_cast<uint32_t>(quarter * 32) << 16) + rb * kGrRegion;
-          for (int dg = 0; dg < I.dgroups; ++dg) {
+          for (int dg = g.dg_lo; dg < g.dg_hi; ++dg) {
           const int dbase = dg * kGrDirs + half * kGrWarpDirs;  // item-relative first direction of this warp
           const int nd = max(0, min(kGrWarpDirs, I.ndir - dbase));
           if (!keep) {
@@ -879,8 +867,10 @@ __global__ void __launch_bounds__(kGrThreads, 1) rotate_average_gridded(const Gr
         }
       }
       if (!ok) break;
-      if (keep) grid_flush(acc, out, half * kGrWarpDirs, max(0, min(kGrWarpDirs, I.ndir - half * kGrWarpDirs)), b,
-                           bval, tl, ps, comp, p.nbl, true);
+      if (keep) {
+        const int dbase = g.dg_lo * kGrDirs + half * kGrWarpDirs;
+        grid_flush(acc, out, dbase, max(0, min(kGrWarpDirs, I.ndir - dbase)), b, bval, tl, ps, comp, p.nbl, true);
+      }
     }
   }
   asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");

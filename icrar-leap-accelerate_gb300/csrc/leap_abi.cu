@@ -67,8 +67,11 @@ struct Integration {
   int32_t channels = 0, pols = 0;
   bool has_map = false;
   CUtensorMap map16, map8;  // [channel][row*8 floats] views of a 4-pol complex<float> integration, box heights 16 / 8
-  CUtensorMap map_g;        // [channel][timestep][nbl*8 floats] view for the gridded kernel (built on first use)
-  int32_t map_g_nbl = 0;    // baseline count map_g was built for (0: none)
+  // Split grid operand of the gridded kernel (TF32 hi/lo tiles in the MMA layout), built on
+  // the first gridded call after the visibilities change; op_nbl: the baseline count it was
+  // built for (0: none).
+  DeviceBuffer op;
+  int32_t op_nbl = 0;
   // Asynchronous ingestion: the upload runs on the context's copy stream and `ready`
   // marks its end; calibrate calls make their stream wait for it.
   cudaEvent_t ready = nullptr;
@@ -120,6 +123,7 @@ struct leap_ctx {
   int gridded = 2;                    // gridded rotate + average (tcgen05 grid product): 0 never, 1 always,
                                       // 2 when every item has >= kGridAutoDirs directions
   bool grid_attr = false;
+  bool grid_shared_groups = false;    // gridded kernel: one grid product per tile for all direction groups
   std::map<int, DeviceBuffer> grid_tabs;  // grid matrix per channel count
   std::vector<GridItem> grid_items_host;
   std::vector<int32_t> grid_order_host;
@@ -295,15 +299,18 @@ int gridded_stage(leap_ctx* ctx, const std::vector<WorkItem>& items, const doubl
   Metadata& md = ctx->md;
   const int32_t nbl = static_cast<int32_t>(md.k.nbaselines);
   const int nquad = (nbl + 3) / 4;
-  auto enc = tensor_map_encoder();
-  if (!enc) return fail(ctx, LEAP_ERR_CUDA, "cuTensorMapEncodeTiled unavailable");
   std::vector<GridItem>& git = ctx->grid_items_host;
   std::vector<ReduceItem>& red = ctx->reduce_items_host;
   git.assign(items.size(), GridItem{});
   red.clear();
-  // A unit is a quad of baselines over a timestep slab, for all of its item's directions.
+  // A unit is a quad of baselines over a timestep slab, for one direction group, or for all of
+  // them (one grid product per tile) with LEAP_OPTION_GRID_SHARED_GROUPS.
+  auto unit_groups = [&](int dgroups) { return ctx->grid_shared_groups ? dgroups : 1; };
   int64_t base_units = 0;
-  for (size_t i = 0; i < items.size(); ++i) base_units += nquad;
+  for (const auto& w : items) {
+    const int dgroups = (w.ndir + kGrDirs - 1) / kGrDirs;
+    base_units += static_cast<int64_t>(nquad) * ((dgroups + unit_groups(dgroups) - 1) / unit_groups(dgroups));
+  }
   // Timestep slabs only when the (quad, direction group) units alone would leave blocks idle.
   const int64_t want_slabs = std::max<int64_t>(1, (4 * static_cast<int64_t>(ctx->sms) + base_units - 1) / base_units);
   int units = 0;
@@ -314,21 +321,22 @@ int gridded_stage(leap_ctx* ctx, const std::vector<WorkItem>& items, const doubl
     Integration& in = ctx->integ.at(w.slot);
     const int T = static_cast<int>(in.rows / nbl);
     const int C = in.channels;
-    if (in.map_g_nbl != nbl) {
-      cuuint64_t dims[3] = {static_cast<cuuint64_t>(nbl) * 8, static_cast<cuuint64_t>(T), static_cast<cuuint64_t>(C)};
-      cuuint64_t strides[2] = {static_cast<cuuint64_t>(nbl) * 32, static_cast<cuuint64_t>(in.rows) * 32};
-      cuuint32_t box[3] = {32, 4, static_cast<cuuint32_t>(kGrChunk)};
-      cuuint32_t estr[3] = {1, 1, 1};
-      CUresult r = enc(&in.map_g, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 3, in.vis.ptr, dims, strides, box, estr,
-                       CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
-                       CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
-      if (r != CUDA_SUCCESS) return fail(ctx, LEAP_ERR_CUDA, "cuTensorMapEncodeTiled (3-D) failed: " + std::to_string(r));
-      in.map_g_nbl = nbl;
+    if (in.op_nbl != nbl) {
+      // The split grid operand: built once per upload (the visibilities read once, hi and lo
+      // written), then read by every gridded call on this integration.
+      if (ctx->capturing) return fail(ctx, LEAP_ERR_INTERNAL, "grid operand missing while recording a graph");
+      LEAP_CUDA(in.op.ensure(static_cast<size_t>(grid_operand_bytes(nbl, T, C))), "alloc grid operand");
+      const dim3 og((nbl + 3) / 4, (T + 3) / 4, grid_chunks(C));
+      grid_split_operand<<<og, 128, 0, s>>>(in.vis.as<float>(), in.rows, nbl, T, C, (T + 3) / 4, in.op.as<float>());
+      LEAP_CUDA(cudaGetLastError(), "grid operand launch");
+      ++kernels;
+      in.op_nbl = nbl;
     }
     const float* tab = grid_table_for(ctx, C);
     if (!tab) return fail(ctx, LEAP_ERR_CUDA, "grid matrix unavailable for this channel count");
     GridItem& it = git[i];
-    it.map = in.map_g;
+    it.op = in.op.as<float>();
+    it.ntb = (T + 3) / 4;
     it.uvw_f = in.uvw_f.as<float>();
     it.etab = tab;
     it.T = T;
@@ -336,10 +344,12 @@ int gridded_stage(leap_ctx* ctx, const std::vector<WorkItem>& items, const doubl
     it.nchunk = grid_chunks(C);
     const int ntb = (T + 3) / 4;
     it.dgroups = (w.ndir + kGrDirs - 1) / kGrDirs;
-    // With several direction groups the epilogue cannot hold every group's sums across a
-    // unit's tiles, so a unit is one tile (a slab per timestep block) and its sums are
-    // stored once; the fixed-order slab reduction adds the tiles.
-    const int nslab_want = it.dgroups > 1 ? ntb : static_cast<int>(std::min<int64_t>(ntb, want_slabs));
+    it.udg = unit_groups(it.dgroups);
+    it.uparts = (it.dgroups + it.udg - 1) / it.udg;
+    // With several direction groups in a unit the epilogue cannot hold every group's sums
+    // across the unit's tiles, so such a unit is one tile (a slab per timestep block) and its
+    // sums are stored once; the fixed-order slab reduction adds the tiles.
+    const int nslab_want = it.udg > 1 ? ntb : static_cast<int>(std::min<int64_t>(ntb, want_slabs));
     it.tb_per_slab = (ntb + nslab_want - 1) / nslab_want;
     it.nslab = (ntb + it.tb_per_slab - 1) / it.tb_per_slab;
     it.nquad = nquad;
@@ -348,7 +358,7 @@ int gridded_stage(leap_ctx* ctx, const std::vector<WorkItem>& items, const doubl
     it.unit_begin = units;
     it.nrg = grid_rows(C) / 8;
     it.lbase = grid_lbase(C);
-    units += it.nquad * it.nslab;
+    units += it.nquad * it.uparts * it.nslab;
     if (it.nslab > 1) {
       partial_off[i] = partial_elems;
       partial_elems += static_cast<int64_t>(it.nslab) * w.ndir * 4 * nbl;
@@ -371,11 +381,11 @@ int gridded_stage(leap_ctx* ctx, const std::vector<WorkItem>& items, const doubl
     std::vector<std::pair<int64_t, int>> cost;
     cost.reserve(units);
     for (const GridItem& it : git) {
-      const int per_item = it.nquad * it.nslab;
+      const int per_item = it.nquad * it.uparts * it.nslab;
       for (int l = 0; l < per_item; ++l) {
         const int slab = l % it.nslab;
         const int t_lo = slab * it.tb_per_slab * 4, t_hi = std::min(it.T, t_lo + it.tb_per_slab * 4);
-        cost.emplace_back(-static_cast<int64_t>((t_hi - t_lo + 3) / 4) * (it.nchunk + 2 * it.dgroups),
+        cost.emplace_back(-static_cast<int64_t>((t_hi - t_lo + 3) / 4) * (it.nchunk + 2 * it.udg),
                           it.unit_begin + l);
       }
     }
@@ -1022,7 +1032,8 @@ int calibrate_impl(leap_ctx* ctx, int32_t slot, const double* d_dd, int32_t ndir
 
 std::string batch_key(const leap_ctx* ctx, const std::vector<WorkItem>& items, int32_t D, int32_t precision) {
   std::string k = std::to_string(D) + ":" + std::to_string(precision) + (ctx->tc_gemm ? ":tc" : ":cc") +
-                  ":mma" + std::to_string(ctx->mma_rotate) + ":grid" + std::to_string(ctx->gridded);
+                  ":mma" + std::to_string(ctx->mma_rotate) + ":grid" + std::to_string(ctx->gridded) +
+                  (ctx->grid_shared_groups ? "s" : "");
   for (const auto& w : items) k += "|" + std::to_string(w.slot) + "," + std::to_string(w.dir0) + "," + std::to_string(w.ndir);
   return k;
 }
@@ -1161,7 +1172,7 @@ int finish_integration(leap_ctx* ctx, Integration& in, int32_t vis_type, int64_t
   in.channels = channels;
   in.pols = pols;
   in.has_map = false;
-  in.map_g_nbl = 0;
+  in.op_nbl = 0;
   if (vis_type == LEAP_VIS_C64 && pols == 4 && rows * 8 < (int64_t(1) << 31)) {
     // The pipelined kernels' view: 2-D floats [channels][rows*8], box 256 floats x 16 channels.
     auto enc = tensor_map_encoder();
@@ -1774,7 +1785,7 @@ int32_t leap_set_integration_ms_async(leap_ctx* ctx, int32_t slot, int32_t vis_t
   in.channels = channels;
   in.pols = pols;
   in.has_map = false;
-  in.map_g_nbl = 0;
+  in.op_nbl = 0;
   if (vis_type == LEAP_VIS_C64 && pols == 4 && rows * 8 < (int64_t(1) << 31)) {
     auto enc = tensor_map_encoder();
     if (!enc) return fail(ctx, LEAP_ERR_CUDA, "cuTensorMapEncodeTiled unavailable");
@@ -1815,6 +1826,7 @@ int32_t leap_apply_flags(leap_ctx* ctx, int32_t slot, const uint8_t* flags, int6
   }
   LEAP_CUDA(ctx->flag_count.ensure(sizeof(unsigned long long)), "alloc flag count");
   LEAP_CUDA(cudaMemsetAsync(ctx->flag_count.ptr, 0, sizeof(unsigned long long), s), "clear flag count");
+  in.op_nbl = 0;  // the visibilities change: rebuild the split grid operand on its next use
   const int grid = grid_1d(in.rows * in.channels, 256);
   if (in.vis_type == LEAP_VIS_C64)
     apply_flag_groups<float2><<<grid, 256, 0, s>>>(in.vis.as<float2>(), dflags, in.rows, in.channels, in.pols, row_channels,
@@ -1843,6 +1855,7 @@ int32_t leap_release_integration(leap_ctx* ctx, int32_t slot) {
   it->second.vis.release();
   it->second.uvw.release();
   it->second.uvw_f.release();
+  it->second.op.release();
   ctx->integ.erase(it);
   return LEAP_OK;
 }
@@ -2001,6 +2014,7 @@ int32_t leap_set_option(leap_ctx* ctx, int32_t option, int32_t value) {
       ctx->gridded = value;
       return LEAP_OK;
     case LEAP_OPTION_GRAPH_REPLAY: ctx->graph_replay = value != 0; return LEAP_OK;
+    case LEAP_OPTION_GRID_SHARED_GROUPS: ctx->grid_shared_groups = value != 0; return LEAP_OK;
     default: return fail(ctx, LEAP_ERR_INVALID_ARGUMENT, "unknown option");
   }
 }

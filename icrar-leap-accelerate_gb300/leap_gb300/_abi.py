@@ -32,6 +32,7 @@ LEAP_OPTION_TENSOR_CORE_CONTRACTION = 2
 LEAP_OPTION_TENSOR_CORE_ROTATION = 3
 LEAP_OPTION_GRIDDED_ROTATION = 4
 LEAP_OPTION_GRAPH_REPLAY = 5
+LEAP_OPTION_GRID_SHARED_GROUPS = 6
 
 # Every entry point include/leap_gb300.h declares, with its ctypes signature.
 i32, i64, f64, vp = ctypes.c_int32, ctypes.c_int64, ctypes.c_double, ctypes.c_void_p

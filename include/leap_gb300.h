@@ -233,6 +233,9 @@ int32_t leap_set_autotune(leap_ctx* ctx, int32_t enable);
                                                     a CUDA graph and replays it for later calls of the same shape;
                                                     0 launches every call eagerly, so that its timing events (and
                                                     leap_get_timings' rotate_ms) bracket the rotate + average stage */
+#define LEAP_OPTION_GRID_SHARED_GROUPS 6        /* gridded rotate + average with more than 64 directions per item:
+                                                    0 (default) each group of 64 directions runs its own grid
+                                                    product; 1 one grid product per tile serves every group */
 int32_t leap_set_option(leap_ctx* ctx, int32_t option, int32_t value);
 
 /* Copy the avgData of `direction` from the last calibrate call to host memory

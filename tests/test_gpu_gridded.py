@@ -14,7 +14,7 @@ import pytest
 import oracle
 import leap_gb300 as lg
 from leap_gb300 import synth
-from leap_gb300._abi import LEAP_OPTION_GRIDDED_ROTATION
+from leap_gb300._abi import LEAP_OPTION_GRIDDED_ROTATION, LEAP_OPTION_GRID_SHARED_GROUPS
 from test_gpu_parity import MIXED_CAL_TOL, _dds, assert_cal_close
 
 pytestmark = pytest.mark.gpu
@@ -168,3 +168,16 @@ def test_gridded_auto_selection(ctx):
         cal = ctx.calibrate(0, dds[:nd], lg.LEAP_PRECISION_MIXED)
         assert_cal_close(cal, cal_o[:nd], avg_o[:nd], mdo, MIXED_CAL_TOL)
     ctx.release_integration(0)
+
+
+@pytest.mark.parametrize("shared", [0, 1], ids=["group_per_unit", "one_product_for_all_groups"])
+def test_gridded_direction_groups(ctx, shared):
+    """130 directions: three groups of up to 64, each with its own grid product, or all served
+    by one product per tile (one-tile units whose sums the slab reduction adds)."""
+    obs, dirs = synth.small_case(stations=20, timesteps=9, channels=40, directions=130, vis_dtype=np.complex64,
+                                 seed_shift=31)
+    ctx.set_option(LEAP_OPTION_GRID_SHARED_GROUPS, shared)
+    try:
+        _check(ctx, obs, dirs)
+    finally:
+        ctx.set_option(LEAP_OPTION_GRID_SHARED_GROUPS, 0)
