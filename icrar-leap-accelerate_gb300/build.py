@@ -37,7 +37,8 @@ def _cuda_home() -> str:
     return os.path.dirname(os.path.dirname(os.path.realpath(_nvcc())))
 
 
-CU_SOURCES = ["leap_abi.cu", "leap_noalloc.cu"]
+CU_SOURCES = ["leap_context.cu", "leap_metadata.cu", "leap_ingest.cu", "leap_calibrate.cu", "leap_adjoint.cu",
+              "leap_noalloc.cu"]
 CC_SOURCES = ["host_math.cc"]
 CPP_SOURCES = ["icrar/calibration.cc", "icrar/MeasurementSet.cc", "icrar/MetaData.cc",
                "icrar/GpuLeapCalibrator.cc", "icrar/LeapCalibratorFactory.cc", "icrar/compute_implementation.cc"]

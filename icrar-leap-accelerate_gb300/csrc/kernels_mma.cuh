@@ -59,7 +59,7 @@ __device__ __forceinline__ void mma_16x8x8_tf32(float (&d)[4], uint32_t a0, uint
       : "r"(a0), "r"(a1), "r"(a2), "r"(a3), "r"(b0), "r"(b1));
 }
 
-__global__ void __launch_bounds__(256, 1) rotate_average_mma_pipe(const PipeParams p) {
+static __global__ void __launch_bounds__(256, 1) rotate_average_mma_pipe(const PipeParams p) {
   constexpr int TPB = 1;
   constexpr int CH = PipeShape<TPB>::CH;
   constexpr int NS = PipeShape<TPB>::STAGES;

@@ -74,7 +74,7 @@ __global__ void tc_pack_operand(const T* __restrict__ src, int rows, int K, int6
 
 // Ad is stored column-major S x K (element (s, k) at s + S*k): rows are s with
 // row stride 1 and k stride S.  Pack it with an explicit k stride.
-__global__ void tc_pack_ad(const double* __restrict__ Ad, int S, int K, int row_tiles, int kblocks,
+static __global__ void tc_pack_ad(const double* __restrict__ Ad, int S, int K, int row_tiles, int kblocks,
                            float* __restrict__ dst) {
   const int R = kTcM;
   const int64_t total = static_cast<int64_t>(row_tiles) * R * kblocks * kTcKB;
