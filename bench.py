@@ -355,7 +355,7 @@ def grid_windows_host(obs, dds: np.ndarray, taps: int = 8, jw_max: int = 64, str
         jw = np.where(single, np.maximum(8, (need + 7) & ~7), jw_max)
         npass = np.where(single, 1, (smax + lbase - r0) // stride + 1)
         ntb = (T + 3) // 4
-        flops += float((ntb * npass * nchunk * 6 * 2 * 128 * 2 * jw * 8).sum())
+        flops += float((ntb * npass * nchunk * 3 * 2 * 128 * 2 * jw * 16).sum())  # 3 FP16 MMAs, K = 16, per chunk
         passes += float((ntb * npass).sum())
         tiles += float(ntb * nquad)
         pmax = max(pmax, int(npass.max()))
@@ -669,12 +669,12 @@ def roofline(w: Workload, k_ms: float, gridded: bool, peaks) -> dict:
                         "once for all directions, so this figure is not a roofline fraction"}}
     if gridded and w.grid is not None:
         flops, mean_pass, max_pass = w.grid
-        tf32_peak = (peaks["bf16_tflops"] / 2 if peaks and "bf16_tflops" in peaks else 950.0) * 1e12
-        roof["tensor"] = {"tf32_flops_per_s": flops / (k_ms / 1e3), "peak_flops_per_s": tf32_peak,
-                          "frac": flops / (k_ms / 1e3) / tf32_peak, "mma_flops_per_call": flops,
+        f16_peak = (peaks["bf16_tflops"] if peaks and "bf16_tflops" in peaks else 1900.0) * 1e12
+        roof["tensor"] = {"f16_flops_per_s": flops / (k_ms / 1e3), "peak_flops_per_s": f16_peak,
+                          "frac": flops / (k_ms / 1e3) / f16_peak, "mma_flops_per_call": flops,
                           "grid_passes_per_tile_mean": mean_pass, "grid_passes_max": max_pass,
-                          "peak_source": "half of MEASURED_PEAKS.json bf16_tflops (TF32 rate, of measured)" if peaks
-                          else "half of the 1.9 PFLOP/s bf16 fallback (of fallback)"}
+                          "peak_source": "MEASURED_PEAKS.json bf16_tflops (the dense FP16 rate, of measured)" if peaks
+                          else "the 1.9 PFLOP/s bf16 fallback (of fallback)"}
     if roof["traffic"]:
         roof["dram_traffic_frac"] = roof["traffic"] / (k_ms / 1e3) / 1e9 / peak
     return roof
@@ -741,7 +741,7 @@ def run_workload(name, args, torch, lg, local, rank, world, dist, steps, warmup,
     cal_main = w.result()
     gridded = uses_gridded(args, w, prec, lg)
     if gridded and name in ("mwa", "ska_low"):
-        w.kernel_name = ("rotate_average_gridded<8> (3xTF32 tcgen05 grid product + 8-point interpolation per "
+        w.kernel_name = ("rotate_average_gridded<8> (3xFP16 tcgen05 grid product + 8-point interpolation per "
                          "direction) + grid_windows + the compensated reference-antenna pass")
         w.traffic = getattr(w, "grid_traffic", None)
     elif name in ("mwa", "ska_low"):

@@ -296,28 +296,72 @@ std::vector<double> es_kernel_transform(int32_t taps, double beta, int32_t n, in
   return out;
 }
 
+void es_kernel_poly(int32_t taps, double beta, int32_t degree, float* out) {
+  // h_m(f) = psi((f + taps/2 - 1 - m) * 2 / taps) for f in [0, 1): interpolate at the
+  // degree + 1 Chebyshev points of x = 2 f - 1, then expand the Chebyshev series into
+  // monomials of x (the Chebyshev coefficients c_n; T_{n+1} = 2 x T_n - T_{n-1}).
+  const int np = degree + 1;
+  const double kPiD = 3.141592653589793238462643383279;
+  std::vector<double> tm(static_cast<size_t>(np) * np, 0.0);  // tm[n * np + j]: x^j coefficient of T_n
+  tm[0] = 1.0;
+  if (np > 1) tm[1 * np + 1] = 1.0;
+  for (int n = 1; n + 1 < np; ++n)
+    for (int j = 0; j < np; ++j)
+      tm[(n + 1) * np + j] = (j > 0 ? 2.0 * tm[n * np + j - 1] : 0.0) - tm[(n - 1) * np + j];
+  for (int m = 0; m < taps; ++m) {
+    std::vector<double> val(np), mono(np, 0.0);
+    for (int k = 0; k < np; ++k) {
+      const double x = std::cos(kPiD * (k + 0.5) / np);
+      const double z = ((x + 1.0) * 0.5 + 0.5 * taps - 1.0 - m) * 2.0 / taps;
+      const double q = 1.0 - z * z;
+      val[k] = q > 0.0 ? std::exp(beta * (std::sqrt(q) - 1.0)) : 0.0;
+    }
+    for (int n = 0; n < np; ++n) {
+      double c = 0.0;
+      for (int k = 0; k < np; ++k) c += val[k] * std::cos(kPiD * n * (k + 0.5) / np);
+      c *= (n == 0 ? 1.0 : 2.0) / np;
+      for (int j = 0; j < np; ++j) mono[j] += c * tm[n * np + j];
+    }
+    for (int j = 0; j < np; ++j) out[m * np + j] = static_cast<float>(mono[j]);
+  }
+}
+
 namespace {
-// Round to the nearest TF32 value (10 mantissa bits), ties away from zero.
-float round_tf32(float x) {
-  uint32_t b;
-  std::memcpy(&b, &x, 4);
-  b = (b + 0x1000u) & 0xFFFFE000u;
-  float y;
-  std::memcpy(&y, &b, 4);
-  return y;
+// IEEE binary16 bits of x rounded to nearest, ties to even (|x| < 65504), and its value.
+uint16_t to_f16_bits(double x) {
+  const uint16_t sign = x < 0 ? 0x8000u : 0u;
+  const double a = std::fabs(x);
+  if (a == 0.0) return sign;
+  int e = 0;
+  const double f = std::frexp(a, &e);  // a = f 2^e, f in [0.5, 1)
+  const int E = e + 14;                // biased exponent of 2 f 2^(e - 1)
+  if (E < 1) return static_cast<uint16_t>(sign | static_cast<uint16_t>(std::nearbyint(std::ldexp(a, 24))));
+  const int mant = static_cast<int>(std::nearbyint((2.0 * f - 1.0) * 1024.0));
+  return static_cast<uint16_t>(sign | ((E << 10) + mant));  // mant == 1024 carries into the exponent
+}
+double from_f16_bits(uint16_t h) {
+  const int E = (h >> 10) & 31, mant = h & 1023;
+  const double v = E == 0 ? std::ldexp(static_cast<double>(mant), -24) : std::ldexp(1.0 + mant / 1024.0, E - 15);
+  return (h & 0x8000u) ? -v : v;
 }
 }  // namespace
 
-void grid_table(int32_t C, int32_t taps, double beta, int32_t lbase, int32_t rows, std::vector<float>& out) {
+float grid_table(int32_t C, int32_t taps, double beta, int32_t lbase, int32_t rows, std::vector<uint16_t>& out) {
   const int n = 2 * C, c0 = C / 2;
   const int nchunk = (C + 15) / 16, nrg = rows / 8;
   const std::vector<double> psi_hat = es_kernel_transform(taps, beta, n, std::max(c0, C - 1 - c0));
-  out.assign(static_cast<size_t>(nchunk) * 2 * 2 * 2 * rows * 8, 0.0f);
+  // One power of two for the table: the largest |E| = max 1 / Psi(k) goes into [2^13, 2^14).
+  double emax = 0.0;
+  for (int c = 0; c < C; ++c) emax = std::max(emax, 1.0 / psi_hat[std::abs(c - c0)]);
+  int e = 0;
+  (void)std::frexp(emax, &e);
+  const double scale = std::ldexp(1.0, 14 - e);
+  out.assign(static_cast<size_t>(nchunk) * 2 * 2 * nrg * 128, 0);
   const double kTwoPiD = 6.283185307179586476925286766559;
   for (int c = 0; c < C; ++c) {
     const int k = c - c0;
-    const double inv = 1.0 / psi_hat[std::abs(k)];
-    const int q = c / 16, ks = (c % 16) / 8, kk = c % 8;
+    const double inv = scale / psi_hat[std::abs(k)];
+    const int q = c / 16, kk = c % 16;
     for (int r = 0; r < rows; ++r) {
       const long long l = static_cast<long long>(r) - lbase;
       long long m = (static_cast<long long>(k) * l) % n;  // exact phase index
@@ -325,16 +369,18 @@ void grid_table(int32_t C, int32_t taps, double beta, int32_t lbase, int32_t row
       const double ang = kTwoPiD * static_cast<double>(m) / n;
       const double v[2] = {std::cos(ang) * inv, std::sin(ang) * inv};
       for (int ri = 0; ri < 2; ++ri) {
-        const float hi = round_tf32(static_cast<float>(v[ri]));
-        const float lo = round_tf32(static_cast<float>(v[ri] - static_cast<double>(hi)));
+        const uint16_t hi = to_f16_bits(v[ri]);
+        const uint16_t lo = to_f16_bits(v[ri] - from_f16_bits(hi));
         const int rr = 2 * r + ri;  // re and im rows of a grid point are neighbours
         for (int hl = 0; hl < 2; ++hl) {
-          const size_t base = (static_cast<size_t>((q * 2 + ks) * 2 + hl) * 2 * nrg + (rr >> 3)) * 64;
-          out[base + ((kk >> 2) & 1) * 32 + (rr & 7) * 4 + (kk & 3)] = hl == 0 ? hi : lo;
+          const size_t base = (static_cast<size_t>(q * 2 + hl) * 2 * nrg) * 128;
+          // The kernel's K-major 16-bit block layout (grid_f16_offset), in 2-byte units.
+          out[base + ((rr >> 3) * 2 + (kk >> 3)) * 64 + (rr & 7) * 8 + (kk & 7)] = hl == 0 ? hi : lo;
         }
       }
     }
   }
+  return static_cast<float>(1.0 / scale);
 }
 
 }  // namespace leapgb

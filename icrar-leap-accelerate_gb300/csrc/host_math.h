@@ -32,10 +32,18 @@ int pseudo_inverse(const double* A, int32_t m, int32_t n, double* Ad, std::strin
 // Grid matrix of the gridded rotate + average (kernels_grid.cuh) for C channels:
 // E[l][c] = exp(2 pi i (c - C/2) l / (2C)) / Psi(c - C/2) for table rows r = l + lbase,
 // r in [0, rows), with Psi the Fourier transform of the exponential-of-semicircle
-// kernel of width `taps` and shape `beta` at frequency k / (2C).  Written as 3xTF32
-// (hi, lo) splits in the packed K-major layout the kernel copies from:
-// [chunk of 16 channels][k-step][hi, lo][re, im][row group of 8][8 rows x 8 k].
-void grid_table(int32_t C, int32_t taps, double beta, int32_t lbase, int32_t rows, std::vector<float>& out);
+// kernel of width `taps` and shape `beta` at frequency k / (2C).  Scaled by a power of
+// two (its largest entry in [2^13, 2^14)) and written as FP16 (hi, lo) splits in the
+// K-major layout the kernel copies from: [chunk of 16 channels][hi, lo][row group of 8]
+// [2 k-halves][8 rows x 8 k], rows 2 l + (0: re, 1: im).  Returns the inverse scale.
+float grid_table(int32_t C, int32_t taps, double beta, int32_t lbase, int32_t rows, std::vector<uint16_t>& out);
+
+// Interpolation weights of the gridded rotate + average as polynomials: for m = 0 .. taps-1,
+// out[m * (degree + 1) + j] is the x^j coefficient (x = 2 f - 1, f in [0, 1)) of the degree
+// `degree` Chebyshev interpolant of psi((f + taps/2 - 1 - m) * 2 / taps), psi the
+// exponential-of-semicircle kernel of width `taps` and shape `beta` (the piecewise-polynomial
+// kernel evaluation of Barnett, Magland & af Klinteberg, SIAM J. Sci. Comput. 41 (2019) C479).
+void es_kernel_poly(int32_t taps, double beta, int32_t degree, float* out);
 
 // Psi(k) = integral over |x| < taps/2 of psi(x) cos(2 pi x k / n), for k = 0..kmax.
 std::vector<double> es_kernel_transform(int32_t taps, double beta, int32_t n, int32_t kmax);

@@ -27,8 +27,12 @@
 // positions differ by far less than a grid step: one warp-uniform 16-column
 // tcgen05.ld per accumulator half serves all 32 lanes of a direction.
 //
-// The product runs in 3xTF32 (V E ~ V_hi E_hi + V_lo E_hi + V_hi E_lo with hi = tf32(x),
-// lo = tf32(x - hi)).  The tensor cores accumulate FP32 with truncation, whose error
+// The product runs in 3xFP16 (V E ~ V_hi E_hi + V_lo E_hi + V_hi E_lo with hi = f16(x),
+// lo = f16(x - hi): 22 significant bits, as 3xTF32, at half the operand bytes and MMAs).
+// Each (baseline, pol) of a tile is scaled by a power of two that puts its largest
+// component near 2^14 and the grid matrix by one for the whole table, so both splits stay
+// in FP16's normal range; the epilogue undoes the scales exactly.  The tensor cores
+// accumulate FP32 with truncation, whose error
 // grows with the number of accumulation steps and the size of the accumulator; so the
 // large hi*hi products restart in a fresh accumulator every 64 channels (a "segment")
 // and the small corrections go to an accumulator of their own.  Converter warps add
@@ -43,11 +47,11 @@
 // (the grid matrix interleaves its re and im rows), so the W + 1 taps of one
 // stencil are 2 (W + 1) = 18 adjacent columns: a 16- and a 2-column tcgen05.ld.
 //
-// Operands.  The tile's visibilities reach shared memory already split into TF32 hi
-// and lo parts in the MMA's canonical K-major layout: grid_split_operand builds that
-// copy of an integration once (16 KB per tile and 16-channel chunk, twice the bytes of
-// the visibilities), and each chunk is then one bulk copy, so no warp converts
-// operands between the copy and the MMAs.
+// Operands.  The tile's visibilities reach shared memory already scaled and split into
+// FP16 hi and lo parts in the MMA's canonical K-major layout: grid_split_operand builds
+// that copy of an integration once (8 KB per tile and 16-channel chunk, the bytes of the
+// visibilities), and each chunk is then one bulk copy, so no warp converts operands
+// between the copy and the MMAs.
 //
 // Warp roles (14 warps): 0 = producer (bulk copies of the split operand and of the E
 // window), 1 = MMA issuer (+ TMEM owner), 2-5 = fold warps (add the finished hi*hi
@@ -57,6 +61,8 @@
 // MMA commit per pair.  Every wait is bounded; a timeout sets the error word, stops every
 // role, and the block still waits (bounded) for its copies and MMAs and frees its TMEM.
 #pragma once
+
+#include <cuda_fp16.h>
 
 #include "leap_common.cuh"
 #include "kernels_tc.cuh"
@@ -73,21 +79,22 @@ constexpr int kGrMacroStages = kGrStages / kGrMacro;
 constexpr int kGrJwMax = 64;          // grid points per pass (MMA N = 2 Jw <= 128)
 constexpr int kGrPassStride = 56;     // grid points between pass windows (multiple of 8)
 constexpr int kGrLoadCols = 9;        // grid points one interpolation load reads (2 TMEM columns each)
-constexpr int kGrBatch = 4;           // directions whose loads share one tcgen05.wait::ld
+constexpr int kGrPolyDeg = 8;         // degree of the per-tap weight polynomials
+constexpr int kGrBatch = 4;           // directions per timestep reduce-scatter (loads go in pairs)
 constexpr int kGrDirs = 64;           // directions per unit (8 epilogue warps x 32 / 4 quarters)
 constexpr int kGrEpiWarps = 8;
 constexpr int kGrWarpDirs = kGrDirs * 4 / kGrEpiWarps;  // directions per epilogue warp
 constexpr int kGrWarps = 6 + kGrEpiWarps;
 constexpr int kGrThreads = kGrWarps * 32;
-constexpr int kGrVBytes = 32 * 4 * kGrChunk * 4;         // one chunk of a tile: 16 ch x 4 t x 32 floats
-constexpr int kGrEBytes = 2 * 2 * 2 * kGrJwMax * 32;     // [hl][ks][2 Jw rows x 32 B]
-constexpr int kGrAHalf = 2 * 128 * 32;                   // one split of A: [ks][128 rows x 32 B]
-static_assert(kGrAHalf == kGrVBytes, "one split of A holds one chunk of a tile");
-// Stage: [A hi][A lo][E]
-constexpr int kGrStageBytes = kGrVBytes + kGrAHalf + kGrEBytes;
-constexpr int kGrEOffset = kGrVBytes + kGrAHalf;
+constexpr int kGrAHalf = 128 * kGrChunk * 2;            // one split of A: 128 rows x 16 f16 (32 B)
+constexpr int kGrOpBytes = 2 * kGrAHalf;                 // hi + lo of one chunk of one tile
+constexpr int kGrEBytes = 2 * 2 * kGrJwMax * kGrChunk * 2;  // [hl][2 Jw rows x 32 B]
+// Stage: [A hi][A lo][E hi][E lo]
+constexpr int kGrStageBytes = kGrOpBytes + kGrEBytes;
+constexpr int kGrEOffset = kGrOpBytes;
 constexpr int kGrRecWords = 12;                          // per (direction, timestep) record: 3 16-byte rows
-constexpr int kGrRecBytes = kGrEpiWarps * 32 * kGrRecWords * 4;  // [warps][4 t][8 dirs][12]
+constexpr int kGrRecDirs = 16;                           // directions whose records a warp holds at a time
+constexpr int kGrRecBytes = kGrEpiWarps * 4 * kGrRecDirs * kGrRecWords * 4;  // [warps][4 t][16 dirs][12]
 constexpr uint32_t kGrRegion = 128;                      // TMEM columns per region
 constexpr uint32_t kGrIS = 2 * kGrRegion, kGrAC = 3 * kGrRegion;
 constexpr int kGrWide = 1 << 16;                         // record flag: the 4 timesteps need separate loads
@@ -101,76 +108,97 @@ static_assert(kGrTaps + 1 <= kGrLoadCols, "one load per stencil");
 __host__ __device__ constexpr int grid_smem_bytes() {
   return kGrStages * kGrStageBytes + kTwiddleSize * 8 + kGrRecBytes + kGrNumBars * 8 + 16;
 }
+static_assert(grid_smem_bytes() <= 227 * 1024, "one block's dynamic shared memory (227 KB on sm_103)");
 
 // Rows of the E table of channel count C: row r is grid point l = r - lbase.
 __host__ __device__ constexpr int grid_lbase(int C) { return ((C + kGrTaps + 8 + 7) / 8) * 8; }
 __host__ __device__ constexpr int grid_rows(int C) { return ((grid_lbase(C) + C + kGrJwMax + 8 + 7) / 8) * 8; }
 __host__ __device__ constexpr int grid_chunks(int C) { return (C + kGrChunk - 1) / kGrChunk; }
-// Floats of the E table: [chunk][ks][hl][row group][8 rows x 8 k], rows 2 l + (0: re, 1: im) of grid
-// point l (relative to -lbase).
-__host__ __device__ constexpr int64_t grid_table_floats(int C) {
-  return static_cast<int64_t>(grid_chunks(C)) * 2 * 2 * 2 * grid_rows(C) * 8;
-}
-
 // Split grid operand of an integration: per (quad, timestep block, 16-channel chunk) the
-// tile's visibilities as TF32 hi and lo parts in the MMA's canonical K-major layout,
-// [hi: 2 k-steps x 16 row groups x 2 k-halves x 8 rows x 16 B][lo: the same], 16 KB,
-// exactly what the shared-memory stage holds before the MMAs of a chunk.
-constexpr int kGrOpBytes = 2 * 2 * 128 * 32;  // hi + lo blocks of one chunk of one tile
+// tile's scaled visibilities as FP16 hi and lo parts in the MMA's canonical K-major layout,
+// [hi: 16 row groups x 2 k-halves x 8 rows x 16 B][lo: the same], 8 KB, exactly what the
+// shared-memory stage holds before the MMAs of a chunk; then the inverse scales, one float
+// per (quad, timestep block, baseline of the quad, pol).
 __host__ __device__ constexpr int64_t grid_operand_bytes(int nbl, int T, int C) {
   return static_cast<int64_t>((nbl + 3) / 4) * ((T + 3) / 4) * ((C + 15) / 16) * kGrOpBytes;
 }
+__host__ __device__ constexpr int64_t grid_scale_bytes(int nbl, int T) {
+  return static_cast<int64_t>((nbl + 3) / 4) * ((T + 3) / 4) * 16 * 4;
+}
+
+// Byte offset of element (row, k) of a K-major operand block of 16-bit values without
+// swizzle: 8-row core matrices of 16 B rows, k-halves 128 B apart, row groups 256 B apart.
+__host__ __device__ constexpr int grid_f16_offset(int row, int k) {
+  return ((row >> 3) * 2 + (k >> 3)) * 128 + (row & 7) * 16 + (k & 7) * 2;
+}
 
 // Builds the split grid operand of a 4-pol complex<float> integration [C][rows][8 floats]:
-// one 128-thread block per (chunk, timestep block, quad); warp w takes timestep w of the
-// block and lane = 8 q + 2 p + s, the baseline q of the quad, pol p, (re, im) s.  Rows and
-// channels past the integration are zero, as a tensor-map load fills them.  hi is the
-// visibility rounded to TF32, lo the remainder rounded to TF32.
+// one 128-thread block per (quad, timestep block); warp w takes timestep w of the block and
+// lane = 8 q + 2 p + s, the baseline q of the quad, pol p, (re, im) s.  The power of two
+// of each (baseline, pol) brings its largest |component| over the block's 4 timesteps and
+// all channels into [2^13, 2^14); vinv holds its inverse (1 for an all-zero one).  hi is
+// the scaled visibility rounded to FP16, lo the remainder rounded to FP16.  Rows and
+// channels past the integration are zero, as a tensor-map load fills them.
 static __global__ void __launch_bounds__(128) grid_split_operand(const float* __restrict__ vis, int64_t rows, int nbl,
-                                                                 int T, int C, int ntb, float* __restrict__ out) {
-  const int q = blockIdx.x, tb = blockIdx.y, chunk = blockIdx.z;
+                                                                 int T, int C, int ntb, unsigned char* __restrict__ out,
+                                                                 float* __restrict__ vinv) {
+  __shared__ float smax[4][32];
+  const int q = blockIdx.x, tb = blockIdx.y, nchunk = (C + kGrChunk - 1) / kGrChunk;
   const int lane = threadIdx.x & 31, tl = threadIdx.x >> 5;
   const int t = tb * 4 + tl, b = q * 4 + (lane >> 3);
   const bool rv = t < T && b < nbl;
-  const int64_t row = static_cast<int64_t>(t) * nbl + b;
-  unsigned char* dst = reinterpret_cast<unsigned char*>(out) +
-                       ((static_cast<int64_t>(q) * ntb + tb) * gridDim.z + chunk) * kGrOpBytes;
+  const float* src = vis + (static_cast<int64_t>(t) * nbl + b) * 8 + (lane & 7);
+  const int64_t cstride = rows * 8;
+  float m = 0.f;
+  if (rv)
+    for (int c = 0; c < C; ++c) m = fmaxf(m, fabsf(__ldg(src + c * cstride)));
+  m = fmaxf(m, __shfl_xor_sync(0xffffffffu, m, 1));  // re and im
+  smax[tl][lane] = m;
+  __syncthreads();
+  m = fmaxf(fmaxf(smax[0][lane], smax[1][lane]), fmaxf(smax[2][lane], smax[3][lane]));
+  int e = 0;
+  (void)frexpf(m, &e);  // m < 2^e
+  const float scale = m > 0.f ? ldexpf(1.f, 14 - e) : 1.f;
+  if (tl == 0 && !(lane & 1)) vinv[(static_cast<int64_t>(q) * ntb + tb) * 16 + (lane >> 1)] = 1.f / scale;
   const int mrow = (lane >> 3) * 32 + tl * 8 + (lane & 7);  // TMEM lane: baseline, timestep, pol, re/im
+  for (int chunk = 0; chunk < nchunk; ++chunk) {
+    unsigned char* dst = out + ((static_cast<int64_t>(q) * ntb + tb) * nchunk + chunk) * kGrOpBytes;
 #pragma unroll
-  for (int cg = 0; cg < 4; ++cg) {
-    float x[4];
+    for (int kh = 0; kh < 2; ++kh) {
+      uint32_t hw[4], lw[4];
 #pragma unroll
-    for (int j = 0; j < 4; ++j) {
-      const int c = chunk * kGrChunk + cg * 4 + j;
-      x[j] = (rv && c < C) ? __ldg(vis + (static_cast<int64_t>(c) * rows + row) * 8 + (lane & 7)) : 0.f;
+      for (int j = 0; j < 8; j += 2) {
+        float x[2];
+#pragma unroll
+        for (int i = 0; i < 2; ++i) {
+          const int c = chunk * kGrChunk + kh * 8 + j + i;
+          x[i] = (rv && c < C) ? __ldg(src + c * cstride) * scale : 0.f;
+        }
+        const __half2 h = __floats2half2_rn(x[0], x[1]);
+        const __half2 l = __floats2half2_rn(x[0] - __low2float(h), x[1] - __high2float(h));
+        hw[j >> 1] = *reinterpret_cast<const uint32_t*>(&h);
+        lw[j >> 1] = *reinterpret_cast<const uint32_t*>(&l);
+      }
+      const int off = grid_f16_offset(mrow, kh * 8);
+      *reinterpret_cast<uint4*>(dst + off) = make_uint4(hw[0], hw[1], hw[2], hw[3]);
+      *reinterpret_cast<uint4*>(dst + kGrAHalf + off) = make_uint4(lw[0], lw[1], lw[2], lw[3]);
     }
-    float4 hi, lo;
-    hi.x = to_tf32(x[0]);
-    hi.y = to_tf32(x[1]);
-    hi.z = to_tf32(x[2]);
-    hi.w = to_tf32(x[3]);
-    lo.x = to_tf32(x[0] - hi.x);
-    lo.y = to_tf32(x[1] - hi.y);
-    lo.z = to_tf32(x[2] - hi.z);
-    lo.w = to_tf32(x[3] - hi.w);
-    const int k = cg * 4;
-    const int off = (k >> 3) * 4096 + (((mrow >> 3) << 1) + ((k >> 2) & 1)) * 128 + (mrow & 7) * 16;
-    *reinterpret_cast<float4*>(dst + off) = hi;
-    *reinterpret_cast<float4*>(dst + kGrAHalf + off) = lo;
   }
 }
 
 // One item of a gridded launch (device memory).
 struct alignas(16) GridItem {
-  const float* op;       // split grid operand: [quad][timestep block][chunk][kGrOpBytes]
+  const unsigned char* op;  // split grid operand: [quad][timestep block][chunk][kGrOpBytes]
+  const float* vinv;     // [quad][timestep block][16]: inverse scales of the operand's (baseline, pol)s
   const float* uvw_f;    // [rows][6] split UVWs
-  const float* etab;     // E table of this channel count
+  const unsigned char* etab;  // E table of this channel count (FP16 hi/lo, scaled by 1 / einv)
   double2* out;          // nslab == 1: avg + dir0*4*nbl; else this item's [nslab][ndir][4][nbl] partials
   int32_t T, C, nchunk, tb_per_slab;
   int32_t nslab, nquad, dgroups, dir0;
   int32_t ndir, unit_begin, nrg, lbase;
   int32_t udg, uparts;   // direction groups per unit, units per (quad, slab): ceil(dgroups / udg)
-  int32_t ntb, pad_;     // timestep blocks of the integration (the operand's second dimension)
+  int32_t ntb;           // timestep blocks of the integration (the operand's second dimension)
+  float einv;            // inverse scale of the E table
 };
 
 // Grid window of one unit, written by grid_windows: table rows [8 rg0, 8 rg0 + jw)
@@ -187,6 +215,9 @@ struct GridParams {
   const float2* twiddle;   // [kTwiddleSize]
   int* err;
   int32_t nslots, nitems, units, nbl;
+  // Weight polynomials: tap m of a stencil at fractional grid position f has weight
+  // sum_j wpoly[m][j] x^j, x = 2 f - 1 (es_kernel_poly on the host).
+  float wpoly[kGrTaps][kGrPolyDeg + 1];
 };
 
 // A unit: one quad of baselines over one timestep slab, for direction groups [dg_lo, dg_hi)
@@ -326,86 +357,88 @@ static __global__ void grid_windows(const GridParams p) {
   }
 }
 
+// The W + 1 weights of a shared load for a stencil at fractional grid position f that starts
+// `shifted` (0 or 1) columns after the load: w[k] = h_{k - shifted}(f), 0 outside the W taps,
+// with h_m the tap polynomials of c (degree kGrPolyDeg in x = 2 f - 1; the weight error is
+// about 1e-7 of the largest weight, FP32 Horner rounding included).
 template <int W>
-__device__ __forceinline__ void grid_weights(float y, float (&w)[W + 1]) {
-  constexpr float kInvHalf = 2.0f / W;
-  constexpr float kBeta2 = kGrBeta * 1.4426950408889634f;  // beta / ln 2
+__device__ __forceinline__ void grid_weights(float f, bool shifted, const float (&c)[W][kGrPolyDeg + 1],
+                                             float (&w)[W + 1]) {
+  const float x = fmaf(2.0f, f, -1.0f);
+  float h[W];
 #pragma unroll
-  for (int k = 0; k <= W; ++k) {
-    // sqrt(1 - z^2) - 1 = -z^2 / (1 + sqrt(1 - z^2)): no cancellation near the centre.
-    // Hardware reciprocal square root and exp2 (~2 ulp): weight error below 1e-7 of the
-    // largest weight.
-    const float z = (y - static_cast<float>(k)) * kInvHalf;
-    const float z2 = z * z;
-    const float q = fmaxf(1e-30f, 1.0f - z2);
-    const float v = exp2f(-kBeta2 * __fdividef(z2, fmaf(q, rsqrtf(q), 1.0f)));
-    w[k] = z2 < 1.0f ? v : 0.0f;  // psi vanishes outside its support (the load's spare tap)
+  for (int m = 0; m < W; ++m) {
+    float a = c[m][kGrPolyDeg];
+#pragma unroll
+    for (int j = kGrPolyDeg - 1; j >= 0; --j) a = fmaf(a, x, c[m][j]);
+    h[m] = a;
   }
+  w[0] = shifted ? 0.f : h[0];
+#pragma unroll
+  for (int k = 1; k < W; ++k) w[k] = shifted ? h[k - 1] : h[k];
+  w[W] = shifted ? h[W - 1] : 0.f;
 }
 
-// kGrBatch directions' stencils from TMEM: a 16- and a 2-column load each (the W + 1
-// taps, re and im interleaved) at columns col[b] of this warp's lanes, and one wait for all.
-__device__ __forceinline__ void grid_load_batch(uint32_t tbase, const uint32_t (&col)[kGrBatch],
-                                                uint32_t (&v)[kGrBatch][18]) {
-  static_assert(kGrBatch == 4 && kGrLoadCols == 9, "four 18-column loads per batch");
+// Two directions' stencils from TMEM: a 16- and a 2-column load each (the W + 1 taps, re
+// and im interleaved) at columns c0 and c1 of this warp's lanes, and one wait for both.
+__device__ __forceinline__ void grid_load_pair(uint32_t tbase, uint32_t c0, uint32_t c1, uint32_t (&v)[2][18]) {
+  static_assert(kGrLoadCols == 9, "18 columns per stencil");
   // All loads and the wait in one statement: the results are defined only after the wait.
   asm volatile(
-      "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%72];\n\t"
-      "tcgen05.ld.sync.aligned.32x32b.x2.b32 {%16,%17}, [%73];\n\t"
-      "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%18,%19,%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31,%32,%33}, [%74];\n\t"
-      "tcgen05.ld.sync.aligned.32x32b.x2.b32 {%34,%35}, [%75];\n\t"
-      "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%36,%37,%38,%39,%40,%41,%42,%43,%44,%45,%46,%47,%48,%49,%50,%51}, [%76];\n\t"
-      "tcgen05.ld.sync.aligned.32x32b.x2.b32 {%52,%53}, [%77];\n\t"
-      "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%54,%55,%56,%57,%58,%59,%60,%61,%62,%63,%64,%65,%66,%67,%68,%69}, [%78];\n\t"
-      "tcgen05.ld.sync.aligned.32x32b.x2.b32 {%70,%71}, [%79];\n\t"
+      "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%36];\n\t"
+      "tcgen05.ld.sync.aligned.32x32b.x2.b32 {%16,%17}, [%37];\n\t"
+      "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%18,%19,%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31,%32,%33}, [%38];\n\t"
+      "tcgen05.ld.sync.aligned.32x32b.x2.b32 {%34,%35}, [%39];\n\t"
       "tcgen05.wait::ld.sync.aligned;"
       : "=r"(v[0][0]), "=r"(v[0][1]), "=r"(v[0][2]), "=r"(v[0][3]), "=r"(v[0][4]), "=r"(v[0][5]), "=r"(v[0][6]),
         "=r"(v[0][7]), "=r"(v[0][8]), "=r"(v[0][9]), "=r"(v[0][10]), "=r"(v[0][11]), "=r"(v[0][12]), "=r"(v[0][13]),
         "=r"(v[0][14]), "=r"(v[0][15]), "=r"(v[0][16]), "=r"(v[0][17]),
         "=r"(v[1][0]), "=r"(v[1][1]), "=r"(v[1][2]), "=r"(v[1][3]), "=r"(v[1][4]), "=r"(v[1][5]), "=r"(v[1][6]),
         "=r"(v[1][7]), "=r"(v[1][8]), "=r"(v[1][9]), "=r"(v[1][10]), "=r"(v[1][11]), "=r"(v[1][12]), "=r"(v[1][13]),
-        "=r"(v[1][14]), "=r"(v[1][15]), "=r"(v[1][16]), "=r"(v[1][17]),
-        "=r"(v[2][0]), "=r"(v[2][1]), "=r"(v[2][2]), "=r"(v[2][3]), "=r"(v[2][4]), "=r"(v[2][5]), "=r"(v[2][6]),
-        "=r"(v[2][7]), "=r"(v[2][8]), "=r"(v[2][9]), "=r"(v[2][10]), "=r"(v[2][11]), "=r"(v[2][12]), "=r"(v[2][13]),
-        "=r"(v[2][14]), "=r"(v[2][15]), "=r"(v[2][16]), "=r"(v[2][17]),
-        "=r"(v[3][0]), "=r"(v[3][1]), "=r"(v[3][2]), "=r"(v[3][3]), "=r"(v[3][4]), "=r"(v[3][5]), "=r"(v[3][6]),
-        "=r"(v[3][7]), "=r"(v[3][8]), "=r"(v[3][9]), "=r"(v[3][10]), "=r"(v[3][11]), "=r"(v[3][12]), "=r"(v[3][13]),
-        "=r"(v[3][14]), "=r"(v[3][15]), "=r"(v[3][16]), "=r"(v[3][17])
-      : "r"(tbase + col[0]), "r"(tbase + col[0] + 16u), "r"(tbase + col[1]), "r"(tbase + col[1] + 16u),
-        "r"(tbase + col[2]), "r"(tbase + col[2] + 16u), "r"(tbase + col[3]), "r"(tbase + col[3] + 16u));
+        "=r"(v[1][14]), "=r"(v[1][15]), "=r"(v[1][16]), "=r"(v[1][17])
+      : "r"(tbase + c0), "r"(tbase + c0 + 16u), "r"(tbase + c1), "r"(tbase + c1 + 16u));
 }
 
 // One direction of one lane: the W + 1 taps v (re, im interleaved) weighted by the
-// lane's record (weights, then the rotation (cr, sr)), combined with the partner
-// lane's component, rotated; returns this lane's component of the rotated sum.
+// lane's record (weights, then the rotation (cr, sr)), rotated and combined with the
+// partner lane (the other component of the same visibility); returns this lane's
+// component of the rotated sum.  sgn is -1 on the real lane (comp 0), +1 on the imaginary.
 template <int W>
-__device__ __forceinline__ float grid_tap_combine(const uint32_t (&v)[18], const float* rec, int comp) {
+__device__ __forceinline__ float grid_tap_combine(const uint32_t (&v)[18], const float* rec, float sgn) {
   static_assert(W + 1 == 9, "record layout: 9 weights, then cr, sr, code");
   const float4 q0 = reinterpret_cast<const float4*>(rec)[0], q1 = reinterpret_cast<const float4*>(rec)[1];
   const float4 q2 = reinterpret_cast<const float4*>(rec)[2];
-  const float2 rot = make_float2(q2.y, q2.z);
   const float w[9] = {q0.x, q0.y, q0.z, q0.w, q1.x, q1.y, q1.z, q1.w, q2.x};
-  float P = 0.f, Q = 0.f;
+  // Two chains per sum (even and odd taps) halve the dependent FMA latency.
+  float P0 = 0.f, P1 = 0.f, Q0 = 0.f, Q1 = 0.f;
 #pragma unroll
   for (int k = 0; k <= W; ++k) {
-    P = fmaf(w[k], __uint_as_float(v[2 * k]), P);
-    Q = fmaf(w[k], __uint_as_float(v[2 * k + 1]), Q);
+    if (k & 1) {
+      P1 = fmaf(w[k], __uint_as_float(v[2 * k]), P1);
+      Q1 = fmaf(w[k], __uint_as_float(v[2 * k + 1]), Q1);
+    } else {
+      P0 = fmaf(w[k], __uint_as_float(v[2 * k]), P0);
+      Q0 = fmaf(w[k], __uint_as_float(v[2 * k + 1]), Q0);
+    }
   }
-  // Lane re (comp 0): P = sum Vr ReE, Q = sum Vr ImE; lane im: P = sum Vi ReE, Q = sum Vi ImE.
-  // G = (P_re - Q_im) + i (Q_re + P_im); the lane's component of G * (cr + i sr).
-  const float o = __shfl_xor_sync(0xffffffffu, Q, 1);
-  const float gown = comp ? (o + P) : (P - o);
-  const float o2 = __shfl_xor_sync(0xffffffffu, gown, 1);
-  return comp ? fmaf(o2, rot.y, gown * rot.x) : fmaf(-o2, rot.y, gown * rot.x);
+  const float P = P0 + P1, Q = Q0 + Q1;
+  // Lane re: P = sum Vr ReE, Q = sum Vr ImE; lane im: P = sum Vi ReE, Q = sum Vi ImE.
+  // G = (P_r - Q_i) + i (Q_r + P_i), and G (cr + i sr) has
+  //   re = (P_r cr - Q_r sr) - (P_i sr + Q_i cr),  im = (P_i cr - Q_i sr) + (P_r sr + Q_r cr):
+  // each lane keeps P cr - Q sr and hands P sr + Q cr to its partner (one shuffle).
+  const float keep = fmaf(P, q2.y, -Q * q2.z);
+  const float send = fmaf(P, q2.z, Q * q2.y);
+  return fmaf(sgn, __shfl_xor_sync(0xffffffffu, send, 1), keep);
 }
 
 // A direction whose 4 timesteps need separate grid windows: one load per timestep
-// (rare; kept out of line so that the common path stays small).
+// (rare; kept out of line so that the common path stays small).  rec_dir is the
+// direction's record at timestep 0; timestep t's is t * kGrRecDirs records further.
 template <int W>
-__device__ __noinline__ float grid_wide_sum(const float* rec_dir, uint32_t tbase, int comp, int tl, int pp) {
+__device__ __noinline__ float grid_wide_sum(const float* rec_dir, uint32_t tbase, float sgn, int tl, int pp) {
   float acc = 0.f;
   for (int tt = 0; tt < 4; ++tt) {
-    const float* r = rec_dir + tt * 8 * kGrRecWords;
+    const float* r = rec_dir + tt * kGrRecDirs * kGrRecWords;
     const int ct = __float_as_int(r[11]);
     if ((ct & 0xFFFF) == 0xFFFF || ((ct >> 8) & 255) != pp) continue;  // same in every lane
     uint32_t v[18];
@@ -418,10 +451,61 @@ __device__ __noinline__ float grid_wide_sum(const float* rec_dir, uint32_t tbase
           "=r"(v[9]), "=r"(v[10]), "=r"(v[11]), "=r"(v[12]), "=r"(v[13]), "=r"(v[14]), "=r"(v[15]), "=r"(v[16]),
           "=r"(v[17])
         : "r"(a0), "r"(a0 + 16u));
-    const float g = grid_tap_combine<W>(v, r, comp);
+    const float g = grid_tap_combine<W>(v, r, sgn);
     if (tl == tt) acc += g;
   }
   return acc;
+}
+
+// The record of one (timestep, direction) for this lane's row of the tile: the W + 1
+// interpolation weights of the quarter's shared stencil, the rotation at the centre
+// channel, and the load code: the pass and the column of the quarter's shared load, with
+// kGrWide when the 4 timesteps need loads of their own (0xFFFF in the column field for a
+// row outside the data), or -1 when the direction reads nothing.  Every lane of the warp
+// calls it together (the 4 timesteps of a direction exchange their stencil starts).
+template <int W>
+__device__ __forceinline__ void grid_record(const GridParams& p, const float (&x)[6], const float2* tab, int d,
+                                            bool dv, bool rval, int n, int c0, int lbase, int r0, int npass,
+                                            float* dst) {
+  float ka[6], kb[6];
+#pragma unroll
+  for (int i = 0; i < 6; ++i) {
+    ka[i] = __ldg(p.dirk + 12 * d + i);
+    kb[i] = __ldg(p.dirk + 12 * d + 6 + i);
+  }
+  const uint32_t pa = df_dot3_turns_u32(ka, x);
+  const uint32_t pb = df_dot3_turns_u32(kb, x);
+  float f;
+  const int i0 = grid_position(pb, n, f);
+  const int st = grid_stencil_start(i0, f);  // this row's stencil start
+  const int sl0 = rval ? st : 0x7fffffff, sh0 = rval ? st : -0x7fffffff;
+  int cw = min(sl0, __shfl_xor_sync(0xffffffffu, sl0, 8));
+  cw = min(cw, __shfl_xor_sync(0xffffffffu, cw, 16));
+  int cm = max(sh0, __shfl_xor_sync(0xffffffffu, sh0, 8));
+  cm = max(cm, __shfl_xor_sync(0xffffffffu, cm, 16));
+  const bool any = cw != 0x7fffffff;
+  // Normally the 4 timesteps' stencils start within one grid point of each other and
+  // share one load from the earliest start; otherwise each timestep loads its own.
+  const bool wide = any && cm - cw > 1;  // W + 1 taps from cw cover starts cw and cw + 1
+  const int base = wide ? st : cw;
+  int code = -1;
+  if (dv && any) {
+    if (wide && !rval) {
+      code = kGrWide | 0xFFFF;
+    } else {
+      const int rr = base + lbase - r0;
+      const int pass = npass == 1 ? 0 : rr / kGrPassStride;
+      code = (wide ? kGrWide : 0) | (pass << 8) | (rr - pass * kGrPassStride);
+    }
+  }
+  float wt[W + 1];
+  grid_weights<W>(f, st - base == 1, p.wpoly, wt);  // starts differ by at most one without kGrWide
+  float cr, sr;
+  twiddle_turns(pa + static_cast<uint32_t>(c0) * pb, tab, cr, sr);
+  float4* my = reinterpret_cast<float4*>(dst);
+  my[0] = make_float4(wt[0], wt[1], wt[2], wt[3]);
+  my[1] = make_float4(wt[4], wt[5], wt[6], wt[7]);
+  my[2] = make_float4(wt[8], cr, sr, __int_as_float(code));
 }
 
 // Sum of TMEM regions into the first one, for this warp's 32 lanes and columns
@@ -468,32 +552,32 @@ __device__ __forceinline__ void grid_fold(uint32_t lanes, uint32_t dst, uint32_t
   asm volatile("tcgen05.wait::st.sync.aligned;" ::: "memory");
 }
 
-// The four correction MMAs of a 16-channel chunk (lo*hi and hi*lo of both k-steps) into one
-// accumulator, from one statement: acc0 = 0 overwrites the accumulator with the first.
-__device__ __forceinline__ void grid_mma_corrections(uint32_t d, uint64_t ah, uint64_t al, uint64_t bh, uint64_t bl,
-                                                     uint64_t ka, uint64_t kb, uint32_t idesc, uint32_t acc0) {
-  asm volatile(
-      "{\n\t.reg .pred p, t;\n\t"
-      "setp.ne.b32 p, %9, 0;\n\t"
-      "setp.eq.b32 t, %9, %9;\n\t"
-      "tcgen05.mma.cta_group::1.kind::tf32 [%0], %1, %2, %8, p;\n\t"
-      "tcgen05.mma.cta_group::1.kind::tf32 [%0], %3, %4, %8, t;\n\t"
-      "tcgen05.mma.cta_group::1.kind::tf32 [%0], %5, %6, %8, t;\n\t"
-      "tcgen05.mma.cta_group::1.kind::tf32 [%0], %7, %10, %8, t;\n\t}" ::"r"(d),
-      "l"(al), "l"(bh), "l"(ah), "l"(bl), "l"(al + ka), "l"(bh + kb), "l"(ah + ka), "r"(idesc), "r"(acc0), "l"(bl + kb)
-      : "memory");
+// Instruction descriptor, kind::f16: D = F32, A = B = F16, both K-major, dense.
+__host__ __device__ constexpr uint32_t grid_idesc_f16(int M, int N) {
+  return (1u << 4) | (static_cast<uint32_t>(N >> 3) << 17) | (static_cast<uint32_t>(M >> 4) << 24);
 }
 
-// The two hi*hi MMAs (both k-steps) of a chunk.
-__device__ __forceinline__ void grid_mma_hihi(uint32_t d, uint64_t ah, uint64_t bh, uint64_t ka, uint64_t kb,
-                                              uint32_t idesc, uint32_t acc0) {
+// The two correction MMAs of a 16-channel chunk (lo*hi and hi*lo) into one accumulator, from
+// one statement: acc0 = 0 overwrites the accumulator with the first.
+__device__ __forceinline__ void grid_mma_corrections(uint32_t d, uint64_t ah, uint64_t al, uint64_t bh, uint64_t bl,
+                                                     uint32_t idesc, uint32_t acc0) {
   asm volatile(
       "{\n\t.reg .pred p, t;\n\t"
       "setp.ne.b32 p, %6, 0;\n\t"
       "setp.eq.b32 t, %6, %6;\n\t"
-      "tcgen05.mma.cta_group::1.kind::tf32 [%0], %1, %2, %5, p;\n\t"
-      "tcgen05.mma.cta_group::1.kind::tf32 [%0], %3, %4, %5, t;\n\t}" ::"r"(d),
-      "l"(ah), "l"(bh), "l"(ah + ka), "l"(bh + kb), "r"(idesc), "r"(acc0)
+      "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %5, p;\n\t"
+      "tcgen05.mma.cta_group::1.kind::f16 [%0], %3, %4, %5, t;\n\t}" ::"r"(d),
+      "l"(al), "l"(bh), "l"(ah), "l"(bl), "r"(idesc), "r"(acc0)
+      : "memory");
+}
+
+// The hi*hi MMA of a chunk.
+__device__ __forceinline__ void grid_mma_hihi(uint32_t d, uint64_t ah, uint64_t bh, uint32_t idesc, uint32_t acc0) {
+  asm volatile(
+      "{\n\t.reg .pred p;\n\t"
+      "setp.ne.b32 p, %4, 0;\n\t"
+      "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}" ::"r"(d),
+      "l"(ah), "l"(bh), "r"(idesc), "r"(acc0)
       : "memory");
 }
 
@@ -502,18 +586,30 @@ __device__ __forceinline__ void tc_commit(uint64_t* bar) {
                : "memory");
 }
 
-// Sum a warp's per-lane sums over the 4 timesteps of its quad lanes and store them
-// (first) or add them to the unit's output: directions dbase .. dbase + nd of the item,
-// out[direction][pol][nbl] complex doubles.  Each output element has one writer lane.
-__device__ __forceinline__ void grid_flush(const float (&acc)[kGrWarpDirs], double2* out, int dbase, int nd, int b,
-                                           bool bval, int tl, int ps, int comp, int nbl, bool first) {
+// The 4 timestep lanes of a quad lane's row (lane bits 3 and 4) each hold one value per
+// direction of a batch (g[bb], direction jb + bb); sum them over the 4 timesteps and leave
+// direction jb + tl's sum in timestep lane tl (a reduce-scatter: 3 shuffles for 4 directions).
+__device__ __forceinline__ float grid_sum_timesteps(const float (&g)[kGrBatch], int tl) {
+  static_assert(kGrBatch == 4, "one direction per timestep lane");
+  const bool h = tl & 2, l = tl & 1;
+  float ka = h ? g[2] : g[0], kb = h ? g[3] : g[1];
+  ka += __shfl_xor_sync(0xffffffffu, h ? g[0] : g[2], 16);
+  kb += __shfl_xor_sync(0xffffffffu, h ? g[1] : g[3], 16);
+  return (l ? kb : ka) + __shfl_xor_sync(0xffffffffu, l ? ka : kb, 8);
+}
+
+// Store (first) or add a warp's sums to the unit's output: acc[k] is this lane's component
+// of direction 4 k + tl of the warp (summed over the 4 timesteps), directions dbase .. dbase
+// + nd of the item, out[direction][pol][nbl] complex doubles.  Each output element has one
+// writer lane.
+__device__ __forceinline__ void grid_flush(const float (&acc)[kGrWarpDirs / kGrBatch], double2* out, int dbase, int nd,
+                                           int b, bool bval, int tl, int ps, int comp, int nbl, bool first) {
 #pragma unroll
-  for (int j = 0; j < kGrWarpDirs; ++j) {
-    float v = acc[j] + __shfl_xor_sync(0xffffffffu, acc[j], 8);
-    v += __shfl_xor_sync(0xffffffffu, v, 16);
-    if (tl == 0 && bval && j < nd) {
+  for (int k = 0; k < kGrWarpDirs / kGrBatch; ++k) {
+    const int j = k * kGrBatch + tl;
+    if (bval && j < nd) {
       double* o = reinterpret_cast<double*>(out + (static_cast<int64_t>(dbase + j) * 4 + (ps >> 1)) * nbl + b);
-      o[comp] = first ? static_cast<double>(v) : o[comp] + static_cast<double>(v);
+      o[comp] = first ? static_cast<double>(acc[k]) : o[comp] + static_cast<double>(acc[k]);
     }
   }
 }
@@ -586,24 +682,21 @@ __global__ void __launch_bounds__(kGrThreads, 1) rotate_average_gridded(const Gr
                 ok = false;
                 break;
               }
-              mbar_arrive_expect_tx(&vfull[m], nq * (kGrOpBytes + 8 * w.jw * 32));
+              mbar_arrive_expect_tx(&vfull[m], nq * (kGrOpBytes + 4 * w.jw * 32));
               const int rg = w.rg0 + ps * (kGrPassStride / 8);
               const int tbi = g.t_lo / 4 + tb;  // the tile's timestep block in the integration
               for (int i = 0; i < nq; ++i) {
                 const int q = q0 + i;
                 unsigned char* st = ve + (m * kGrMacro + i) * kGrStageBytes;
                 // The chunk's A operand, hi and lo, already in the MMA layout.
-                bulk_copy_g2s(st, reinterpret_cast<const unsigned char*>(I.op) +
-                                      ((static_cast<int64_t>(g.quad) * I.ntb + tbi) * I.nchunk + q) * kGrOpBytes,
+                bulk_copy_g2s(st, I.op + ((static_cast<int64_t>(g.quad) * I.ntb + tbi) * I.nchunk + q) * kGrOpBytes,
                               kGrOpBytes, &vfull[m]);
 #pragma unroll
-                for (int ks = 0; ks < 2; ++ks)
-#pragma unroll
-                  for (int hl = 0; hl < 2; ++hl) {
-                    // Window grid points [8 rg, 8 rg + jw): 2 jw interleaved (re, im) rows.
-                    const float* src = I.etab + (static_cast<int64_t>((q * 2 + ks) * 2 + hl) * 2 * I.nrg + 2 * rg) * 64;
-                    bulk_copy_g2s(st + kGrEOffset + (hl * 2 + ks) * 2 * w.jw * 32, src, 2 * w.jw * 32, &vfull[m]);
-                  }
+                for (int hl = 0; hl < 2; ++hl) {
+                  // Window grid points [8 rg, 8 rg + jw): 2 jw interleaved (re, im) rows.
+                  const unsigned char* src = I.etab + (static_cast<int64_t>(q * 2 + hl) * 2 * I.nrg + 2 * rg) * 256;
+                  bulk_copy_g2s(st + kGrEOffset + hl * 2 * w.jw * 32, src, 2 * w.jw * 32, &vfull[m]);
+                }
               }
             }
       }
@@ -622,7 +715,7 @@ __global__ void __launch_bounds__(kGrThreads, 1) rotate_average_gridded(const Gr
         const GridUnit g = grid_unit(p, u);
         const GridItem& I = p.items[g.item];
         const GridWindow w = p.win[u];
-        const uint32_t idesc = tc_idesc_tf32(128, 2 * w.jw);
+        const uint32_t idesc = grid_idesc_f16(128, 2 * w.jw);
         const uint64_t adesc0 = tc_smem_desc(ve, kTcLbo, kTcSbo);
         const uint64_t edesc0 = tc_smem_desc(ve + kGrEOffset, kTcLbo, kTcSbo);
         for (int tb = 0; tb < g.ntb && ok; ++tb)
@@ -648,21 +741,20 @@ __global__ void __launch_bounds__(kGrThreads, 1) rotate_average_gridded(const Gr
               for (int i = 0; i < nq; ++i) {
                 const int q = q0 + i;
                 const int seg = q / kGrSegChunks, qs = q % kGrSegChunks;
-                // Descriptors of this stage: A hi/lo at +0 / +2*4096, E hi/lo at +0 / +4*jw*32 from
-                // their bases; k-step 1 is 4096 (A) or 2*jw*32 (E) bytes further (address field >> 4).
+                // Descriptors of this stage: A hi/lo at +0 / +kGrAHalf, E hi/lo at +0 / +2*jw*32 from
+                // their bases (address field >> 4).
                 const uint64_t so = static_cast<uint64_t>((m * kGrMacro + i) * (kGrStageBytes >> 4));
                 const uint64_t ah = adesc0 + so, bh = edesc0 + so;
-                const uint64_t al = ah + (2 * 4096 >> 4), bl = bh + static_cast<uint64_t>(4 * w.jw * 2);
-                const uint64_t ka = 4096 >> 4, kb = static_cast<uint64_t>(2 * w.jw * 2);
+                const uint64_t al = ah + (kGrAHalf >> 4), bl = bh + static_cast<uint64_t>(2 * w.jw * 2);
                 // Corrections first: they give the fold of the previous segment time to finish.
-                grid_mma_corrections(tmem + kGrAC, ah, al, bh, bl, ka, kb, idesc, q > 0 ? 1u : 0u);
+                grid_mma_corrections(tmem + kGrAC, ah, al, bh, bl, idesc, q > 0 ? 1u : 0u);
                 if (seg >= 2 && qs == 0 && !grid_wait(is_empty, (mids - 1) & 1, abort_flag)) {
                   grid_fail(p, abort_flag);
                   ok = false;
                   break;
                 }
                 const uint32_t dst = seg == 0 ? rs : tmem + kGrIS;
-                grid_mma_hihi(dst, ah, bh, ka, kb, idesc, qs > 0 ? 1u : 0u);
+                grid_mma_hihi(dst, ah, bh, idesc, qs > 0 ? 1u : 0u);
                 issued = true;
                 if (seg >= 1 && qs == kGrSegChunks - 1 && q != I.nchunk - 1) {
                   tc_commit(is_full);  // a middle segment, folded by the converters
@@ -734,7 +826,11 @@ __global__ void __launch_bounds__(kGrThreads, 1) rotate_average_gridded(const Gr
     const int half = e >> 2;       // which kGrWarpDirs directions of the unit
     const int quarter = warp & 3;  // TMEM lanes 32*quarter .. (hardware rule: warp id mod 4)
     const int tl = lane >> 3, ps = lane & 7, comp = lane & 1;
-    float* rec = rec_all + e * (32 * kGrRecWords);  // record (t, direction jj) at (8 t + jj) * kGrRecWords
+    const float sgn = comp ? 1.f : -1.f;
+    // Records of kGrRecDirs of the warp's directions at a time: record (t, j) at
+    // (t * kGrRecDirs + j % kGrRecDirs) * kGrRecWords.
+    float* rec = rec_all + e * (4 * kGrRecDirs * kGrRecWords);
+    float* rec_t = rec + tl * kGrRecDirs * kGrRecWords;  // this lane's timestep
     uint32_t blk = 0;
     bool ok = true;
     for (int sl = blockIdx.x; ok; sl += gridDim.x) {
@@ -753,16 +849,17 @@ __global__ void __launch_bounds__(kGrThreads, 1) rotate_average_gridded(const Gr
       // passes; with several, each (tile, pass, group) adds its sums to the unit's output in
       // order (the first stores), since every group's sums do not fit in registers.
       const bool keep = g.dg_hi - g.dg_lo == 1;
-      float acc[kGrWarpDirs];
+      float acc[kGrWarpDirs / kGrBatch];  // acc[k]: direction k * kGrBatch + tl, summed over timesteps
 #pragma unroll
-      for (int j = 0; j < kGrWarpDirs; ++j) acc[j] = 0.f;
+      for (int k = 0; k < kGrWarpDirs / kGrBatch; ++k) acc[k] = 0.f;
       for (int tb = 0; tb < g.ntb && ok; ++tb) {
         const int t = g.t_lo + tb * 4 + tl;
         const bool rval = bval && t < g.t_hi;
         const int64_t r = rval ? static_cast<int64_t>(t) * p.nbl + b : 0;
-        float x[6];
-#pragma unroll
-        for (int i = 0; i < 6; ++i) x[i] = __ldg(I.uvw_f + 6 * r + i);
+        // Undoes the operand's and the E table's scales of this lane's (baseline, pol).
+        const float sc =
+            __ldg(I.vinv + (static_cast<int64_t>(g.quad) * I.ntb + g.t_lo / 4 + tb) * 16 + quarter * 4 + (ps >> 1)) *
+            I.einv;
         for (int pp = 0; pp < w.npass; ++pp, ++blk) {
           const uint32_t rb = blk & 1;
           if (!grid_wait(&rs_full[rb], (blk >> 1) & 1, abort_flag)) {
@@ -773,93 +870,66 @@ __global__ void __launch_bounds__(kGrThreads, 1) rotate_average_gridded(const Gr
           asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
           const uint32_t tbase = tmem + (static_cast<uint32_t>(quarter * 32) << 16) + rb * kGrRegion;
           for (int dg = g.dg_lo; dg < g.dg_hi; ++dg) {
-          const int dbase = dg * kGrDirs + half * kGrWarpDirs;  // item-relative first direction of this warp
-          const int nd = max(0, min(kGrWarpDirs, I.ndir - dbase));
-          if (!keep) {
+            const int dbase = dg * kGrDirs + half * kGrWarpDirs;  // item-relative first direction of this warp
+            const int nd = max(0, min(kGrWarpDirs, I.ndir - dbase));
+            if (!keep) {
 #pragma unroll
-            for (int j = 0; j < kGrWarpDirs; ++j) acc[j] = 0.f;
-          }
-#pragma unroll
-          for (int gi = 0; gi < kGrWarpDirs / 8; ++gi) {
-            if (gi * 8 >= nd) break;
-            {
-              // This lane's record: direction gi*8 + ps at timestep tl.
-              const int dj = gi * 8 + ps;
-              const bool dv = dj < nd;
-              const int d = I.dir0 + dbase + min(dj, nd - 1);
-              float ka[6], kb[6];
-#pragma unroll
-              for (int i = 0; i < 6; ++i) {
-                ka[i] = __ldg(p.dirk + 12 * d + i);
-                kb[i] = __ldg(p.dirk + 12 * d + 6 + i);
-              }
-              const uint32_t pa = df_dot3_turns_u32(ka, x);
-              const uint32_t pb = df_dot3_turns_u32(kb, x);
-              float f;
-              const int i0 = grid_position(pb, n, f);
-              const int st = grid_stencil_start(i0, f);  // this row's stencil start
-              const int sl0 = rval ? st : 0x7fffffff, sh0 = rval ? st : -0x7fffffff;
-              int cw = min(sl0, __shfl_xor_sync(0xffffffffu, sl0, 8));
-              cw = min(cw, __shfl_xor_sync(0xffffffffu, cw, 16));
-              int cm = max(sh0, __shfl_xor_sync(0xffffffffu, sh0, 8));
-              cm = max(cm, __shfl_xor_sync(0xffffffffu, cm, 16));
-              const bool any = cw != 0x7fffffff;
-              // Normally the 4 timesteps' stencils start within one grid point of each other and
-              // share one load from the earliest start; otherwise each timestep loads its own.
-              const bool wide = any && cm - cw > 1;  // W + 1 taps from cw cover starts cw and cw + 1
-              const int base = wide ? st : cw;
-              int code = -1;
-              if (dv && any) {
-                if (wide && !rval) {
-                  code = kGrWide | 0xFFFF;
-                } else {
-                  const int rr = base + I.lbase - r0;
-                  const int pass = w.npass == 1 ? 0 : rr / kGrPassStride;
-                  code = (wide ? kGrWide : 0) | (pass << 8) | (rr - pass * kGrPassStride);
-                }
-              }
-              float wt[W + 1];
-              grid_weights<W>(any ? static_cast<float>(i0 - base) + f : 0.f, wt);
-              float cr, sr;
-              twiddle_turns(pa + static_cast<uint32_t>(c0) * pb, tab, cr, sr);
-              // Record: weights 0-8, then cr, sr, code.
-              float4* my = reinterpret_cast<float4*>(rec + (tl * 8 + ps) * kGrRecWords);
-              my[0] = make_float4(wt[0], wt[1], wt[2], wt[3]);
-              my[1] = make_float4(wt[4], wt[5], wt[6], wt[7]);
-              my[2] = make_float4(wt[8], cr, sr, __int_as_float(code));
+              for (int k = 0; k < kGrWarpDirs / kGrBatch; ++k) acc[k] = 0.f;
             }
-            __syncwarp();
 #pragma unroll
-            for (int jb = 0; jb < 8; jb += kGrBatch) {
-              // The batch's directions that read this pass with one shared load (codes are the
-              // same in every lane for those): their loads, one wait, then their sums.
-              uint32_t col[kGrBatch];
-              int live = 0;
+            for (int hr = 0; hr < kGrWarpDirs; hr += kGrRecDirs) {
+              if (hr >= nd) break;  // the same in every lane
+              {
+                // Lane (t, ps) computes the records of directions hr + ps and hr + 8 + ps at
+                // timestep t (independent chains); the records past nd say "no load".
+                float x[6];
 #pragma unroll
-              for (int bb = 0; bb < kGrBatch; ++bb) {
-                const int code = __float_as_int(rec[(tl * 8 + jb + bb) * kGrRecWords + 11]);
-                const bool use = code >= 0 && !(code & kGrWide) && ((code >> 8) & 255) == pp;
-                col[bb] = use ? 2u * static_cast<uint32_t>(code & 255) : 0u;
-                live |= (use ? 1 : 0) << bb;
+                for (int i = 0; i < 6; ++i) x[i] = __ldg(I.uvw_f + 6 * r + i);
+                const int j0 = hr + ps, j1 = j0 + 8;
+                const int d0 = I.dir0 + dbase + min(j0, nd - 1), d1 = I.dir0 + dbase + min(j1, nd - 1);
+                __syncwarp();
+                grid_record<W>(p, x, tab, d0, j0 < nd, rval, n, c0, I.lbase, r0, w.npass, rec_t + ps * kGrRecWords);
+                grid_record<W>(p, x, tab, d1, j1 < nd, rval, n, c0, I.lbase, r0, w.npass,
+                               rec_t + (ps + 8) * kGrRecWords);
+                __syncwarp();
               }
-              if (live) {
-                uint32_t v[kGrBatch][18];
-                grid_load_batch(tbase, col, v);
+#pragma unroll
+              for (int jb = hr; jb < hr + kGrRecDirs; jb += kGrBatch) {
+                if (jb >= nd) break;  // the same in every lane
+                // The batch's directions that read this pass with one shared load (codes are the
+                // same in every lane for those): loads and one wait per pair, then their sums.
+                const float* rb = rec_t + (jb - hr) * kGrRecWords;
+                uint32_t col[kGrBatch];
+                int code[kGrBatch];
+                int live = 0;
+#pragma unroll
+                for (int bb = 0; bb < kGrBatch; ++bb) {
+                  code[bb] = __float_as_int(rb[bb * kGrRecWords + 11]);
+                  const bool use = code[bb] >= 0 && !(code[bb] & kGrWide) && ((code[bb] >> 8) & 255) == pp;
+                  col[bb] = use ? 2u * static_cast<uint32_t>(code[bb] & 255) : 0u;
+                  live |= (use ? 1 : 0) << bb;
+                }
+                float gs[kGrBatch] = {0.f, 0.f, 0.f, 0.f};
+#pragma unroll
+                for (int bp = 0; bp < kGrBatch; bp += 2) {
+                  if ((live >> bp) & 3) {
+                    uint32_t v[2][18];
+                    grid_load_pair(tbase, col[bp], col[bp + 1], v);
+#pragma unroll
+                    for (int bb = 0; bb < 2; ++bb) {
+                      const float gsum = grid_tap_combine<W>(v[bb], rb + (bp + bb) * kGrRecWords, sgn);
+                      gs[bp + bb] = ((live >> (bp + bb)) & 1) ? gsum : 0.f;
+                    }
+                  }
+                }
 #pragma unroll
                 for (int bb = 0; bb < kGrBatch; ++bb)
-                  if (live & (1 << bb))
-                    acc[gi * 8 + jb + bb] += grid_tap_combine<W>(v[bb], rec + (tl * 8 + jb + bb) * kGrRecWords, comp);
-              }
-#pragma unroll
-              for (int bb = 0; bb < kGrBatch; ++bb) {
-                const int code = __float_as_int(rec[(tl * 8 + jb + bb) * kGrRecWords + 11]);
-                if (code >= 0 && (code & kGrWide))  // the kGrWide bit is the same in every lane
-                  acc[gi * 8 + jb + bb] += grid_wide_sum<W>(rec + (jb + bb) * kGrRecWords, tbase, comp, tl, pp);
+                  if (code[bb] >= 0 && (code[bb] & kGrWide))  // the kGrWide bit is the same in every lane
+                    gs[bb] += grid_wide_sum<W>(rec + (jb - hr + bb) * kGrRecWords, tbase, sgn, tl, pp);
+                acc[jb / kGrBatch] = fmaf(sc, grid_sum_timesteps(gs, tl), acc[jb / kGrBatch]);
               }
             }
-            __syncwarp();
-          }
-          if (!keep) grid_flush(acc, out, dbase, nd, b, bval, tl, ps, comp, p.nbl, tb == 0 && pp == 0);
+            if (!keep) grid_flush(acc, out, dbase, nd, b, bval, tl, ps, comp, p.nbl, tb == 0 && pp == 0);
           }
           asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
           __syncwarp();

@@ -26,17 +26,23 @@ int dispatch_pols(const RotateArgs& a, dim3 grid, int precision, cudaStream_t s)
   }
 }
 
-// Grid matrix of the gridded kernel for C channels (built once per channel count).
-const float* grid_table_for(leap_ctx* ctx, int C) {
+// Grid matrix of the gridded kernel for C channels (built once per channel count) and the
+// inverse of its scale.
+const unsigned char* grid_table_for(leap_ctx* ctx, int C, float& einv) {
   auto it = ctx->grid_tabs.find(C);
-  if (it != ctx->grid_tabs.end()) return it->second.as<float>();
+  if (it != ctx->grid_tabs.end()) {
+    einv = ctx->grid_einv.at(C);
+    return it->second.as<unsigned char>();
+  }
   if (ctx->capturing) return nullptr;
-  std::vector<float> tab;
-  grid_table(C, kGrTaps, kGrBeta, grid_lbase(C), grid_rows(C), tab);
+  std::vector<uint16_t> tab;
+  einv = grid_table(C, kGrTaps, kGrBeta, grid_lbase(C), grid_rows(C), tab);
   DeviceBuffer& b = ctx->grid_tabs[C];
-  if (b.ensure(sizeof(float) * tab.size()) != cudaSuccess) return nullptr;
-  if (cudaMemcpy(b.ptr, tab.data(), sizeof(float) * tab.size(), cudaMemcpyHostToDevice) != cudaSuccess) return nullptr;
-  return b.as<float>();
+  if (b.ensure(sizeof(uint16_t) * tab.size()) != cudaSuccess) return nullptr;
+  if (cudaMemcpy(b.ptr, tab.data(), sizeof(uint16_t) * tab.size(), cudaMemcpyHostToDevice) != cudaSuccess)
+    return nullptr;
+  ctx->grid_einv[C] = einv;
+  return b.as<unsigned char>();
 }
 
 // Rotate + average of every item through the gridded kernel (4-pol complex<float>
@@ -69,21 +75,27 @@ int gridded_stage(leap_ctx* ctx, const std::vector<WorkItem>& items, const doubl
     Integration& in = ctx->integ.at(w.slot);
     const int T = static_cast<int>(in.rows / nbl);
     const int C = in.channels;
+    const int64_t op_bytes = grid_operand_bytes(nbl, T, C);
     if (in.op_nbl != nbl) {
-      // The split grid operand: built once per upload (the visibilities read once, hi and lo
-      // written), then read by every gridded call on this integration.
+      // The split grid operand and its scales: built once per upload (the visibilities read
+      // twice, hi and lo written), then read by every gridded call on this integration.
       if (ctx->capturing) return fail(ctx, LEAP_ERR_INTERNAL, "grid operand missing while recording a graph");
-      LEAP_CUDA(in.op.ensure(static_cast<size_t>(grid_operand_bytes(nbl, T, C))), "alloc grid operand");
-      const dim3 og((nbl + 3) / 4, (T + 3) / 4, grid_chunks(C));
-      grid_split_operand<<<og, 128, 0, s>>>(in.vis.as<float>(), in.rows, nbl, T, C, (T + 3) / 4, in.op.as<float>());
+      LEAP_CUDA(in.op.ensure(static_cast<size_t>(op_bytes + grid_scale_bytes(nbl, T))), "alloc grid operand");
+      const dim3 og((nbl + 3) / 4, (T + 3) / 4);
+      grid_split_operand<<<og, 128, 0, s>>>(in.vis.as<float>(), in.rows, nbl, T, C, (T + 3) / 4,
+                                            in.op.as<unsigned char>(),
+                                            reinterpret_cast<float*>(in.op.as<unsigned char>() + op_bytes));
       LEAP_CUDA(cudaGetLastError(), "grid operand launch");
       ++kernels;
       in.op_nbl = nbl;
     }
-    const float* tab = grid_table_for(ctx, C);
+    float einv = 1.f;
+    const unsigned char* tab = grid_table_for(ctx, C, einv);
     if (!tab) return fail(ctx, LEAP_ERR_CUDA, "grid matrix unavailable for this channel count");
     GridItem& it = git[i];
-    it.op = in.op.as<float>();
+    it.op = in.op.as<unsigned char>();
+    it.vinv = reinterpret_cast<const float*>(in.op.as<unsigned char>() + op_bytes);
+    it.einv = einv;
     it.ntb = (T + 3) / 4;
     it.uvw_f = in.uvw_f.as<float>();
     it.etab = tab;
@@ -184,6 +196,7 @@ int gridded_stage(leap_ctx* ctx, const std::vector<WorkItem>& items, const doubl
   gp.nitems = static_cast<int32_t>(git.size());
   gp.units = units;
   gp.nbl = nbl;
+  es_kernel_poly(kGrTaps, kGrBeta, kGrPolyDeg, &gp.wpoly[0][0]);
   grid_windows<<<static_cast<unsigned>((static_cast<int64_t>(units) * 32 + 255) / 256), 256, 0, s>>>(gp);
   ++kernels;
   if (!ctx->grid_attr) {

@@ -67,9 +67,9 @@ struct Integration {
   int32_t channels = 0, pols = 0;
   bool has_map = false;
   CUtensorMap map16, map8;  // [channel][row*8 floats] views of a 4-pol complex<float> integration, box heights 16 / 8
-  // Split grid operand of the gridded kernel (TF32 hi/lo tiles in the MMA layout), built on
-  // the first gridded call after the visibilities change; op_nbl: the baseline count it was
-  // built for (0: none).
+  // Split grid operand of the gridded kernel (scaled FP16 hi/lo tiles in the MMA layout, then
+  // the inverse scales), built on the first gridded call after the visibilities change;
+  // op_nbl: the baseline count it was built for (0: none).
   DeviceBuffer op;
   int32_t op_nbl = 0;
   // Asynchronous ingestion: the upload runs on the context's copy stream and `ready`
@@ -128,6 +128,7 @@ struct leap_ctx {
   bool grid_attr = false;
   bool grid_shared_groups = false;    // gridded kernel: one grid product per tile for all direction groups
   std::map<int, DeviceBuffer> grid_tabs;  // grid matrix per channel count
+  std::map<int, float> grid_einv;         // ... and the inverse of its scale
   std::vector<GridItem> grid_items_host;
   std::vector<int32_t> grid_order_host;
   DeviceBuffer grid_items, grid_order, grid_win;

@@ -224,9 +224,9 @@ int32_t leap_set_autotune(leap_ctx* ctx, int32_t enable);
                                                     autotuner measures it faster; 2: always */
 #define LEAP_OPTION_GRIDDED_ROTATION 4         /* mixed form, 4-pol complex<float>: evaluate each row's channel sum
                                                     at every direction's phase slope through a 2x-oversampled grid
-                                                    (a type-2 non-uniform DFT): the grid values are one 3xTF32
-                                                    tcgen05 product per tile, shared by all directions, then a
-                                                    10-point interpolation per (row, direction).  0: never;
+                                                    (a type-2 non-uniform DFT): the grid values are one 3xFP16
+                                                    tcgen05 product per tile, shared by all directions, then an
+                                                    8-point interpolation per (row, direction).  0: never;
                                                     1: always; 2 (default): when every work item has at least
                                                     32 directions (unless the tensor-core rotation is forced) */
 #define LEAP_OPTION_GRAPH_REPLAY 5             /* leap_calibrate_batched: 1 (default) records a call's launches as

@@ -1,6 +1,6 @@
 """Gridded rotate + average (LEAP_OPTION_GRIDDED_ROTATION): the channel sum of every
 (row, pol) evaluated at each direction's phase slope through a 2x-oversampled grid,
-the grid values as one 3xTF32 tcgen05 product per tile.
+the grid values as one 3xFP16 tcgen05 product per tile (scaled FP16 hi/lo splits).
 
 Bars, as for the other mixed-form kernels: avgData within 2e-6 of the oracle's
 FP64 sums relative to the sum of |terms| of each (baseline, pol); per-antenna cal
