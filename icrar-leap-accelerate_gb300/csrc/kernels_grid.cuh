@@ -290,55 +290,55 @@ __device__ __forceinline__ void grid_fail(const GridParams& p, volatile int* abo
   *abort_flag = 1;
 }
 
-// Per unit: the range of interpolation stencil starts over its valid rows and
-// directions, as a window of E-table rows (one warp per unit).
-static __global__ void grid_windows(const GridParams p) {
-  const int u = static_cast<int>((blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x) >> 5);
-  const int lane = threadIdx.x & 31;
-  if (u >= p.units) return;
+// Grid window of each unit: the range of stencil starts over the unit's rows and its
+// direction groups.  One 64-thread block per unit: thread r takes rows r, r + 64, ... of the
+// unit (baseline r % 4 of the quad, timestep t_lo + r / 4), loads its UVWs once and walks the
+// directions, whose slopes the block stages in shared memory 64 at a time.
+constexpr int kGrWinThreads = 64;
+static __global__ void __launch_bounds__(kGrWinThreads) grid_windows(const GridParams p) {
+  __shared__ float kbs[kGrDirs][6];
+  __shared__ int red[2][kGrWinThreads / 32];
+  const int u = blockIdx.x;
   const GridUnit g = grid_unit(p, u);
   const GridItem& I = p.items[g.item];
   const int n = 2 * I.C;
+  const int nrow = (g.t_hi - g.t_lo) * 4;
   int smin = 0x7fffffff, smax = -0x7fffffff;
-  // Every direction group of the item: lanes hold the slopes of directions lane and
-  // lane + 32 of the group and walk the unit's rows; a row's UVWs are one broadcast load.
-  static_assert(kGrDirs == 64, "two directions per lane");
   for (int dg = g.dg_lo; dg < g.dg_hi; ++dg) {
     const int nd = min(kGrDirs, I.ndir - dg * kGrDirs);
-    float kb[2][6];
-    bool has[2];
+    __syncthreads();  // the previous group's slopes are no longer read
+    for (int i = threadIdx.x; i < nd * 6; i += kGrWinThreads)
+      kbs[i / 6][i % 6] = __ldg(p.dirk + 12 * (I.dir0 + dg * kGrDirs + i / 6) + 6 + i % 6);
+    __syncthreads();
+    for (int rr = threadIdx.x; rr < nrow; rr += kGrWinThreads) {
+      const int b = g.quad * 4 + (rr & 3), t = g.t_lo + (rr >> 2);
+      if (b >= p.nbl) continue;
+      const int64_t r = static_cast<int64_t>(t) * p.nbl + b;
+      float x[6];
 #pragma unroll
-    for (int h = 0; h < 2; ++h) {
-      const int dj = lane + 32 * h;
-      has[h] = dj < nd;
-      const int d = I.dir0 + dg * kGrDirs + min(dj, nd - 1);
-#pragma unroll
-      for (int i = 0; i < 6; ++i) kb[h][i] = __ldg(p.dirk + 12 * d + 6 + i);
-    }
-    for (int t = g.t_lo; t < g.t_hi; ++t) {
-#pragma unroll
-      for (int q = 0; q < 4; ++q) {
-        const int b = g.quad * 4 + q;
-        if (b >= p.nbl) continue;
-        const int64_t r = static_cast<int64_t>(t) * p.nbl + b;
-        float x[6];
-#pragma unroll
-        for (int i = 0; i < 6; ++i) x[i] = __ldg(I.uvw_f + 6 * r + i);
-#pragma unroll
-        for (int h = 0; h < 2; ++h) {
-          if (!has[h]) continue;
-          float f;
-          const int i0 = grid_position(df_dot3_turns_u32(kb[h], x), n, f);
-          const int s = grid_stencil_start(i0, f);
-          smin = min(smin, s);
-          smax = max(smax, s);
-        }
+      for (int i = 0; i < 6; ++i) x[i] = __ldg(I.uvw_f + 6 * r + i);
+      for (int d = 0; d < nd; ++d) {
+        float f;
+        const int i0 = grid_position(df_dot3_turns_u32(kbs[d], x), n, f);
+        const int st = grid_stencil_start(i0, f);
+        smin = min(smin, st);
+        smax = max(smax, st);
       }
     }
   }
   smin = __reduce_min_sync(0xffffffffu, smin);
   smax = __reduce_max_sync(0xffffffffu, smax);
-  if (lane == 0) {
+  if ((threadIdx.x & 31) == 0) {
+    red[0][threadIdx.x >> 5] = smin;
+    red[1][threadIdx.x >> 5] = smax;
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+#pragma unroll
+    for (int w = 1; w < kGrWinThreads / 32; ++w) {
+      smin = min(smin, red[0][w]);
+      smax = max(smax, red[1][w]);
+    }
     GridWindow w{0, 16, 0, 0};
     if (smin <= smax) {
       w.rg0 = (smin + I.lbase) >> 3;

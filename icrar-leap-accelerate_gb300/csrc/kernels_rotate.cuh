@@ -479,33 +479,43 @@ struct RefantItem {
 
 constexpr int kRefantPrefetch = 16;  // channel loads in flight per lane in the compensated pass
 
+// The compensated reference-antenna pass of one call: its work items, the reference
+// baselines, and the number of warp tasks (4 per block of the standalone launch).
+struct RefantParams {
+  const RefantItem* items;
+  const int32_t* I1;
+  double f0, df;
+  int32_t nitems, nbl, nI1, ntasks;
+};
+
+// One warp task of the compensated reference-antenna pass: task w is warp w % 4 of block
+// w / 4 of the standalone launch, i.e. directions j0, j0 + 1 of one group of 4*DPW, for the
+// 32 reference baselines of one tile (one per lane), over one (timestep, channel) slab.
+// tab is the double-float twiddle table in shared memory.  Lanes without a baseline, and
+// warps without a direction, have nothing to do (no warp-collective operations here).
 template <int DPW>
-__global__ void __launch_bounds__(128, 5) refant_average_df_items(const RefantItem* __restrict__ items, int nitems,
-                                                                 int nbl, double f0, double df,
-                                                                 const int32_t* __restrict__ I1, int nI1,
-                                                                 const float4* __restrict__ df_tab) {
-  __shared__ float4 tab[kTwiddleSize];
-  for (int i = threadIdx.x; i < kTwiddleSize; i += blockDim.x) tab[i] = __ldg(df_tab + i);
-  __syncthreads();
+__device__ __forceinline__ void refant_warp_task(const RefantParams& rp, int task, const float4* tab, int lane) {
+  const RefantItem* items = rp.items;
+  const int blk = task >> 2, warp = task & 3;
   int ii = 0;
-  while (ii + 1 < nitems && items[ii + 1].block_begin <= static_cast<int>(blockIdx.x)) ++ii;
+  while (ii + 1 < rp.nitems && items[ii + 1].block_begin <= blk) ++ii;
   const RefantItem it = items[ii];
   constexpr int NW = 4;
   const int nslab = it.n_tslab * it.n_cslab;
-  const int local = blockIdx.x - it.block_begin;
+  const int local = blk - it.block_begin;
   const int ktile = local / (it.dgroups * nslab);
   const int dg = (local / nslab) % it.dgroups;
   const int slab = local % nslab;
-  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   const int k = ktile * 32 + lane;
   const int j0 = (dg * NW + warp) * DPW;
   const int ts = slab / it.n_cslab, cs = slab % it.n_cslab;
   const int t_lo = ts * it.t_per_slab, t_hi = min(it.T, t_lo + it.t_per_slab);
   const int c_lo = cs * it.c_per_slab, c_hi = min(it.C, c_lo + it.c_per_slab);
+  const int nI1 = rp.nI1, nbl = rp.nbl;
   if (j0 >= it.ndir || k >= nI1) return;
-  int b = __ldg(I1 + k);
+  int b = __ldg(rp.I1 + k);
   if (b < 0) b += nbl;  // VectorRangeSelect wrap-around (LA/math/cpu/vector.h:97-104)
-  const double kA = f0 / kSpeedOfLight, kB = df / kSpeedOfLight;
+  const double kA = rp.f0 / kSpeedOfLight, kB = rp.df / kSpeedOfLight;
   static_assert(DPW == 2, "the two directions of a warp are the halves of paired instructions");
   DfAcc2 re{make_float2(0.f, 0.f), make_float2(0.f, 0.f)}, im = re;
   for (int t = t_lo; t < t_hi; ++t) {
@@ -552,6 +562,17 @@ __global__ void __launch_bounds__(128, 5) refant_average_df_items(const RefantIt
   if (j0 + 1 < it.ndir)
     out[static_cast<int64_t>(j0 + 1) * nI1 + k] = make_double2(static_cast<double>(re.s.y) + static_cast<double>(re.c.y),
                                                                static_cast<double>(im.s.y) + static_cast<double>(im.c.y));
+}
+
+// The pass as its own launch: rp.ntasks / 4 blocks of 4 warps.
+template <int DPW>
+__global__ void __launch_bounds__(128, 5) refant_average_df_items(const RefantParams rp,
+                                                                 const float4* __restrict__ df_tab) {
+  __shared__ float4 tab[kTwiddleSize];
+  for (int i = threadIdx.x; i < kTwiddleSize; i += blockDim.x) tab[i] = __ldg(df_tab + i);
+  __syncthreads();
+  refant_warp_task<DPW>(rp, static_cast<int>(blockIdx.x) * 4 + static_cast<int>(threadIdx.x >> 5), tab,
+                        static_cast<int>(threadIdx.x & 31));
 }
 
 // Sum of slab partials in slab order: avg[i] = sum_s partial[s][i].

@@ -197,7 +197,7 @@ int gridded_stage(leap_ctx* ctx, const std::vector<WorkItem>& items, const doubl
   gp.units = units;
   gp.nbl = nbl;
   es_kernel_poly(kGrTaps, kGrBeta, kGrPolyDeg, &gp.wpoly[0][0]);
-  grid_windows<<<static_cast<unsigned>((static_cast<int64_t>(units) * 32 + 255) / 256), 256, 0, s>>>(gp);
+  grid_windows<<<static_cast<unsigned>(units), kGrWinThreads, 0, s>>>(gp);
   ++kernels;
   if (!ctx->grid_attr) {
     LEAP_CUDA(cudaFuncSetAttribute(rotate_average_gridded<kGrTaps>, cudaFuncAttributeMaxDynamicSharedMemorySize,
@@ -483,9 +483,23 @@ int rotate_stage(leap_ctx* ctx, const std::vector<WorkItem>& items, const double
   return LEAP_OK;
 }
 
+// Sum of the reference-antenna pass's slab partials into ctx->avg_i1, on stream st (fixed order).
+int refant_reduce(leap_ctx* ctx, cudaStream_t st, int& kernels) {
+  const std::vector<ReduceItem>& red = ctx->refant_reduce_host;
+  if (red.empty()) return LEAP_OK;
+  const int nI1 = ctx->md.A1rows - 1;
+  int64_t maxn = 0;
+  for (const auto& r : red) maxn = std::max<int64_t>(maxn, static_cast<int64_t>(r.ndir) * nI1);
+  const dim3 rg(static_cast<unsigned>(std::min<int64_t>((maxn + 255) / 256, 1024)), static_cast<unsigned>(red.size()));
+  reduce_item_slabs<<<rg, 256, 0, st>>>(ctx->refant_reduce.as<ReduceItem>(), static_cast<int>(red.size()), nI1,
+                                         ctx->avg_i1.as<double2>());
+  ++kernels;
+  return LEAP_OK;
+}
+
 // Mixed form: compensated sums of pol 0 of the reference-antenna baselines into
-// ctx->avg_i1 ([D][nI1]), on the aux stream.  complex<float> items go through
-// one item-table launch; complex<double> items keep the FP64 kernel.
+// ctx->avg_i1 ([D][nI1]), on the aux stream.  complex<float> items go through one
+// item-table launch; complex<double> items keep the FP64 kernel.
 int refant_stage(leap_ctx* ctx, const std::vector<WorkItem>& items, const double* d_dd, int32_t D, int& kernels) {
   Metadata& md = ctx->md;
   const int32_t nbl = static_cast<int32_t>(md.k.nbaselines);
@@ -502,15 +516,16 @@ int refant_stage(leap_ctx* ctx, const std::vector<WorkItem>& items, const double
   int blocks = 0;
   // Each block sums 4*DPW directions of 32 reference baselines over a slab of
   // (timestep, channel) pairs.  Slabs are sized to one budget across items (about
-  // 32 blocks per SM in total, several waves of the 5 resident blocks), so that chunks
+  // 10 blocks per SM in total, two waves of the 5 resident blocks), so that chunks
   // of 1 x 48 and 64 x 384 samples give blocks of similar length instead of the same
-  // number of blocks each, and the last wave is a small part of the pass.
+  // number of blocks each; fewer, longer slabs also keep the partial sums (and their
+  // reduction) small.
   int64_t work_total = 0;
   for (const auto& w : items) {
     const Integration& in = ctx->integ.at(w.slot);
     work_total += (in.rows / nbl) * in.channels * rtiles * ((w.ndir + 7) / 8);
   }
-  const int64_t slab_budget = std::max<int64_t>(64, (work_total + 32 * ctx->sms - 1) / (32 * ctx->sms));
+  const int64_t slab_budget = std::max<int64_t>(64, (work_total + 10 * ctx->sms - 1) / (10 * ctx->sms));
   for (const auto& w : items) {
     Integration& in = ctx->integ.at(w.slot);
     const int T = static_cast<int>(in.rows / nbl);
@@ -594,17 +609,18 @@ int refant_stage(leap_ctx* ctx, const std::vector<WorkItem>& items, const double
                               cudaMemcpyHostToDevice, a),
               "upload refant reduce table");
   }
-  refant_average_df_items<2><<<blocks, 128, 0, a>>>(ctx->refant_items.as<RefantItem>(), static_cast<int>(rit.size()), nbl,
-                                                    md.k.freq_start_hz, md.k.freq_inc_hz, md.I1.as<int32_t>(), nI1,
-                                                    ctx->twiddle_df.as<float4>());
+  RefantParams rp{};
+  rp.items = ctx->refant_items.as<RefantItem>();
+  rp.I1 = md.I1.as<int32_t>();
+  rp.f0 = md.k.freq_start_hz;
+  rp.df = md.k.freq_inc_hz;
+  rp.nitems = static_cast<int32_t>(rit.size());
+  rp.nbl = nbl;
+  rp.nI1 = nI1;
+  rp.ntasks = blocks * 4;
+  refant_average_df_items<2><<<blocks, 128, 0, a>>>(rp, ctx->twiddle_df.as<float4>());
   ++kernels;
-  int64_t maxn = 0;
-  for (const auto& r : red) maxn = std::max<int64_t>(maxn, static_cast<int64_t>(r.ndir) * nI1);
-  const dim3 rg(static_cast<unsigned>(std::min<int64_t>((maxn + 255) / 256, 1024)), static_cast<unsigned>(red.size()));
-  reduce_item_slabs<<<rg, 256, 0, a>>>(ctx->refant_reduce.as<ReduceItem>(), static_cast<int>(red.size()), nI1,
-                                        ctx->avg_i1.as<double2>());
-  ++kernels;
-  return LEAP_OK;
+  return refant_reduce(ctx, a, kernels);
 }
 
 template <int N>
@@ -744,9 +760,10 @@ int calibrate_items(leap_ctx* ctx, const std::vector<WorkItem>& items, const dou
     LEAP_CUDA(cudaStreamWaitEvent(ctx->aux, ctx->fork, 0), "fork");
   }
   // The reference-antenna pass cannot share an SM with either bulk kernel (registers or shared
-  // memory).  Beside the gridded kernel it goes first, so that it overlaps the small kernels
-  // that set up the grid windows; beside the pipelined kernel it goes after it, so that the
-  // persistent blocks, whose unit schedule assumes they start together, take the SMs first.
+  // memory; running it on extra warps of the gridded kernel measured slower than two launches).
+  // Beside the gridded kernel it goes first, so that it overlaps the small kernels that set up
+  // the grid windows; beside the pipelined kernel it goes after it, so that the persistent
+  // blocks, whose unit schedule assumes they start together, take the SMs first.
   const bool refant_first = refant && uses_gridded(ctx, items, D, precision, P);
   int rc = LEAP_OK;
   if (refant_first) {
