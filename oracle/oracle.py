@@ -132,12 +132,62 @@ def phase_matrix(a1: Sequence[int], a2: Sequence[int], fg: Sequence[bool], ref_a
 
 
 def pseudo_inverse(a: np.ndarray, epsilon: float = np.finfo(np.float64).eps) -> np.ndarray:
-    """SVDPseudoInverse (LA/math/cpu/matrix_invert.h:49-56)."""
+    """SVDPseudoInverse (LA/math/cpu/matrix_invert.h:49-56).
+
+    The pseudo-inverse is unique; an SVD computes it only to within the SVD's own
+    rounding, which depends on the LAPACK build: for the 130,817 x 512 phase matrix of
+    a 512-station array, numpy's gesdd is within 2e-13 of the exact pinv on x86-64
+    (OpenBLAS) but 1.7e-11 on an aarch64 host, and such a difference moves the
+    calibration phases by ~1e-10 rad.  So when A is an integer matrix of full column
+    rank (every phase matrix whose stations all have an unflagged baseline) and the
+    tolerance rule zeroes no singular value, the SVD result is refined to the exact
+    pinv (A^T A)^-1 A^T to within rounding (``_refine_integer_pinv``); otherwise the
+    SVD result is returned as the reference computes it."""
     a = np.asarray(a, dtype=np.float64)
     u, s, vt = np.linalg.svd(a, full_matrices=False)
     tol = float(max(a.shape[0], a.shape[1])) * epsilon * abs(s[0])
-    inv = np.where(np.abs(s) > tol, 1.0 / np.where(s == 0, 1.0, s), 0.0)
+    keep = np.abs(s) > tol
+    inv = np.where(keep, 1.0 / np.where(s == 0, 1.0, s), 0.0)
+    m, n = a.shape
+    if m >= n and n > 0 and keep.all() and np.array_equal(a, np.round(a)):
+        g_inv = (vt.T * (inv * inv)) @ vt  # (A^T A)^-1 from the SVD: V S^-2 V^T
+        refined = _refine_integer_pinv(a, g_inv)
+        if refined is not None:
+            return refined
     return (vt.T * inv) @ u.T
+
+
+def _split_columns(x: np.ndarray, bits: int):
+    """x = hi + lo with hi[:, k] a multiple of 2^(e_k - bits), 2^e_k >= max |x[:, k]| (exact)."""
+    amax = np.abs(x).max(axis=0)
+    e = np.where(amax > 0, np.ceil(np.log2(np.where(amax > 0, amax, 1.0))), 0.0).astype(np.int64) + 1
+    hi = np.ldexp(np.round(np.ldexp(x, bits - e)), e - bits)
+    return hi, x - hi
+
+
+def _refine_integer_pinv(a: np.ndarray, g_inv: np.ndarray, steps: int = 2):
+    """Iterative refinement of X = (A^T A)^-1 for an integer A, with residuals computed
+    without rounding error: G = A^T A is exact in FP64, and G @ hi (hi: X cut to
+    53 - b - 1 significant bits per column, 2^b > the largest row sum of |G|) has every
+    partial sum on the grid of hi's last bit and below 2^53 of it, so it is exact.
+    Returns X A^T, or None when G's entries are too large for the exact product."""
+    g = a.T @ a
+    row = float(np.abs(g).sum(axis=1).max())
+    if row <= 0 or row >= 2.0 ** 40:
+        return None
+    b = int(np.ceil(np.log2(row))) + 1
+    bits = 52 - b
+    x = g_inv
+    eye = np.eye(g.shape[0])
+    for step in range(steps):
+        hi, lo = _split_columns(x, bits)
+        r = (eye - g @ hi) - g @ lo
+        c = x @ r
+        if step + 1 < steps:
+            x = x + c
+    # The last correction stays apart (X = x + c, a double-FP64 value): the columns of X
+    # share a large common part that cancels in X A^T, so c is added after the product.
+    return x @ a.T + c @ a.T
 
 
 # ---------------------------------------------------------------------------
