@@ -146,3 +146,28 @@ def test_pinv_identity_properties_synthetic():
     np.testing.assert_allclose(md.A1 @ md.Ad1 @ md.A1, md.A1, atol=1e-12)
     np.testing.assert_allclose(md.Ad, mdo.Ad, atol=1e-12)
     np.testing.assert_allclose(md.Ad1, mdo.Ad1, atol=1e-12)
+
+
+def _exact_phase_pinv(A: np.ndarray) -> np.ndarray:
+    """(A^T A)^-1 A^T in exact rational arithmetic, rounded once to FP64."""
+    import sympy
+    Am = sympy.Matrix(A.astype(int).tolist())
+    X = (Am.T * Am).inv() * Am.T
+    return np.array([[float(X[i, j]) for j in range(X.shape[1])] for i in range(X.shape[0])])
+
+
+@pytest.mark.parametrize("stations,keep,ref", [(9, 0.7, 0), (11, 0.85, None), (13, 0.6, None)])
+def test_oracle_pinv_of_phase_matrix_is_exact(stations, keep, ref):
+    # Full-column-rank phase matrices (0 / +-1 entries) of arrays whose station counts are
+    # not powers of two, with flagged baselines: the oracle's pinv must not depend on the
+    # LAPACK build, so it equals the exact pinv to within a few ulp of its largest entry,
+    # as does the library's.
+    rng = np.random.default_rng(stations)
+    a1, a2 = np.triu_indices(stations, 1)
+    fg = rng.random(a1.size) > keep
+    fg[:stations - 1] = False  # every station keeps a baseline
+    A, _ = oracle.phase_matrix(a1, a2, fg, ref)
+    exact = _exact_phase_pinv(A)
+    scale = np.abs(exact).max()
+    for got in (oracle.pseudo_inverse(A), lg.pseudo_inverse(A)):
+        assert np.abs(got - exact).max() <= 4 * np.finfo(np.float64).eps * scale
