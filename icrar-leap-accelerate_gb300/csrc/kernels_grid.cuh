@@ -881,16 +881,18 @@ __global__ void __launch_bounds__(kGrThreads, 1) rotate_average_gridded(const Gr
               if (hr >= nd) break;  // the same in every lane
               {
                 // Lane (t, ps) computes the records of directions hr + ps and hr + 8 + ps at
-                // timestep t (independent chains); the records past nd say "no load".
+                // timestep t; the records past nd say "no load".  (Written as a loop, the two
+                // records take fewer registers than two inlined calls: the kernel does not spill.)
                 float x[6];
 #pragma unroll
                 for (int i = 0; i < 6; ++i) x[i] = __ldg(I.uvw_f + 6 * r + i);
-                const int j0 = hr + ps, j1 = j0 + 8;
-                const int d0 = I.dir0 + dbase + min(j0, nd - 1), d1 = I.dir0 + dbase + min(j1, nd - 1);
                 __syncwarp();
-                grid_record<W>(p, x, tab, d0, j0 < nd, rval, n, c0, I.lbase, r0, w.npass, rec_t + ps * kGrRecWords);
-                grid_record<W>(p, x, tab, d1, j1 < nd, rval, n, c0, I.lbase, r0, w.npass,
-                               rec_t + (ps + 8) * kGrRecWords);
+#pragma unroll 1
+                for (int jj = 0; jj < 2; ++jj) {
+                  const int j = hr + ps + 8 * jj;
+                  grid_record<W>(p, x, tab, I.dir0 + dbase + min(j, nd - 1), j < nd, rval, n, c0, I.lbase, r0,
+                                 w.npass, rec_t + (ps + 8 * jj) * kGrRecWords);
+                }
                 __syncwarp();
               }
 #pragma unroll
