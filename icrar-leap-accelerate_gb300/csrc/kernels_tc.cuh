@@ -19,13 +19,16 @@
 // packed this way once per metadata upload, dphi once per call; a CTA moves
 // its two blocks in with plain bulk copies.
 //
-// One CTA = one (128-row M tile, N-column tile, 64-k block); 128 threads.
-// Warp 0 allocates (and finally frees) N TMEM columns; thread 0 issues the
-// copies and the 24 MMAs (8 k-steps x 3) and commits them to an mbarrier; the
-// four warps then read their 32 accumulator rows (TMEM lanes) with
-// tcgen05.ld and write FP64 partial sums.  Waits are bounded: on a timeout
-// the CTA sets the error word, still waits (bounded) for its copies, frees its
-// TMEM and returns.
+// One CTA = one (128-row M tile, N-column tile, run of 64-k blocks); 128
+// threads.  Warp 0 allocates (and finally frees) N TMEM columns; thread 0
+// streams the run through a ring of half-block stages (4 k-steps: the hi and
+// lo halves of both operands, four bulk copies), issues 12 MMAs (4 k-steps x
+// 3) per stage and commits them to the stage's mbarrier, and refills a stage
+// once its MMAs have completed while the next stage's MMAs run; the four warps
+// then read their 32 accumulator rows (TMEM lanes) with tcgen05.ld and write
+// FP64 partial sums.  Waits are bounded: on a timeout the CTA sets the error
+// word, still waits (bounded) for its copies and MMAs, frees its TMEM and
+// returns.
 #pragma once
 
 #include "leap_common.cuh"
@@ -113,23 +116,33 @@ __device__ __forceinline__ void tc_mma_tf32(uint32_t tmem, uint64_t adesc, uint6
       : "memory");
 }
 
+// Ring of the Ad contraction: stages of half a K block (4 k-steps of 8), sized so that the ring
+// holds about 192 KB of operands whatever N.
+template <int N>
+__host__ __device__ constexpr int tc_half_bytes() { return 2 * (kTcM + N) * (kTcKB / 2) * 4; }  // A, B: hi + lo
+template <int N>
+__host__ __device__ constexpr int tc_stages() { return N >= 256 ? 2 : (N >= 128 ? 3 : 4); }
+
 // N columns of FP32 accumulator per CTA; N is a multiple of 16 in [16, 256].
-// CTA (mt, nt, kc) accumulates K blocks [kc*kb_per_cta, ...) in TMEM, one
-// block at a time (load, 24 MMAs, wait), then writes partial[kc][d][s].
+// CTA (mt, nt, kc) accumulates K blocks [kc*kb_per_cta, ...) in TMEM through a ring of
+// tc_stages<N>() half-block stages: thread 0 keeps the copies of the next stages in flight
+// while the MMAs of the current one run (a stage is refilled once the MMAs that read it
+// have completed), then the four warps write partial[kc][d][s].
 template <int N>
 __global__ void __launch_bounds__(128, 1) tc_gemm_ad(const float* __restrict__ A_packed, const float* __restrict__ B_packed,
                                                      int S, int D, int kblocks, int kb_per_cta,
                                                      double* __restrict__ partial, int* __restrict__ err) {
   static_assert(N % 16 == 0 && N >= 16 && N <= 256, "N tile");
   constexpr int kCols = N <= 32 ? 32 : (N <= 64 ? 64 : (N <= 128 ? 128 : 256));  // power of two >= 32
-  constexpr int kBytesA = 2 * tc_block_bytes(kTcM);
-  constexpr int kBytesB = 2 * tc_block_bytes(N);
+  constexpr int kBlockA = tc_block_bytes(kTcM), kBlockB = tc_block_bytes(N);  // one split (hi or lo) of a block
+  constexpr int kHalfA = kBlockA / 2, kHalfB = kBlockB / 2;                   // 4 of its 8 k-step slabs
+  constexpr int kStage = tc_half_bytes<N>(), kStages = tc_stages<N>();
+  static_assert(kStage == 2 * kHalfA + 2 * kHalfB, "stage layout: [A hi][A lo][B hi][B lo]");
   extern __shared__ __align__(128) unsigned char tc_smem[];
-  unsigned char* sA = tc_smem;                 // [hi | lo], 128 rows
-  unsigned char* sB = tc_smem + kBytesA;       // [hi | lo], N rows
-  uint64_t* bars = reinterpret_cast<uint64_t*>(tc_smem + kBytesA + kBytesB);  // [0] loads, [1] MMAs
-  uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(bars + 2);
-  int* status = reinterpret_cast<int*>(tmem_slot + 1);  // 0 = MMAs of every block issued
+  uint64_t* full = reinterpret_cast<uint64_t*>(tc_smem + kStages * kStage);  // [kStages] copies landed
+  uint64_t* empty = full + kStages;                                          // [kStages] MMAs that read it done
+  uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(empty + kStages);
+  int* status = reinterpret_cast<int*>(tmem_slot + 1);  // 0 = MMAs of every block issued and completed
 
   const int mt = blockIdx.x, nt = blockIdx.y, kc = blockIdx.z;
   const int kb0 = kc * kb_per_cta, kb1 = min(kblocks, kb0 + kb_per_cta);
@@ -142,8 +155,10 @@ __global__ void __launch_bounds__(128, 1) tc_gemm_ad(const float* __restrict__ A
     asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
   }
   if (threadIdx.x == 0) {
-    mbar_init(&bars[0], 1);
-    mbar_init(&bars[1], 1);
+    for (int i = 0; i < kStages; ++i) {
+      mbar_init(&full[i], 1);
+      mbar_init(&empty[i], 1);
+    }
     fence_mbar_init();
     *status = 0;
   }
@@ -154,44 +169,73 @@ __global__ void __launch_bounds__(128, 1) tc_gemm_ad(const float* __restrict__ A
 
   if (threadIdx.x == 0) {
     constexpr uint32_t idesc = tc_idesc_tf32(kTcM, N);
-    constexpr uint32_t lboA = kTcLbo, lboB = kTcLbo, sbo = kTcSbo;
-    const unsigned char* aparts[2] = {sA, sA + tc_block_bytes(kTcM)};
-    const unsigned char* bparts[2] = {sB, sB + tc_block_bytes(N)};
-    for (int kb = kb0; kb < kb1; ++kb) {
-      const uint32_t phase = static_cast<uint32_t>(kb - kb0) & 1u;
-      const unsigned char* ga = reinterpret_cast<const unsigned char*>(A_packed) +
-                                (static_cast<int64_t>(mt) * kblocks + kb) * static_cast<int64_t>(kBytesA);
-      const unsigned char* gb = reinterpret_cast<const unsigned char*>(B_packed) +
-                                (static_cast<int64_t>(nt) * kblocks + kb) * static_cast<int64_t>(kBytesB);
-      mbar_arrive_expect_tx(&bars[0], kBytesA + kBytesB);
-      for (int off = 0; off < kBytesA; off += 16384)
-        bulk_copy_g2s(sA + off, ga + off, min(16384, kBytesA - off), &bars[0]);
-      for (int off = 0; off < kBytesB; off += 16384)
-        bulk_copy_g2s(sB + off, gb + off, min(16384, kBytesB - off), &bars[0]);
-      if (!mbar_wait_bounded(&bars[0], phase)) {
-        atomicOr(err, kDevErrTimeout);
-        *status = 1;
-        mbar_wait_bounded(&bars[0], phase);  // do not leave while the copies may still land
+    const int nu = 2 * (kb1 - kb0);  // half blocks
+    const unsigned char* ga0 = reinterpret_cast<const unsigned char*>(A_packed) +
+                               static_cast<int64_t>(mt) * kblocks * (2 * static_cast<int64_t>(kBlockA));
+    const unsigned char* gb0 = reinterpret_cast<const unsigned char*>(B_packed) +
+                               static_cast<int64_t>(nt) * kblocks * (2 * static_cast<int64_t>(kBlockB));
+    // Half block u of this CTA: k-step slabs 4h .. 4h + 3 of block kb0 + u / 2, from the hi and lo
+    // parts of each operand (a packed block is [hi: 8 slabs][lo: 8 slabs]).
+    auto issue = [&](int u) {
+      unsigned char* st = tc_smem + (u % kStages) * kStage;
+      const int64_t kb = kb0 + u / 2, h = u & 1;
+      const unsigned char* ga = ga0 + kb * (2 * kBlockA) + h * kHalfA;
+      const unsigned char* gb = gb0 + kb * (2 * kBlockB) + h * kHalfB;
+      mbar_arrive_expect_tx(&full[u % kStages], kStage);
+      bulk_copy_g2s(st, ga, kHalfA, &full[u % kStages]);
+      bulk_copy_g2s(st + kHalfA, ga + kBlockA, kHalfA, &full[u % kStages]);
+      bulk_copy_g2s(st + 2 * kHalfA, gb, kHalfB, &full[u % kStages]);
+      bulk_copy_g2s(st + 2 * kHalfA + kHalfB, gb + kBlockB, kHalfB, &full[u % kStages]);
+    };
+    int issued = 0, waited = 0, committed = 0;  // units copied / landed / whose MMAs were committed
+    for (; issued < min(kStages, nu); ++issued) issue(issued);
+    bool ok = true;
+    for (int u = 0; u < nu && ok; ++u) {
+      const int sidx = u % kStages;
+      if (!mbar_wait_bounded(&full[sidx], (u / kStages) & 1)) {
+        ok = false;
         break;
       }
+      waited = u + 1;
       asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+      const unsigned char* st = tc_smem + sidx * kStage;
 #pragma unroll
-      for (int ks = 0; ks < kTcKB / 8; ++ks) {
-        const int ao = ks * kTcM * 32, bo = ks * N * 32;
-        tc_mma_tf32(tmem, tc_smem_desc(aparts[0] + ao, lboA, sbo), tc_smem_desc(bparts[0] + bo, lboB, sbo), idesc,
-                    (kb > kb0 || ks > 0) ? 1u : 0u);
-        tc_mma_tf32(tmem, tc_smem_desc(aparts[0] + ao, lboA, sbo), tc_smem_desc(bparts[1] + bo, lboB, sbo), idesc, 1u);
-        tc_mma_tf32(tmem, tc_smem_desc(aparts[1] + ao, lboA, sbo), tc_smem_desc(bparts[0] + bo, lboB, sbo), idesc, 1u);
+      for (int ks = 0; ks < kTcKB / 16; ++ks) {
+        const uint64_t ah = tc_smem_desc(st + ks * kTcM * 32, kTcLbo, kTcSbo);
+        const uint64_t al = tc_smem_desc(st + kHalfA + ks * kTcM * 32, kTcLbo, kTcSbo);
+        const uint64_t bh = tc_smem_desc(st + 2 * kHalfA + ks * N * 32, kTcLbo, kTcSbo);
+        const uint64_t bl = tc_smem_desc(st + 2 * kHalfA + kHalfB + ks * N * 32, kTcLbo, kTcSbo);
+        tc_mma_tf32(tmem, ah, bh, idesc, (u > 0 || ks > 0) ? 1u : 0u);
+        tc_mma_tf32(tmem, ah, bl, idesc, 1u);
+        tc_mma_tf32(tmem, al, bh, idesc, 1u);
       }
       asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
-                       smem_u32(&bars[1]))
+                       smem_u32(&empty[sidx]))
                    : "memory");
-      // The next block's copies overwrite the operands: wait for these MMAs first.
-      if (!mbar_wait_bounded(&bars[1], phase)) {
+      committed = u + 1;
+      // The previous unit's stage is refilled once its MMAs have completed (this unit's run meanwhile).
+      const int v = u - 1;
+      if (v >= 0 && v + kStages < nu) {
+        if (!mbar_wait_bounded(&empty[v % kStages], (v / kStages) & 1)) {
+          ok = false;
+          break;
+        }
+        issue(v + kStages);
+        ++issued;
+      }
+    }
+    if (!ok) {
+      atomicOr(err, kDevErrTimeout);
+      *status = 1;
+      // Do not leave while copies may still land in shared memory.
+      for (int j = waited; j < issued; ++j) mbar_wait_bounded(&full[j % kStages], (j / kStages) & 1);
+    }
+    // No MMA may be in flight when the accumulator is read or TMEM is freed (commits complete in order).
+    if (committed > 0) {
+      const int c = committed - 1;
+      if (!mbar_wait_bounded(&empty[c % kStages], (c / kStages) & 1)) {
         atomicOr(err, kDevErrTimeout);
         *status = 1;
-        mbar_wait_bounded(&bars[1], phase);  // one more bounded chance before TMEM is freed
-        break;
       }
     }
   }
@@ -236,7 +280,10 @@ __global__ void __launch_bounds__(128, 1) tc_gemm_ad(const float* __restrict__ A
 
 template <int N>
 __host__ __device__ constexpr int tc_gemm_smem_bytes() {
-  return 2 * tc_block_bytes(kTcM) + 2 * tc_block_bytes(N) + 64;
+  return tc_stages<N>() * tc_half_bytes<N>() + 16 * tc_stages<N>() + 16;
 }
+static_assert(tc_gemm_smem_bytes<256>() <= 227 * 1024 && tc_gemm_smem_bytes<128>() <= 227 * 1024 &&
+                  tc_gemm_smem_bytes<64>() <= 227 * 1024 && tc_gemm_smem_bytes<32>() <= 227 * 1024,
+              "ring of the Ad contraction within one block's shared memory");
 
 }  // namespace leapgb
