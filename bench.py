@@ -342,7 +342,7 @@ def per_direction_bytes(samples: float, rows: float, nbl: int, ndir: int) -> flo
     return ndir * (samples * 8 + rows * 24) + ndir * nbl * 4 * 16
 
 
-def grid_windows_host(obs, dds: np.ndarray, taps: int = 8, jw_max: int = 64, stride: int = 56, load: int = 9):
+def grid_windows_host(obs, dds: np.ndarray, taps: int = 10, jw_max: int = 64, stride: int = 48, load: int = 11):
     """The gridded kernel's grid windows of one call, computed as its grid_windows kernel does
     (one window per quad of baselines over all directions): (tensor-core FLOPs per call, mean
     passes per tile, max passes)."""
@@ -756,7 +756,7 @@ def run_workload(name, args, torch, lg, local, rank, world, dist, steps, warmup,
     cal_main = w.result()
     gridded = uses_gridded(args, w, prec, lg)
     if gridded and name in ("mwa", "ska_low"):
-        w.kernel_name = ("rotate_average_gridded<8> (3xFP16 tcgen05 grid product + 8-point interpolation per "
+        w.kernel_name = ("rotate_average_gridded<10> (3xFP16 tcgen05 grid product + 10-point interpolation per "
                          "direction) + grid_windows + the compensated reference-antenna pass")
         w.traffic = getattr(w, "grid_traffic", None)
     elif name in ("mwa", "ska_low"):

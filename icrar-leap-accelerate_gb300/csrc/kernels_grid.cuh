@@ -14,9 +14,11 @@
 // over the W grid points nearest n B, with psi the "exponential of semicircle"
 // kernel psi(x) = exp(beta (sqrt(1 - (2x/W)^2) - 1)) and Psi its Fourier
 // transform at frequency k / n (Barnett, Magland & af Klinteberg, SIAM J. Sci.
-// Comput. 41 (2019) C479).  With W = 8, beta = 2.3 W the interpolation error is
-// about 1e-7 of the l2 norm of f (their rule for a 2x grid: W = log10(1/eps) + 1;
-// W = 7 was measured too coarse for 16-station arrays, whose solve averages little).
+// Comput. 41 (2019) C479).  With W = 10, beta = 2.3 W the interpolation error is
+// about 1e-9 of the l2 norm of f (their rule for a 2x grid: W = log10(1/eps) + 1).
+// W = 8 (error ~1e-7) was measured too coarse for long integrations: the error of a
+// bright source's fringe adds coherently over timesteps while the averages of
+// directions away from it do not, and a 47-timestep chunk reached 2e-5 rad.
 // Per (row, direction) the work is W + 1 complex multiply-adds instead of C, so the
 // direction count no longer multiplies the channel work; the channel work moves to
 // the tensor cores.
@@ -33,19 +35,20 @@
 // component near 2^14 and the grid matrix by one for the whole table, so both splits stay
 // in FP16's normal range; the epilogue undoes the scales exactly.  The tensor cores
 // accumulate FP32 with truncation, whose error
-// grows with the number of accumulation steps and the size of the accumulator; so the
-// large hi*hi products restart in a fresh accumulator every 64 channels (a "segment")
-// and the small corrections go to an accumulator of their own.  Converter warps add
-// the segments together with rounded FP32 adds.  Measured on 128 antennas x 384
-// channels this keeps the averages within ~5e-7 of the FP64 sums (relative to the
-// sum of |terms|).
+// grows with the number of accumulation steps and the size of the accumulator, and is
+// biased (toward zero), so it too adds coherently over timesteps; so the large hi*hi
+// products restart in a fresh accumulator every 64 channels (a "segment") and the small
+// corrections go to an accumulator of their own.  Fold warps add the segments together
+// with rounded FP32 adds.  Emulated on a 47-timestep, 384-channel chunk of 128
+// antennas, the truncation is then the largest error left, ~1e-7 of the sum of |terms|.
+// (32-channel segments measured 5% slower at 128 antennas, with no lower maximum error.)
 //
 // TMEM (512 columns, one block per SM): RS[0], RS[1] (running sums, double
 // buffered: the epilogue reads one while the next tile accumulates into the
 // other), IS (segments 1.. of the current tile), AC (corrections).  Column 2j of
 // a region holds sum V_s Re E at window grid point j, column 2j + 1 sum V_s Im E
 // (the grid matrix interleaves its re and im rows), so the W + 1 taps of one
-// stencil are 2 (W + 1) = 18 adjacent columns: a 16- and a 2-column tcgen05.ld.
+// stencil are 2 (W + 1) = 22 adjacent columns: a 16-, a 4- and a 2-column tcgen05.ld.
 //
 // Operands.  The tile's visibilities reach shared memory already scaled and split into
 // FP16 hi and lo parts in the MMA's canonical K-major layout: grid_split_operand builds
@@ -69,16 +72,16 @@
 
 namespace leapgb {
 
-constexpr int kGrTaps = 8;            // W, grid points per interpolation
-constexpr float kGrBeta = 18.4f;      // 2.3 W
+constexpr int kGrTaps = 10;           // W, grid points per interpolation
+constexpr float kGrBeta = 23.0f;      // 2.3 W
 constexpr int kGrChunk = 16;          // channels per stage
 constexpr int kGrSegChunks = 4;       // chunks per hi*hi accumulation segment (64 channels)
 constexpr int kGrStages = 6;          // {visibility box / A hi, A lo, E window} ring
 constexpr int kGrMacro = 2;           // chunks handed over per barrier round (stages go in pairs)
 constexpr int kGrMacroStages = kGrStages / kGrMacro;
 constexpr int kGrJwMax = 64;          // grid points per pass (MMA N = 2 Jw <= 128)
-constexpr int kGrPassStride = 56;     // grid points between pass windows (multiple of 8)
-constexpr int kGrLoadCols = 9;        // grid points one interpolation load reads (2 TMEM columns each)
+constexpr int kGrPassStride = 48;     // grid points between pass windows (multiple of 8)
+constexpr int kGrLoadCols = kGrTaps + 1;  // grid points one interpolation load reads (2 TMEM columns each)
 constexpr int kGrPolyDeg = 8;         // degree of the per-tap weight polynomials
 constexpr int kGrBatch = 4;           // directions per timestep reduce-scatter (loads go in pairs)
 constexpr int kGrDirs = 64;           // directions per unit (8 epilogue warps x 32 / 4 quarters)
@@ -92,7 +95,8 @@ constexpr int kGrEBytes = 2 * 2 * kGrJwMax * kGrChunk * 2;  // [hl][2 Jw rows x 
 // Stage: [A hi][A lo][E hi][E lo]
 constexpr int kGrStageBytes = kGrOpBytes + kGrEBytes;
 constexpr int kGrEOffset = kGrOpBytes;
-constexpr int kGrRecWords = 12;                          // per (direction, timestep) record: 3 16-byte rows
+constexpr int kGrRecWords = 16;                          // per (direction, timestep) record: 4 16-byte rows
+constexpr int kGrCodeWord = kGrTaps + 3;                 // record: W + 1 weights, cr, sr, then the load code
 constexpr int kGrRecDirs = 16;                           // directions whose records a warp holds at a time
 constexpr int kGrRecBytes = kGrEpiWarps * 4 * kGrRecDirs * kGrRecWords * 4;  // [warps][4 t][16 dirs][12]
 constexpr uint32_t kGrRegion = 128;                      // TMEM columns per region
@@ -104,6 +108,7 @@ constexpr int kGrNumBars = 2 * kGrMacroStages + 8;
 // columns one load reads past the stencil.
 static_assert(kGrPassStride % 8 == 0 && kGrPassStride - 1 + kGrLoadCols <= kGrJwMax, "pass windows");
 static_assert(kGrTaps + 1 <= kGrLoadCols, "one load per stencil");
+static_assert(kGrCodeWord < kGrRecWords, "record layout");
 
 __host__ __device__ constexpr int grid_smem_bytes() {
   return kGrStages * kGrStageBytes + kTwiddleSize * 8 + kGrRecBytes + kGrNumBars * 8 + 16;
@@ -216,7 +221,8 @@ struct GridParams {
   int* err;
   int32_t nslots, nitems, units, nbl;
   // Weight polynomials: tap m of a stencil at fractional grid position f has weight
-  // sum_j wpoly[m][j] x^j, x = 2 f - 1 (es_kernel_poly on the host).
+  // sum_j wpoly[m][j] x^j, x = 2 f - 1 (es_kernel_poly on the host; the kernel reads the
+  // rows m < W / 2 and mirrors them).
   float wpoly[kGrTaps][kGrPolyDeg + 1];
 };
 
@@ -359,19 +365,28 @@ static __global__ void __launch_bounds__(kGrWinThreads) grid_windows(const GridP
 
 // The W + 1 weights of a shared load for a stencil at fractional grid position f that starts
 // `shifted` (0 or 1) columns after the load: w[k] = h_{k - shifted}(f), 0 outside the W taps,
-// with h_m the tap polynomials of c (degree kGrPolyDeg in x = 2 f - 1; the weight error is
-// about 1e-7 of the largest weight, FP32 Horner rounding included).
+// with h_m the tap polynomials of c (degree kGrPolyDeg in x = 2 f - 1).  psi is even, so tap
+// W - 1 - m is tap m mirrored, h_{W-1-m}(x) = h_m(-x): each pair is evaluated from the even and
+// odd parts of h_m in y = x^2 (half the multiply-adds of W separate Horner chains, and chains
+// half as long).  Only rows m < W / 2 of c are read.  The weight error is about 8e-8 of the
+// largest weight, FP32 rounding included.
 template <int W>
 __device__ __forceinline__ void grid_weights(float f, bool shifted, const float (&c)[W][kGrPolyDeg + 1],
                                              float (&w)[W + 1]) {
+  static_assert(W % 2 == 0 && kGrPolyDeg % 2 == 0, "tap pairs; even and odd parts of an even degree");
   const float x = fmaf(2.0f, f, -1.0f);
+  const float y = x * x;
   float h[W];
 #pragma unroll
-  for (int m = 0; m < W; ++m) {
-    float a = c[m][kGrPolyDeg];
+  for (int m = 0; m < W / 2; ++m) {
+    float e = c[m][kGrPolyDeg];
 #pragma unroll
-    for (int j = kGrPolyDeg - 1; j >= 0; --j) a = fmaf(a, x, c[m][j]);
-    h[m] = a;
+    for (int j = kGrPolyDeg - 2; j >= 0; j -= 2) e = fmaf(e, y, c[m][j]);
+    float o = c[m][kGrPolyDeg - 1];
+#pragma unroll
+    for (int j = kGrPolyDeg - 3; j >= 1; j -= 2) o = fmaf(o, y, c[m][j]);
+    h[m] = fmaf(x, o, e);
+    h[W - 1 - m] = fmaf(-x, o, e);
   }
   w[0] = shifted ? 0.f : h[0];
 #pragma unroll
@@ -379,24 +394,44 @@ __device__ __forceinline__ void grid_weights(float f, bool shifted, const float 
   w[W] = shifted ? h[W - 1] : 0.f;
 }
 
-// Two directions' stencils from TMEM: a 16- and a 2-column load each (the W + 1 taps, re
-// and im interleaved) at columns c0 and c1 of this warp's lanes, and one wait for both.
-__device__ __forceinline__ void grid_load_pair(uint32_t tbase, uint32_t c0, uint32_t c1, uint32_t (&v)[2][18]) {
-  static_assert(kGrLoadCols == 9, "18 columns per stencil");
+// Two directions' stencils from TMEM: a 16-, a 4- and a 2-column load each (the W + 1 = 11
+// taps, re and im interleaved) at columns c0 and c1 of this warp's lanes, and one wait for both.
+constexpr int kGrLoadRegs = 2 * kGrLoadCols;
+static_assert(kGrLoadRegs == 22, "22 columns per stencil: x16 + x4 + x2 loads");
+__device__ __forceinline__ void grid_load_pair(uint32_t tbase, uint32_t c0, uint32_t c1,
+                                               uint32_t (&v)[2][kGrLoadRegs]) {
   // All loads and the wait in one statement: the results are defined only after the wait.
   asm volatile(
-      "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%36];\n\t"
-      "tcgen05.ld.sync.aligned.32x32b.x2.b32 {%16,%17}, [%37];\n\t"
-      "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%18,%19,%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31,%32,%33}, [%38];\n\t"
-      "tcgen05.ld.sync.aligned.32x32b.x2.b32 {%34,%35}, [%39];\n\t"
+      "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%44];\n\t"
+      "tcgen05.ld.sync.aligned.32x32b.x4.b32 {%16,%17,%18,%19}, [%45];\n\t"
+      "tcgen05.ld.sync.aligned.32x32b.x2.b32 {%20,%21}, [%46];\n\t"
+      "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%22,%23,%24,%25,%26,%27,%28,%29,%30,%31,%32,%33,%34,%35,%36,%37}, [%47];\n\t"
+      "tcgen05.ld.sync.aligned.32x32b.x4.b32 {%38,%39,%40,%41}, [%48];\n\t"
+      "tcgen05.ld.sync.aligned.32x32b.x2.b32 {%42,%43}, [%49];\n\t"
       "tcgen05.wait::ld.sync.aligned;"
       : "=r"(v[0][0]), "=r"(v[0][1]), "=r"(v[0][2]), "=r"(v[0][3]), "=r"(v[0][4]), "=r"(v[0][5]), "=r"(v[0][6]),
         "=r"(v[0][7]), "=r"(v[0][8]), "=r"(v[0][9]), "=r"(v[0][10]), "=r"(v[0][11]), "=r"(v[0][12]), "=r"(v[0][13]),
-        "=r"(v[0][14]), "=r"(v[0][15]), "=r"(v[0][16]), "=r"(v[0][17]),
+        "=r"(v[0][14]), "=r"(v[0][15]), "=r"(v[0][16]), "=r"(v[0][17]), "=r"(v[0][18]), "=r"(v[0][19]),
+        "=r"(v[0][20]), "=r"(v[0][21]),
         "=r"(v[1][0]), "=r"(v[1][1]), "=r"(v[1][2]), "=r"(v[1][3]), "=r"(v[1][4]), "=r"(v[1][5]), "=r"(v[1][6]),
         "=r"(v[1][7]), "=r"(v[1][8]), "=r"(v[1][9]), "=r"(v[1][10]), "=r"(v[1][11]), "=r"(v[1][12]), "=r"(v[1][13]),
-        "=r"(v[1][14]), "=r"(v[1][15]), "=r"(v[1][16]), "=r"(v[1][17])
-      : "r"(tbase + c0), "r"(tbase + c0 + 16u), "r"(tbase + c1), "r"(tbase + c1 + 16u));
+        "=r"(v[1][14]), "=r"(v[1][15]), "=r"(v[1][16]), "=r"(v[1][17]), "=r"(v[1][18]), "=r"(v[1][19]),
+        "=r"(v[1][20]), "=r"(v[1][21])
+      : "r"(tbase + c0), "r"(tbase + c0 + 16u), "r"(tbase + c0 + 20u), "r"(tbase + c1), "r"(tbase + c1 + 16u),
+        "r"(tbase + c1 + 20u));
+}
+
+// One stencil from TMEM (a 16-, a 4- and a 2-column load) and its wait.
+__device__ __forceinline__ void grid_load_one(uint32_t a0, uint32_t (&v)[kGrLoadRegs]) {
+  asm volatile(
+      "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%22];\n\t"
+      "tcgen05.ld.sync.aligned.32x32b.x4.b32 {%16,%17,%18,%19}, [%23];\n\t"
+      "tcgen05.ld.sync.aligned.32x32b.x2.b32 {%20,%21}, [%24];\n\t"
+      "tcgen05.wait::ld.sync.aligned;"
+      : "=r"(v[0]), "=r"(v[1]), "=r"(v[2]), "=r"(v[3]), "=r"(v[4]), "=r"(v[5]), "=r"(v[6]), "=r"(v[7]), "=r"(v[8]),
+        "=r"(v[9]), "=r"(v[10]), "=r"(v[11]), "=r"(v[12]), "=r"(v[13]), "=r"(v[14]), "=r"(v[15]), "=r"(v[16]),
+        "=r"(v[17]), "=r"(v[18]), "=r"(v[19]), "=r"(v[20]), "=r"(v[21])
+      : "r"(a0), "r"(a0 + 16u), "r"(a0 + 20u));
 }
 
 // One direction of one lane: the W + 1 taps v (re, im interleaved) weighted by the
@@ -404,30 +439,37 @@ __device__ __forceinline__ void grid_load_pair(uint32_t tbase, uint32_t c0, uint
 // partner lane (the other component of the same visibility); returns this lane's
 // component of the rotated sum.  sgn is -1 on the real lane (comp 0), +1 on the imaginary.
 template <int W>
-__device__ __forceinline__ float grid_tap_combine(const uint32_t (&v)[18], const float* rec, float sgn) {
-  static_assert(W + 1 == 9, "record layout: 9 weights, then cr, sr, code");
-  const float4 q0 = reinterpret_cast<const float4*>(rec)[0], q1 = reinterpret_cast<const float4*>(rec)[1];
-  const float4 q2 = reinterpret_cast<const float4*>(rec)[2];
-  const float w[9] = {q0.x, q0.y, q0.z, q0.w, q1.x, q1.y, q1.z, q1.w, q2.x};
+__device__ __forceinline__ float grid_tap_combine(const uint32_t (&v)[kGrLoadRegs], const float* rec, float sgn) {
+  static_assert(W + 1 == kGrLoadCols && kGrRecWords == 16, "record layout: W + 1 weights, then cr, sr, code");
+  float r[16];
+#pragma unroll
+  for (int i = 0; i < 4; ++i) {
+    const float4 q = reinterpret_cast<const float4*>(rec)[i];
+    r[4 * i] = q.x;
+    r[4 * i + 1] = q.y;
+    r[4 * i + 2] = q.z;
+    r[4 * i + 3] = q.w;
+  }
   // Two chains per sum (even and odd taps) halve the dependent FMA latency.
   float P0 = 0.f, P1 = 0.f, Q0 = 0.f, Q1 = 0.f;
 #pragma unroll
   for (int k = 0; k <= W; ++k) {
     if (k & 1) {
-      P1 = fmaf(w[k], __uint_as_float(v[2 * k]), P1);
-      Q1 = fmaf(w[k], __uint_as_float(v[2 * k + 1]), Q1);
+      P1 = fmaf(r[k], __uint_as_float(v[2 * k]), P1);
+      Q1 = fmaf(r[k], __uint_as_float(v[2 * k + 1]), Q1);
     } else {
-      P0 = fmaf(w[k], __uint_as_float(v[2 * k]), P0);
-      Q0 = fmaf(w[k], __uint_as_float(v[2 * k + 1]), Q0);
+      P0 = fmaf(r[k], __uint_as_float(v[2 * k]), P0);
+      Q0 = fmaf(r[k], __uint_as_float(v[2 * k + 1]), Q0);
     }
   }
   const float P = P0 + P1, Q = Q0 + Q1;
+  const float cr = r[W + 1], sr = r[W + 2];
   // Lane re: P = sum Vr ReE, Q = sum Vr ImE; lane im: P = sum Vi ReE, Q = sum Vi ImE.
   // G = (P_r - Q_i) + i (Q_r + P_i), and G (cr + i sr) has
   //   re = (P_r cr - Q_r sr) - (P_i sr + Q_i cr),  im = (P_i cr - Q_i sr) + (P_r sr + Q_r cr):
   // each lane keeps P cr - Q sr and hands P sr + Q cr to its partner (one shuffle).
-  const float keep = fmaf(P, q2.y, -Q * q2.z);
-  const float send = fmaf(P, q2.z, Q * q2.y);
+  const float keep = fmaf(P, cr, -Q * sr);
+  const float send = fmaf(P, sr, Q * cr);
   return fmaf(sgn, __shfl_xor_sync(0xffffffffu, send, 1), keep);
 }
 
@@ -439,18 +481,10 @@ __device__ __noinline__ float grid_wide_sum(const float* rec_dir, uint32_t tbase
   float acc = 0.f;
   for (int tt = 0; tt < 4; ++tt) {
     const float* r = rec_dir + tt * kGrRecDirs * kGrRecWords;
-    const int ct = __float_as_int(r[11]);
+    const int ct = __float_as_int(r[kGrCodeWord]);
     if ((ct & 0xFFFF) == 0xFFFF || ((ct >> 8) & 255) != pp) continue;  // same in every lane
-    uint32_t v[18];
-    const uint32_t a0 = tbase + 2u * static_cast<uint32_t>(ct & 255);
-    asm volatile(
-        "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%18];\n\t"
-        "tcgen05.ld.sync.aligned.32x32b.x2.b32 {%16,%17}, [%19];\n\t"
-        "tcgen05.wait::ld.sync.aligned;"
-        : "=r"(v[0]), "=r"(v[1]), "=r"(v[2]), "=r"(v[3]), "=r"(v[4]), "=r"(v[5]), "=r"(v[6]), "=r"(v[7]), "=r"(v[8]),
-          "=r"(v[9]), "=r"(v[10]), "=r"(v[11]), "=r"(v[12]), "=r"(v[13]), "=r"(v[14]), "=r"(v[15]), "=r"(v[16]),
-          "=r"(v[17])
-        : "r"(a0), "r"(a0 + 16u));
+    uint32_t v[kGrLoadRegs];
+    grid_load_one(tbase + 2u * static_cast<uint32_t>(ct & 255), v);
     const float g = grid_tap_combine<W>(v, r, sgn);
     if (tl == tt) acc += g;
   }
@@ -502,10 +536,12 @@ __device__ __forceinline__ void grid_record(const GridParams& p, const float (&x
   grid_weights<W>(f, st - base == 1, p.wpoly, wt);  // starts differ by at most one without kGrWide
   float cr, sr;
   twiddle_turns(pa + static_cast<uint32_t>(c0) * pb, tab, cr, sr);
+  static_assert(W == 10 && kGrCodeWord == 13 && kGrRecWords == 16, "record layout");
   float4* my = reinterpret_cast<float4*>(dst);
   my[0] = make_float4(wt[0], wt[1], wt[2], wt[3]);
   my[1] = make_float4(wt[4], wt[5], wt[6], wt[7]);
-  my[2] = make_float4(wt[8], cr, sr, __int_as_float(code));
+  my[2] = make_float4(wt[8], wt[9], wt[10], cr);
+  my[3] = make_float4(sr, __int_as_float(code), 0.f, 0.f);
 }
 
 // Sum of TMEM regions into the first one, for this warp's 32 lanes and columns
@@ -906,7 +942,7 @@ __global__ void __launch_bounds__(kGrThreads, 1) rotate_average_gridded(const Gr
                 int live = 0;
 #pragma unroll
                 for (int bb = 0; bb < kGrBatch; ++bb) {
-                  code[bb] = __float_as_int(rb[bb * kGrRecWords + 11]);
+                  code[bb] = __float_as_int(rb[bb * kGrRecWords + kGrCodeWord]);
                   const bool use = code[bb] >= 0 && !(code[bb] & kGrWide) && ((code[bb] >> 8) & 255) == pp;
                   col[bb] = use ? 2u * static_cast<uint32_t>(code[bb] & 255) : 0u;
                   live |= (use ? 1 : 0) << bb;
@@ -915,7 +951,7 @@ __global__ void __launch_bounds__(kGrThreads, 1) rotate_average_gridded(const Gr
 #pragma unroll
                 for (int bp = 0; bp < kGrBatch; bp += 2) {
                   if ((live >> bp) & 3) {
-                    uint32_t v[2][18];
+                    uint32_t v[2][kGrLoadRegs];
                     grid_load_pair(tbase, col[bp], col[bp + 1], v);
 #pragma unroll
                     for (int bb = 0; bb < 2; ++bb) {

@@ -181,3 +181,16 @@ def test_gridded_direction_groups(ctx, shared):
         _check(ctx, obs, dirs)
     finally:
         ctx.set_option(LEAP_OPTION_GRID_SHARED_GROUPS, 0)
+
+
+def test_gridded_long_integration_bright_source(ctx):
+    """47 timesteps x 384 channels of the 128-antenna array with a bright source, 8 of the
+    batched workload's directions: the stencil and accumulation errors of the source's fringe
+    add coherently over the timesteps, while the averages of directions away from the source
+    do not (with 8-point stencils a chunk of this shape reached 2e-5 rad)."""
+    spec = synth.ArraySpec(128, 1500.0)
+    obs = synth.make_observation(spec, timesteps=47, channels=384, freq_start_hz=150e6, freq_inc_hz=40e3,
+                                 noise_sigma=0.5, source_lm=(0.01, -0.005), vis_dtype=np.complex64,
+                                 positions=synth.antenna_positions(spec, 0), seeds=(0, 1, 2))
+    dirs, _ = synth.random_directions(256)
+    _check(ctx, obs, dirs[::32])
