@@ -76,7 +76,7 @@ constexpr int kGrTaps = 10;           // W, grid points per interpolation
 constexpr float kGrBeta = 23.0f;      // 2.3 W
 constexpr int kGrChunk = 16;          // channels per stage
 constexpr int kGrSegChunks = 4;       // chunks per hi*hi accumulation segment (64 channels)
-constexpr int kGrStages = 6;          // {visibility box / A hi, A lo, E window} ring
+constexpr int kGrStages = 8;          // {A hi, A lo, E window} ring (4 stage pairs: 0.5% faster than 3)
 constexpr int kGrMacro = 2;           // chunks handed over per barrier round (stages go in pairs)
 constexpr int kGrMacroStages = kGrStages / kGrMacro;
 constexpr int kGrJwMax = 64;          // grid points per pass (MMA N = 2 Jw <= 128)
