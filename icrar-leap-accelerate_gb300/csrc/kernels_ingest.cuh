@@ -15,6 +15,36 @@
 
 namespace leapgb {
 
+// Integration-layout upload in one pass from a source the device can read (device memory,
+// page-locked host memory, or pageable host memory on hosts whose GPU uses the host page
+// tables): 16-byte vectors, one per lane, so that every load and store instruction of a warp
+// covers 512 contiguous bytes; the V lanes that hold one (row, channel) group of pols agree
+// on its NaN flag by shuffles and zero it together (the NaN rule of the transpose above).
+// n16: 16-byte vectors in all, a multiple of V (V = 1, 2 or 4 vectors per group).
+template <typename S, int V>
+__global__ void __launch_bounds__(256) copy_sanitize_groups(const uint4* __restrict__ src, uint4* __restrict__ dst,
+                                                            int64_t n16) {
+  static_assert(V == 1 || V == 2 || V == 4, "a group is 16, 32 or 64 bytes");
+  const int lane = threadIdx.x & 31;
+  const int64_t warps = static_cast<int64_t>(gridDim.x) * (blockDim.x >> 5);
+  for (int64_t w = (static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x) >> 5; w * 32 < n16; w += warps) {
+    const int64_t i = w * 32 + lane;
+    const bool act = i < n16;  // the same for all V lanes of a group (n16 is a multiple of V)
+    uint4 v = act ? src[i] : make_uint4(0u, 0u, 0u, 0u);
+    bool nan;
+    if (sizeof(S) == 4)
+      nan = isnan(__uint_as_float(v.x)) || isnan(__uint_as_float(v.y)) || isnan(__uint_as_float(v.z)) ||
+            isnan(__uint_as_float(v.w));
+    else
+      nan = isnan(__hiloint2double(static_cast<int>(v.y), static_cast<int>(v.x))) ||
+            isnan(__hiloint2double(static_cast<int>(v.w), static_cast<int>(v.z)));
+#pragma unroll
+    for (int o = 1; o < V; o <<= 1) nan |= __shfl_xor_sync(0xffffffffu, nan, o) != 0;
+    if (nan) v = make_uint4(0u, 0u, 0u, 0u);
+    if (act) dst[i] = v;
+  }
+}
+
 template <typename VisT, int P>
 struct IngestGroup {
   VisT v[P];

@@ -99,8 +99,39 @@ int32_t leap_set_integration(leap_ctx* ctx, int32_t slot, int32_t vis_type, cons
   LEAP_CUDA(in.vis.ensure(vbytes), "alloc vis");
   LEAP_CUDA(in.uvw.ensure(sizeof(double) * 3 * rows), "alloc uvw");
   const cudaMemcpyKind kind = memory == LEAP_MEMORY_HOST ? cudaMemcpyHostToDevice : cudaMemcpyDeviceToDevice;
-  LEAP_CUDA(cudaMemcpyAsync(in.vis.ptr, vis, vbytes, kind, ctx->stream), "copy vis");
   LEAP_CUDA(cudaMemcpyAsync(in.uvw.ptr, uvw, sizeof(double) * 3 * rows, kind, ctx->stream), "copy uvw");
+  // A source the kernels can read (device memory, page-locked host memory, or pageable host
+  // memory read in place through the host page tables) is copied and cleaned in one pass by
+  // 16-byte vectors.  Measured on a Grace host, uploading 52.5 GB from page-locked memory: 201
+  // GB/s, against 182 GB/s for a copy-engine transfer followed by the NaN pass in place, which
+  // is what other sources still take.
+  const void* direct = memory == LEAP_MEMORY_DEVICE ? vis : nullptr;
+  if (!direct) {
+    cudaPointerAttributes at{};
+    if (cudaPointerGetAttributes(&at, vis) == cudaSuccess && at.type == cudaMemoryTypeHost && at.devicePointer)
+      direct = at.devicePointer;
+    else
+      cudaGetLastError();  // pageable memory: not an error
+    if (!direct && ctx->pageable_direct) direct = vis;
+  }
+  const size_t group_bytes = esz * static_cast<size_t>(pols);
+  if (direct && reinterpret_cast<uintptr_t>(direct) % 16 == 0 && group_bytes % 16 == 0) {
+    const int64_t n16 = static_cast<int64_t>(vbytes / 16);
+    const int V = static_cast<int>(group_bytes / 16);
+    const int grid = static_cast<int>(std::min<int64_t>((n16 + 255) / 256, static_cast<int64_t>(ctx->sms) * 8));
+    const uint4* sp = static_cast<const uint4*>(direct);
+    uint4* dp = in.vis.as<uint4>();
+    if (vis_type == LEAP_VIS_C64) {
+      if (V == 1) copy_sanitize_groups<float, 1><<<grid, 256, 0, ctx->stream>>>(sp, dp, n16);
+      else copy_sanitize_groups<float, 2><<<grid, 256, 0, ctx->stream>>>(sp, dp, n16);
+    } else {
+      if (V == 1) copy_sanitize_groups<double, 1><<<grid, 256, 0, ctx->stream>>>(sp, dp, n16);
+      else if (V == 2) copy_sanitize_groups<double, 2><<<grid, 256, 0, ctx->stream>>>(sp, dp, n16);
+      else copy_sanitize_groups<double, 4><<<grid, 256, 0, ctx->stream>>>(sp, dp, n16);
+    }
+    return finish_integration(ctx, in, vis_type, rows, channels, pols);
+  }
+  LEAP_CUDA(cudaMemcpyAsync(in.vis.ptr, vis, vbytes, kind, ctx->stream), "copy vis");
   const int grid = grid_1d(groups, 256);
   if (vis_type == LEAP_VIS_C64) {
     float2* p = in.vis.as<float2>();
