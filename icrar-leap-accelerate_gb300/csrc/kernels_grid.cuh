@@ -77,7 +77,11 @@ constexpr float kGrBeta = 23.0f;      // 2.3 W
 constexpr int kGrChunk = 16;          // channels per stage
 constexpr int kGrSegChunks = 4;       // chunks per hi*hi accumulation segment (64 channels)
 constexpr int kGrStages = 8;          // {A hi, A lo, E window} ring (4 stage pairs: 0.5% faster than 3)
-constexpr int kGrMacro = 2;           // chunks handed over per barrier round (stages go in pairs)
+constexpr int kGrMacro = 4;           // chunks handed over per barrier round: one hi*hi segment
+// One MMA commit per round releases the round's stages to the producer and tells the fold warps
+// that the segment is complete: a commit makes the issuing thread wait for the MMAs before it
+// (measured: 72 MMAs issue in 12.3K cycles without commits, 24.6K with one every 6), so the
+// kernel commits once per segment rather than per stage pair, per segment and per tile.
 constexpr int kGrMacroStages = kGrStages / kGrMacro;
 constexpr int kGrJwMax = 64;          // grid points per pass (MMA N = 2 Jw <= 128)
 constexpr int kGrPassStride = 48;     // grid points between pass windows (multiple of 8)
@@ -107,6 +111,8 @@ constexpr int kGrNumBars = 2 * kGrMacroStages + 8;
 // A pass window must hold every stencil whose start falls in its stride, plus the
 // columns one load reads past the stencil.
 static_assert(kGrPassStride % 8 == 0 && kGrPassStride - 1 + kGrLoadCols <= kGrJwMax, "pass windows");
+static_assert(kGrMacro == kGrSegChunks, "a barrier round is a segment");
+static_assert(kGrStages % kGrMacro == 0 && kGrStages / kGrMacro >= 2, "at least two rounds in flight");
 static_assert(kGrTaps + 1 <= kGrLoadCols, "one load per stencil");
 static_assert(kGrCodeWord < kGrRecWords, "record layout");
 
@@ -660,10 +666,8 @@ __global__ void __launch_bounds__(kGrThreads, 1) rotate_average_gridded(const Gr
   uint64_t* bars = reinterpret_cast<uint64_t*>(rec_all + kGrRecBytes / 4);
   uint64_t* vfull = bars;                      // [kGrMacroStages] bytes of a stage pair landed
   uint64_t* sdone = vfull + kGrMacroStages;    // [kGrMacroStages] MMAs that read it completed
-  uint64_t* is_full = sdone + kGrMacroStages;  // a middle segment is complete in IS
-  uint64_t* is_empty = is_full + 1;            // ... and was folded into RS
-  uint64_t* blk_full = is_empty + 1;           // every MMA of a tile completed
-  uint64_t* ac_free = blk_full + 1;            // final fold of a tile done: IS and AC reusable
+  uint64_t* is_empty = sdone + kGrMacroStages;  // a middle segment was folded into RS (sdone: its MMAs completed)
+  uint64_t* ac_free = is_empty + 1;             // final fold of a tile done: IS and AC reusable
   uint64_t* rs_full = ac_free + 1;             // [2] running sum final: epilogue may read
   uint64_t* rs_free = rs_full + 2;             // [2] epilogue finished reading
   uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(bars + kGrNumBars);
@@ -681,9 +685,7 @@ __global__ void __launch_bounds__(kGrThreads, 1) rotate_average_gridded(const Gr
       mbar_init(&vfull[i], 1);
       mbar_init(&sdone[i], 1);
     }
-    mbar_init(is_full, 1);
     mbar_init(is_empty, 4);
-    mbar_init(blk_full, 1);
     mbar_init(ac_free, 4);
     for (int i = 0; i < 2; ++i) {
       mbar_init(&rs_full[i], 4);
@@ -792,14 +794,10 @@ __global__ void __launch_bounds__(kGrThreads, 1) rotate_average_gridded(const Gr
                 const uint32_t dst = seg == 0 ? rs : tmem + kGrIS;
                 grid_mma_hihi(dst, ah, bh, idesc, qs > 0 ? 1u : 0u);
                 issued = true;
-                if (seg >= 1 && qs == kGrSegChunks - 1 && q != I.nchunk - 1) {
-                  tc_commit(is_full);  // a middle segment, folded by the converters
-                  ++mids;
-                }
+                if (seg >= 1 && qs == kGrSegChunks - 1 && q != I.nchunk - 1) ++mids;  // a middle segment, folded
               }
               if (issued) tc_commit(&sdone[m]);
             }
-            if (ok) tc_commit(blk_full);
           }
       }
       // No MMA of this block may be in flight when its TMEM is freed.
@@ -811,7 +809,7 @@ __global__ void __launch_bounds__(kGrThreads, 1) rotate_average_gridded(const Gr
   } else if (warp < 6) {
     // ---------------- fold warps: segments and corrections into the running sums ----------------
     const uint32_t lanes = static_cast<uint32_t>((warp & 3) * 32) << 16;
-    uint32_t blk = 0, mids = 0;
+    uint32_t blk = 0, rnd = 0;  // tiles (x passes) and barrier rounds (segments), as the MMA issuer counts them
     bool ok = true;
     for (int sl = blockIdx.x; ok; sl += gridDim.x) {
       const int u = sl < p.nslots ? __ldg(p.order + sl) : -1;
@@ -821,12 +819,14 @@ __global__ void __launch_bounds__(kGrThreads, 1) rotate_average_gridded(const Gr
       const GridWindow w = p.win[u];
       const int nseg = (I.nchunk + kGrSegChunks - 1) / kGrSegChunks;
       for (int tb = 0; tb < g.ntb && ok; ++tb)
-        for (int ps = 0; ps < w.npass && ok; ++ps, ++blk) {
+        for (int ps = 0; ps < w.npass && ok; ++ps, ++blk, rnd += nseg) {
           const uint32_t b = blk & 1;
-          // Middle segments 1 .. nseg - 2 complete in IS one after another: each is added to RS
-          // as soon as its MMAs have completed, so that the next segment can restart IS.
+          // Middle segments 1 .. nseg - 2 complete in IS one after another (round rnd + sg of the
+          // stage ring): each is added to RS as soon as its MMAs have completed, so that the next
+          // segment can restart IS.  (Segment 0 accumulates in RS itself.)
           for (int sg = 1; sg <= nseg - 2; ++sg) {
-            if (!grid_wait(is_full, mids & 1, abort_flag)) {
+            const uint32_t r = rnd + sg;
+            if (!grid_wait(&sdone[r % kGrMacroStages], (r / kGrMacroStages) & 1, abort_flag)) {
               grid_fail(p, abort_flag);
               ok = false;
               break;
@@ -836,12 +836,12 @@ __global__ void __launch_bounds__(kGrThreads, 1) rotate_average_gridded(const Gr
             asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
             __syncwarp();
             if (lane == 0) mbar_arrive(is_empty);
-            ++mids;
           }
           if (!ok) break;
           // Final fold: RS += last segment (if any beyond the first) + corrections.
+          const uint32_t rl = rnd + nseg - 1;  // the tile's last round: every MMA of the tile completed
           if ((blk >= 2 && !grid_wait(&rs_free[b], ((blk >> 1) - 1) & 1, abort_flag)) ||
-              !grid_wait(blk_full, blk & 1, abort_flag)) {
+              !grid_wait(&sdone[rl % kGrMacroStages], (rl / kGrMacroStages) & 1, abort_flag)) {
             grid_fail(p, abort_flag);
             ok = false;
             break;
