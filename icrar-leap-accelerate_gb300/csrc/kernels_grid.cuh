@@ -60,8 +60,8 @@
 // window), 1 = MMA issuer (+ TMEM owner), 2-5 = fold warps (add the finished hi*hi
 // segments and the corrections into the running sums), 6-13 = epilogue (warp w reads
 // TMEM lanes 32 (w % 4) ..; two warps per quarter take 32 directions each).  One ring of
-// kGrStages stages of {A hi, A lo, E window}, handed over in pairs and released by one
-// MMA commit per pair.  Every wait is bounded; a timeout sets the error word, stops every
+// kGrStages stages of {A hi, A lo, E window}, handed over in rounds of kGrMacro (one 64-channel
+// segment) and released by one MMA commit per round.  Every wait is bounded; a timeout sets the error word, stops every
 // role, and the block still waits (bounded) for its copies and MMAs and frees its TMEM.
 #pragma once
 
@@ -76,7 +76,7 @@ constexpr int kGrTaps = 10;           // W, grid points per interpolation
 constexpr float kGrBeta = 23.0f;      // 2.3 W
 constexpr int kGrChunk = 16;          // channels per stage
 constexpr int kGrSegChunks = 4;       // chunks per hi*hi accumulation segment (64 channels)
-constexpr int kGrStages = 8;          // {A hi, A lo, E window} ring (4 stage pairs: 0.5% faster than 3)
+constexpr int kGrStages = 8;          // {A hi, A lo, E window} ring: two rounds in flight
 constexpr int kGrMacro = 4;           // chunks handed over per barrier round: one hi*hi segment
 // One MMA commit per round releases the round's stages to the producer and tells the fold warps
 // that the segment is complete: a commit makes the issuing thread wait for the MMAs before it
@@ -664,7 +664,7 @@ __global__ void __launch_bounds__(kGrThreads, 1) rotate_average_gridded(const Gr
   float2* tab = reinterpret_cast<float2*>(smem + kGrStages * kGrStageBytes);
   float* rec_all = reinterpret_cast<float*>(tab + kTwiddleSize);
   uint64_t* bars = reinterpret_cast<uint64_t*>(rec_all + kGrRecBytes / 4);
-  uint64_t* vfull = bars;                      // [kGrMacroStages] bytes of a stage pair landed
+  uint64_t* vfull = bars;                      // [kGrMacroStages] bytes of a round's stages landed
   uint64_t* sdone = vfull + kGrMacroStages;    // [kGrMacroStages] MMAs that read it completed
   uint64_t* is_empty = sdone + kGrMacroStages;  // a middle segment was folded into RS (sdone: its MMAs completed)
   uint64_t* ac_free = is_empty + 1;             // final fold of a tile done: IS and AC reusable
