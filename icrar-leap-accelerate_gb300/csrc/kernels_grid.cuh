@@ -61,7 +61,9 @@
 // segments and the corrections into the running sums), 6-13 = epilogue (warp w reads
 // TMEM lanes 32 (w % 4) ..; two warps per quarter take 32 directions each).  One ring of
 // kGrStages stages of {A hi, A lo, E window}, handed over in rounds of kGrMacro (one 64-channel
-// segment) and released by one MMA commit per round.  Every wait is bounded; a timeout sets the error word, stops every
+// segment) and released by one MMA commit per round.  A round issues its 8 correction MMAs
+// before its 4 hi*hi MMAs, so the fold that frees IS overlaps the corrections (a round's
+// stages all land before it starts).  Every wait is bounded; a timeout sets the error word, stops every
 // role, and the block still waits (bounded) for its copies and MMAs and frees its TMEM.
 #pragma once
 
@@ -776,25 +778,27 @@ __global__ void __launch_bounds__(kGrThreads, 1) rotate_average_gridded(const Gr
                 break;
               }
               asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+              // A round is one segment.  Its correction MMAs go first: they give the fold of the
+              // previous segment time to finish before the hi*hi MMAs restart IS.
+              const int seg = q0 / kGrSegChunks;
+              // Descriptors of stage i: A hi/lo at +0 / +kGrAHalf, E hi/lo at +0 / +2*jw*32 from their
+              // bases (address field >> 4).
+              const uint64_t so0 = static_cast<uint64_t>(m * kGrMacro * (kGrStageBytes >> 4));
+              const uint64_t sst = static_cast<uint64_t>(kGrStageBytes >> 4);
               for (int i = 0; i < nq; ++i) {
-                const int q = q0 + i;
-                const int seg = q / kGrSegChunks, qs = q % kGrSegChunks;
-                // Descriptors of this stage: A hi/lo at +0 / +kGrAHalf, E hi/lo at +0 / +2*jw*32 from
-                // their bases (address field >> 4).
-                const uint64_t so = static_cast<uint64_t>((m * kGrMacro + i) * (kGrStageBytes >> 4));
-                const uint64_t ah = adesc0 + so, bh = edesc0 + so;
+                const uint64_t ah = adesc0 + so0 + i * sst, bh = edesc0 + so0 + i * sst;
                 const uint64_t al = ah + (kGrAHalf >> 4), bl = bh + static_cast<uint64_t>(2 * w.jw * 2);
-                // Corrections first: they give the fold of the previous segment time to finish.
-                grid_mma_corrections(tmem + kGrAC, ah, al, bh, bl, idesc, q > 0 ? 1u : 0u);
-                if (seg >= 2 && qs == 0 && !grid_wait(is_empty, (mids - 1) & 1, abort_flag)) {
-                  grid_fail(p, abort_flag);
-                  ok = false;
-                  break;
-                }
+                grid_mma_corrections(tmem + kGrAC, ah, al, bh, bl, idesc, q0 + i > 0 ? 1u : 0u);
+              }
+              issued = true;
+              if (seg >= 2 && !grid_wait(is_empty, (mids - 1) & 1, abort_flag)) {
+                grid_fail(p, abort_flag);
+                ok = false;
+              } else {
                 const uint32_t dst = seg == 0 ? rs : tmem + kGrIS;
-                grid_mma_hihi(dst, ah, bh, idesc, qs > 0 ? 1u : 0u);
-                issued = true;
-                if (seg >= 1 && qs == kGrSegChunks - 1 && q != I.nchunk - 1) ++mids;  // a middle segment, folded
+                for (int i = 0; i < nq; ++i)
+                  grid_mma_hihi(dst, adesc0 + so0 + i * sst, edesc0 + so0 + i * sst, idesc, i > 0 ? 1u : 0u);
+                if (seg >= 1 && q0 + nq < I.nchunk) ++mids;  // a middle segment, folded
               }
               if (issued) tc_commit(&sdone[m]);
             }
