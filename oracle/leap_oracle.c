@@ -2,8 +2,8 @@
  * ORACLE — test infrastructure only.
  *
  * A plain-C, all-FP64 restatement of the LEAP-Accelerate CPU calibration
- * path (the reference's Eigen implementation).  It is the checker for the
- * GPU product: only the tests, the smoke check and the benchmark's CPU
+ * path (the reference's Eigen implementation).  The GPU product's results are
+ * compared against it: only the tests, the smoke check and the benchmark's CPU
  * baseline leg may load it, and never as the thing measured or shipped.
  *
  * Each function cites the reference file:line it follows (paths relative to

@@ -1,7 +1,7 @@
 """ORACLE — test infrastructure only.
 
-Float64 restatement of LEAP-Accelerate's CPU calibration path, used as the
-checker for the GPU product.  Only the tests, ``__graft_entry__.smoke()`` and
+Float64 restatement of LEAP-Accelerate's CPU calibration path, against which
+the GPU product's results are compared.  Only the tests, ``__graft_entry__.smoke()`` and
 the CPU-baseline leg of ``bench.py`` may import this module, and only to check
 or to time the reference algorithm on the host; nothing shipped calls it.
 
