@@ -61,6 +61,7 @@ def _check(ctx, obs, dirs, avg_tol=AVG_TOL):
     (12, 20, 48, 70),   # two direction groups, several timestep slabs
     (128, 2, 96, 64),   # one full direction group
     (40, 7, 70, 9),
+    (24, 6, 200, 36),   # 13 chunks: three full 64-channel segments (middle folds), a last one of one chunk
 ])
 def test_gridded_matches_oracle(ctx, stations, timesteps, channels, ndir):
     obs, dirs = synth.small_case(stations=stations, timesteps=timesteps, channels=channels, directions=ndir,
